@@ -1,0 +1,360 @@
+"""grudon_gb300: GB300-native per-round graph operator of Grudon.
+
+Python mirror of the C ABI (include/grudon_gpu.h).  The compute path is the
+in-tree CUDA library libgrudon_gpu.so; importing works without a GPU (the
+host graph tools run on the CPU), but every device call raises GrdError when
+no CUDA device is present — there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import (GRD_CC, GRD_DIR_AUTO, GRD_DIR_PULL, GRD_DIR_PUSH, GRD_FMT_AUTO, GRD_FMT_BITVEC,
+                   GRD_FMT_LIST, GRD_PR_DELTA, GRD_PR_PULL, GRD_RUN_STRICT, GRD_SSSP_HOP, GRD_SSSP_W)
+
+__all__ = [
+    "GrdError", "Graph", "Context", "lib", "device_count", "rmat_seed",
+    "GRD_PR_DELTA", "GRD_PR_PULL", "GRD_CC", "GRD_SSSP_HOP", "GRD_SSSP_W",
+    "GRD_DIR_AUTO", "GRD_DIR_PUSH", "GRD_DIR_PULL", "GRD_FMT_AUTO", "GRD_FMT_BITVEC", "GRD_FMT_LIST",
+    "GRD_RUN_STRICT", "ALGO_NAMES",
+]
+
+ALGO_NAMES = {"pr": GRD_PR_DELTA, "pr_delta": GRD_PR_DELTA, "pr_pull": GRD_PR_PULL, "cc": GRD_CC,
+              "sssp": GRD_SSSP_HOP, "sssp_hop": GRD_SSSP_HOP, "sssp_w": GRD_SSSP_W}
+
+
+class GrdError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ffi.ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    return _ffi.load()
+
+
+def device_count() -> int:
+    return int(lib().grd_device_count())
+
+
+def rmat_seed(scale: int, edge_factor: int) -> int:
+    return int(lib().grd_rmat_seed(scale, edge_factor))
+
+
+def _u32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+class Graph:
+    """Host CSR owned by the library (generators / readers) or copied in."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    # -- constructors --------------------------------------------------------
+    @staticmethod
+    def _make(fn, *args) -> "Graph":
+        out = C.POINTER(_ffi.grd_host_graph)()
+        rc = fn(*args, C.byref(out))
+        if rc != 0:
+            raise GrdError(rc, f"{fn.__name__} failed")
+        return Graph(out)
+
+    @classmethod
+    def rmat(cls, scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: Optional[int] = None, symmetrize: bool = False, weighted: bool = False,
+             threads: int = 0) -> "Graph":
+        if seed is None:
+            seed = rmat_seed(scale, edge_factor)
+        return cls._make(lib().grd_gen_rmat, scale, edge_factor, a, b, c, seed, int(symmetrize),
+                         int(weighted), threads)
+
+    @classmethod
+    def er(cls, num_vertices: int, edge_factor: int, seed: int, symmetrize: bool = False,
+           weighted: bool = False, threads: int = 0) -> "Graph":
+        return cls._make(lib().grd_gen_er, num_vertices, edge_factor, seed, int(symmetrize), int(weighted),
+                         threads)
+
+    @classmethod
+    def grid(cls, k: int, seed: int = 1, weighted: bool = True, threads: int = 0) -> "Graph":
+        return cls._make(lib().grd_gen_grid, k, seed, int(weighted), threads)
+
+    @classmethod
+    def from_csr(cls, row_offsets, col_indices, weights=None) -> "Graph":
+        ro = np.ascontiguousarray(row_offsets, dtype=np.uint64)
+        ci = _u32(col_indices)
+        w = None if weights is None else _u32(weights)
+        csr = _ffi.grd_csr(len(ro) - 1, len(ci), ro.ctypes.data_as(_ffi.u64p), ci.ctypes.data_as(_ffi.u32p),
+                           w.ctypes.data_as(_ffi.u32p) if w is not None else None)
+        return cls._make(lib().grd_graph_from_csr, C.byref(csr))
+
+    @classmethod
+    def from_edges(cls, num_vertices: int, src, dst, weights=None) -> "Graph":
+        """Edges in any order; rows are sorted by destination (stable for weights)."""
+        src = np.asarray(src, dtype=np.int64)
+        dst = np.asarray(dst, dtype=np.int64)
+        order = np.lexsort((dst, src))
+        ro = np.zeros(num_vertices + 1, dtype=np.uint64)
+        np.add.at(ro, src + 1, 1)
+        ro = np.cumsum(ro).astype(np.uint64)
+        w = None if weights is None else np.asarray(weights)[order]
+        return cls.from_csr(ro, dst[order], w)
+
+    @classmethod
+    def read_gr(cls, path: str) -> "Graph":
+        return cls._make(lib().grd_read_gr, path.encode())
+
+    @classmethod
+    def read_mtx(cls, path: str) -> "Graph":
+        return cls._make(lib().grd_read_mtx, path.encode())
+
+    # -- accessors -------------------------------------------------------------
+    @property
+    def num_vertices(self) -> int:
+        return int(self._h.contents.num_vertices)
+
+    @property
+    def num_edges(self) -> int:
+        return int(self._h.contents.num_edges)
+
+    @property
+    def seed(self) -> int:
+        return int(self._h.contents.seed)
+
+    @property
+    def row_offsets(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self._h.contents.row_offsets, shape=(self.num_vertices + 1,))
+
+    @property
+    def col_indices(self) -> np.ndarray:
+        if self.num_edges == 0:
+            return np.zeros(0, dtype=np.uint32)
+        return np.ctypeslib.as_array(self._h.contents.col_indices, shape=(self.num_edges,))
+
+    @property
+    def weights(self) -> Optional[np.ndarray]:
+        if not self._h.contents.weights:
+            return None
+        if self.num_edges == 0:
+            return np.zeros(0, dtype=np.uint32)
+        return np.ctypeslib.as_array(self._h.contents.weights, shape=(self.num_edges,))
+
+    def csr_struct(self) -> _ffi.grd_csr:
+        h = self._h.contents
+        return _ffi.grd_csr(h.num_vertices, h.num_edges, h.row_offsets, h.col_indices, h.weights)
+
+    def out_degrees(self) -> np.ndarray:
+        return np.diff(self.row_offsets).astype(np.uint32)
+
+    def write_gr(self, path: str) -> None:
+        rc = lib().grd_write_gr(self._h, path.encode())
+        if rc != 0:
+            raise GrdError(rc, f"cannot write {path}")
+
+    def write_mtx(self, path: str) -> None:
+        rc = lib().grd_write_mtx(self._h, path.encode())
+        if rc != 0:
+            raise GrdError(rc, f"cannot write {path}")
+
+    def partition_edge_balanced(self, num_memory: int) -> np.ndarray:
+        part = np.zeros(self.num_vertices, dtype=np.uint32)
+        rc = lib().grd_partition_edge_balanced(self._h, num_memory, part.ctypes.data_as(_ffi.u32p))
+        if rc != 0:
+            raise GrdError(rc, "partitioning failed")
+        return part
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                lib().grd_graph_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+def layout_preview(graph: Graph, mirror_part, num_memory: int, part: int):
+    """Slot -> gid order of one memory partition, built on the host (no GPU)."""
+    mp = None if mirror_part is None else _u32(mirror_part)
+    cap = 2 * graph.num_vertices + 1
+    out = np.zeros(cap, dtype=np.uint32)
+    no, npx = C.c_uint32(), C.c_uint32()
+    csr = graph.csr_struct()
+    rc = lib().grd_layout_preview(C.byref(csr), None if mp is None else mp.ctypes.data_as(_ffi.u32p), num_memory,
+                                  part, out.ctypes.data_as(C.c_void_p), cap, C.byref(no), C.byref(npx))
+    if rc != 0:
+        raise GrdError(rc, lib().grd_create_error().decode())
+    return out[: no.value + npx.value].copy(), int(no.value)
+
+
+def write_partition_file(part, path: str) -> None:
+    p = _u32(part)
+    rc = lib().grd_write_partition_file(p.ctypes.data_as(_ffi.u32p), len(p), path.encode())
+    if rc != 0:
+        raise GrdError(rc, f"cannot write {path}")
+
+
+def read_partition_file(path: str, n: int, num_memory: int) -> np.ndarray:
+    p = np.zeros(n, dtype=np.uint32)
+    rc = lib().grd_read_partition_file(path.encode(), n, num_memory, p.ctypes.data_as(_ffi.u32p))
+    if rc != 0:
+        raise GrdError(rc, f"cannot read partition file {path}")
+    return p
+
+
+class Context:
+    """One partitioned graph resident on one GPU (grd_ctx)."""
+
+    def __init__(self, graph: Graph, mirror_part=None, num_memory: int = 1, device: int = 0):
+        self._lib = lib()
+        self._ctx = C.c_void_p()
+        self._graph = graph  # keeps host arrays alive for the create call
+        self.num_vertices = graph.num_vertices
+        mp = None
+        if mirror_part is not None:
+            self._mp = _u32(mirror_part)
+            if len(self._mp) != graph.num_vertices:
+                raise ValueError("mirror_part must have one entry per vertex")
+            mp = self._mp.ctypes.data_as(_ffi.u32p)
+        csr = graph.csr_struct()
+        rc = self._lib.grd_ctx_create(C.byref(csr), mp, 1, num_memory, device, C.byref(self._ctx))
+        if rc != 0:
+            raise GrdError(rc, self._lib.grd_create_error().decode())
+        self.algo = None
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            raise GrdError(rc, self._lib.grd_last_error(self._ctx).decode())
+
+    def set_algo(self, algo, source: int = 0, max_rounds: int = 1000, damping: float = 0.85,
+                 tolerance: Optional[float] = None, direction: int = GRD_DIR_AUTO,
+                 frontier_format: int = GRD_FMT_AUTO) -> None:
+        if isinstance(algo, str):
+            algo = ALGO_NAMES[algo]
+        if tolerance is None:
+            tolerance = 1e-7 if algo == GRD_PR_PULL else 1e-6
+        p = _ffi.grd_params(source, max_rounds, damping, tolerance, direction, frontier_format)
+        self._check(self._lib.grd_set_algo(self._ctx, algo, C.byref(p)))
+        self.algo = algo
+
+    def init(self) -> None:
+        self._check(self._lib.grd_init(self._ctx))
+
+    def sync_fwd(self) -> None:
+        self._check(self._lib.grd_sync_fwd(self._ctx))
+
+    def edge_map(self) -> None:
+        self._check(self._lib.grd_edge_map(self._ctx))
+
+    def sync_bwd(self) -> None:
+        self._check(self._lib.grd_sync_bwd(self._ctx))
+
+    def aggregate(self) -> None:
+        self._check(self._lib.grd_aggregate(self._ctx))
+
+    def update(self) -> int:
+        f = C.c_uint64()
+        self._check(self._lib.grd_update(self._ctx, C.byref(f)))
+        return int(f.value)
+
+    def round(self) -> int:
+        """One round through the per-stage API; returns |frontier|."""
+        self.sync_fwd()
+        self.edge_map()
+        self.sync_bwd()
+        self.aggregate()
+        return self.update()
+
+    @staticmethod
+    def _stats_dict(s) -> dict:
+        out = {}
+        for f, _ in _ffi.grd_stats._fields_:
+            v = getattr(s, f)
+            out[f] = list(v) if isinstance(v, C.Array) else v
+        return out
+
+    def run(self, strict: bool = False) -> dict:
+        s = _ffi.grd_stats()
+        self._check(self._lib.grd_run(self._ctx, GRD_RUN_STRICT if strict else 0, C.byref(s)))
+        return self._stats_dict(s)
+
+    def stats(self) -> dict:
+        s = _ffi.grd_stats()
+        self._check(self._lib.grd_get_stats(self._ctx, C.byref(s)))
+        return self._stats_dict(s)
+
+    def set_profiling(self, enable: bool = True) -> None:
+        self._check(self._lib.grd_set_profiling(self._ctx, int(enable)))
+
+    def upload(self) -> int:
+        b = C.c_uint64()
+        self._check(self._lib.grd_upload(self._ctx, C.byref(b)))
+        return int(b.value)
+
+    def _read(self, fn, dtype, n):
+        out = np.empty(n, dtype=dtype)
+        self._check(fn(self._ctx, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+    def read_props(self) -> np.ndarray:
+        dt = np.float32 if self.algo in (GRD_PR_DELTA, GRD_PR_PULL) else np.uint32
+        return self._read(self._lib.grd_read_props, dt, self.num_vertices)
+
+    def read_ranks(self) -> np.ndarray:
+        out = np.empty(self.num_vertices, dtype=np.float32)
+        self._check(self._lib.grd_read_ranks(self._ctx, out.ctypes.data_as(C.c_void_p), out.size))
+        return out
+
+    def read_updates(self) -> np.ndarray:
+        dt = np.float32 if self.algo in (GRD_PR_DELTA, GRD_PR_PULL) else np.uint32
+        return self._read(self._lib.grd_read_updates, dt, self.num_vertices)
+
+    def read_frontier(self) -> np.ndarray:
+        words = (self.num_vertices + 31) // 32
+        out = np.empty(words, dtype=np.uint32)
+        self._check(self._lib.grd_read_frontier(self._ctx, out.ctypes.data_as(C.c_void_p), words))
+        bits = np.unpackbits(out.view(np.uint8), bitorder="little")[: self.num_vertices]
+        return bits.astype(bool)
+
+    def layout_info(self, part: int) -> tuple:
+        no, npx, ne = C.c_uint32(), C.c_uint32(), C.c_uint64()
+        self._check(self._lib.grd_layout_info(self._ctx, part, C.byref(no), C.byref(npx), C.byref(ne)))
+        return int(no.value), int(npx.value), int(ne.value)
+
+    def layout_slots(self, part: int) -> np.ndarray:
+        no, npx, _ = self.layout_info(part)
+        out = np.empty(no + npx, dtype=np.uint32)
+        self._check(self._lib.grd_layout_slots(self._ctx, part, out.ctypes.data_as(C.c_void_p), out.size))
+        return out
+
+    def device_props_ptr(self) -> int:
+        p = C.c_void_p()
+        self._check(self._lib.grd_device_props(self._ctx, C.byref(p)))
+        return int(p.value or 0)
+
+    def stream(self) -> int:
+        return int(self._lib.grd_stream(self._ctx) or 0)
+
+    def synchronize(self) -> None:
+        self._check(self._lib.grd_synchronize(self._ctx))
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            self._lib.grd_ctx_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,127 @@
+"""ctypes declarations of include/grudon_gpu.h (the C ABI)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libgrudon_gpu.so"
+
+GRD_OK = 0
+GRD_E_INVALID = -1
+GRD_E_OOM = -2
+GRD_E_CUDA = -3
+GRD_E_TIMEOUT = -4
+GRD_E_ROUND_CAP = -5
+GRD_E_IO = -6
+
+GRD_PR_DELTA = 0
+GRD_PR_PULL = 1
+GRD_CC = 2
+GRD_SSSP_HOP = 3
+GRD_SSSP_W = 4
+
+GRD_DIR_AUTO, GRD_DIR_PUSH, GRD_DIR_PULL = 0, 1, 2
+GRD_FMT_AUTO, GRD_FMT_BITVEC, GRD_FMT_LIST = 0, 1, 2
+GRD_RUN_STRICT = 1
+
+ERROR_NAMES = {
+    GRD_E_INVALID: "GRD_E_INVALID", GRD_E_OOM: "GRD_E_OOM", GRD_E_CUDA: "GRD_E_CUDA",
+    GRD_E_TIMEOUT: "GRD_E_TIMEOUT", GRD_E_ROUND_CAP: "GRD_E_ROUND_CAP", GRD_E_IO: "GRD_E_IO",
+}
+
+u8p = C.POINTER(C.c_uint8)
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+
+
+class grd_csr(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("num_edges", C.c_uint64),
+                ("row_offsets", u64p), ("col_indices", u32p), ("weights", u32p)]
+
+
+class grd_params(C.Structure):
+    _fields_ = [("source", C.c_uint32), ("max_rounds", C.c_uint32), ("damping", C.c_double),
+                ("tolerance", C.c_double), ("direction", C.c_int), ("frontier_format", C.c_int)]
+
+
+class grd_stats(C.Structure):
+    _fields_ = [("rounds", C.c_uint32), ("converged", C.c_uint32), ("edges_scanned", C.c_uint64),
+                ("bytes_synced", C.c_uint64), ("reference_bytes_moved", C.c_uint64),
+                ("last_residual", C.c_double), ("push_rounds", C.c_uint32), ("pull_rounds", C.c_uint32),
+                ("actives_total", C.c_uint64), ("kernel_launches", C.c_uint64), ("stage_ms", C.c_double * 5)]
+
+
+class grd_host_graph(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("num_edges", C.c_uint64), ("row_offsets", u64p),
+                ("col_indices", u32p), ("weights", u32p), ("seed", C.c_uint64)]
+
+
+# name -> (restype, argtypes); every symbol here is declared in include/grudon_gpu.h
+SIGNATURES = {
+    "grd_version": (C.c_char_p, []),
+    "grd_device_count": (C.c_int, []),
+    "grd_ctx_create": (C.c_int, [C.POINTER(grd_csr), u32p, C.c_uint32, C.c_uint32, C.c_int, C.POINTER(C.c_void_p)]),
+    "grd_ctx_destroy": (None, [C.c_void_p]),
+    "grd_last_error": (C.c_char_p, [C.c_void_p]),
+    "grd_create_error": (C.c_char_p, []),
+    "grd_upload": (C.c_int, [C.c_void_p, u64p]),
+    "grd_set_algo": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(grd_params)]),
+    "grd_init": (C.c_int, [C.c_void_p]),
+    "grd_sync_fwd": (C.c_int, [C.c_void_p]),
+    "grd_edge_map": (C.c_int, [C.c_void_p]),
+    "grd_sync_bwd": (C.c_int, [C.c_void_p]),
+    "grd_aggregate": (C.c_int, [C.c_void_p]),
+    "grd_update": (C.c_int, [C.c_void_p, u64p]),
+    "grd_run": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(grd_stats)]),
+    "grd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(grd_stats)]),
+    "grd_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "grd_read_props": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "grd_read_ranks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "grd_read_updates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "grd_read_frontier": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "grd_layout_info": (C.c_int, [C.c_void_p, C.c_uint32, u32p, u32p, u64p]),
+    "grd_layout_slots": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t]),
+    "grd_layout_preview": (C.c_int, [C.POINTER(grd_csr), u32p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_size_t,
+                                     u32p, u32p]),
+    "grd_device_props": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "grd_device_ranks": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "grd_stream": (C.c_void_p, [C.c_void_p]),
+    "grd_synchronize": (C.c_int, [C.c_void_p]),
+    "grd_gen_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                               C.c_int, C.c_int, C.c_int, C.POINTER(C.POINTER(grd_host_graph))]),
+    "grd_gen_er": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_int, C.c_int, C.c_int,
+                             C.POINTER(C.POINTER(grd_host_graph))]),
+    "grd_gen_grid": (C.c_int, [C.c_uint32, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.POINTER(grd_host_graph))]),
+    "grd_graph_from_csr": (C.c_int, [C.POINTER(grd_csr), C.POINTER(C.POINTER(grd_host_graph))]),
+    "grd_graph_free": (None, [C.POINTER(grd_host_graph)]),
+    "grd_rmat_seed": (C.c_uint64, [C.c_uint32, C.c_uint32]),
+    "grd_write_gr": (C.c_int, [C.POINTER(grd_host_graph), C.c_char_p]),
+    "grd_read_gr": (C.c_int, [C.c_char_p, C.POINTER(C.POINTER(grd_host_graph))]),
+    "grd_write_mtx": (C.c_int, [C.POINTER(grd_host_graph), C.c_char_p]),
+    "grd_read_mtx": (C.c_int, [C.c_char_p, C.POINTER(C.POINTER(grd_host_graph))]),
+    "grd_partition_edge_balanced": (C.c_int, [C.POINTER(grd_host_graph), C.c_uint32, u32p]),
+    "grd_write_partition_file": (C.c_int, [u32p, C.c_uint32, C.c_char_p]),
+    "grd_read_partition_file": (C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, u32p]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the in-tree CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the CUDA extension is required; there is no CPU fallback)")
+    lib = C.CDLL(os.fspath(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib

@@ -1,0 +1,653 @@
+// C ABI of the per-round graph operator: context lifetime, layout upload and
+// the round stages.  See include/grudon_gpu.h for the contract and the
+// reference interface each entry point replaces.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/grudon_gpu.h"
+#include "ctx.hpp"
+#include "kernels.cuh"
+
+using namespace grd;
+
+static thread_local std::string g_create_error;
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                   \
+      return GRD_E_CUDA;                                                               \
+    }                                                                                  \
+  } while (0)
+
+#define CK_LAUNCH()                                                                    \
+  do {                                                                                 \
+    cudaError_t e_ = cudaGetLastError();                                               \
+    if (e_ != cudaSuccess) {                                                           \
+      ctx->err = std::string("kernel launch: ") + cudaGetErrorString(e_);              \
+      return GRD_E_CUDA;                                                               \
+    }                                                                                  \
+  } while (0)
+
+namespace {
+
+template <class T>
+int dev_alloc(grd_ctx* ctx, T** p, size_t count) {
+  size_t bytes = sizeof(T) * std::max<size_t>(count, 1);
+  void* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, bytes);
+  if (e != cudaSuccess) {
+    ctx->err = "cudaMalloc(" + std::to_string(bytes) + " B): " + cudaGetErrorString(e);
+    (void)cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? GRD_E_OOM : GRD_E_CUDA;
+  }
+  ctx->allocs.push_back(d);
+  *p = static_cast<T*>(d);
+  return GRD_OK;
+}
+
+template <class T>
+int upload(grd_ctx* ctx, T* dst, const std::vector<T>& src) {
+  if (src.empty()) return GRD_OK;
+  CK(cudaMemcpyAsync(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, ctx->stream));
+  ctx->upload_bytes += sizeof(T) * src.size();
+  return GRD_OK;
+}
+
+#define TRY(x)                 \
+  do {                         \
+    int r_ = (x);              \
+    if (r_ != GRD_OK) return r_; \
+  } while (0)
+
+int alloc_and_upload(grd_ctx* ctx) {
+  const Layout& L = ctx->L;
+  DevGraph& g = ctx->g;
+  DevState& st = ctx->st;
+  g.V = L.V;
+  g.M = L.M;
+  g.S = L.S;
+  g.num_tiles = (uint32_t)L.num_tiles();
+  g.num_hubs = (uint32_t)L.hubs.size();
+  const size_t V = L.V, S = L.S, E = L.E, M = L.M, T = L.num_tiles();
+  const size_t VW = (V + 31) / 32, SW = S / 32;
+  TRY(dev_alloc(ctx, (uint32_t**)&g.slot_gid, S));
+  TRY(dev_alloc(ctx, (uint32_t**)&g.row_off, S + 1));
+  TRY(dev_alloc(ctx, (uint32_t**)&g.col, std::max<size_t>(E, 4)));
+  if (L.weighted) TRY(dev_alloc(ctx, (uint32_t**)&g.wgt, std::max<size_t>(E, 4)));
+  TRY(dev_alloc(ctx, (uint32_t**)&g.outdeg, V));
+  TRY(dev_alloc(ctx, (HubChunkD**)&g.hubs, L.hubs.size()));
+  TRY(dev_alloc(ctx, (uint32_t**)&g.tile_part, T));
+  TRY(dev_alloc(ctx, (uint32_t**)&g.part_base, M));
+  TRY(dev_alloc(ctx, (uint32_t**)&g.part_T, M));
+  TRY(dev_alloc(ctx, (uint32_t**)&g.part_owned, M));
+  TRY(dev_alloc(ctx, &st.prop, V));
+  TRY(dev_alloc(ctx, &st.upd, V));
+  TRY(dev_alloc(ctx, &st.ranks, V));
+  TRY(dev_alloc(ctx, &st.F, VW));
+  TRY(dev_alloc(ctx, &st.UD, VW));
+  TRY(dev_alloc(ctx, &st.mprop, S));
+  TRY(dev_alloc(ctx, &st.mupd, S));
+  TRY(dev_alloc(ctx, &st.FB, SW));
+  TRY(dev_alloc(ctx, &st.MD, SW));
+  TRY(dev_alloc(ctx, &st.FV, S));
+  TRY(dev_alloc(ctx, &st.BV, S));
+  TRY(dev_alloc(ctx, &st.AL, S));
+  TRY(dev_alloc(ctx, &st.tile_cnt, T));
+  TRY(dev_alloc(ctx, &st.tile_off, T));
+  TRY(dev_alloc(ctx, &st.tile_goff, T));
+  TRY(dev_alloc(ctx, &st.part_cnt, M));
+  TRY(dev_alloc(ctx, &st.counters, NUM_COUNTERS));
+  CK(cudaMemsetAsync(st.counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, ctx->stream));
+  return GRD_OK;
+}
+
+}  // namespace
+
+int grd_upload_layout(grd_ctx* ctx) {
+  const Layout& L = ctx->L;
+  DevGraph& g = ctx->g;
+  ctx->upload_bytes = 0;
+  TRY(upload(ctx, (uint32_t*)g.slot_gid, L.slot_gid));
+  TRY(upload(ctx, (uint32_t*)g.row_off, L.row_off));
+  TRY(upload(ctx, (uint32_t*)g.col, L.col));
+  if (L.weighted) TRY(upload(ctx, (uint32_t*)g.wgt, L.wgt));
+  TRY(upload(ctx, (uint32_t*)g.outdeg, L.outdeg));
+  if (!L.hubs.empty()) {
+    static_assert(sizeof(HubChunk) == sizeof(HubChunkD), "hub chunk layout");
+    CK(cudaMemcpyAsync((void*)g.hubs, L.hubs.data(), sizeof(HubChunk) * L.hubs.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    ctx->upload_bytes += sizeof(HubChunk) * L.hubs.size();
+  }
+  TRY(upload(ctx, (uint32_t*)g.tile_part, L.tile_part));
+  TRY(upload(ctx, (uint32_t*)g.part_base, L.slot_base));
+  std::vector<uint32_t> T(L.M);
+  for (uint32_t p = 0; p < L.M; ++p) T[p] = L.T(p);
+  TRY(upload(ctx, (uint32_t*)g.part_T, T));
+  TRY(upload(ctx, (uint32_t*)g.part_owned, L.n_owned));
+  if (ctx->in_edges_alloc) {
+    TRY(upload(ctx, (uint32_t*)g.in_off, L.in_off));
+    TRY(upload(ctx, (uint32_t*)g.in_src, L.in_src));
+    if (L.weighted) TRY(upload(ctx, (uint32_t*)g.in_wgt, L.in_wgt));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GRD_OK;
+}
+
+int grd_ensure_in_edges(grd_ctx* ctx) {
+  if (ctx->in_edges_alloc) return GRD_OK;
+  build_in_edges(ctx->L);
+  const Layout& L = ctx->L;
+  TRY(dev_alloc(ctx, (uint32_t**)&ctx->g.in_off, L.S + 1));
+  TRY(dev_alloc(ctx, (uint32_t**)&ctx->g.in_src, std::max<size_t>(L.E, 4)));
+  if (L.weighted) TRY(dev_alloc(ctx, (uint32_t**)&ctx->g.in_wgt, std::max<size_t>(L.E, 4)));
+  ctx->in_edges_alloc = true;
+  TRY(upload(ctx, (uint32_t*)ctx->g.in_off, L.in_off));
+  TRY(upload(ctx, (uint32_t*)ctx->g.in_src, L.in_src));
+  if (L.weighted) TRY(upload(ctx, (uint32_t*)ctx->g.in_wgt, L.in_wgt));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GRD_OK;
+}
+
+// ---------------------------------------------------------------- stages --
+namespace {
+
+template <class F>
+int dispatch(int algo, F&& f) {
+  switch (algo) {
+    case GRD_PR_DELTA: return f(std::integral_constant<int, A_PR_DELTA>{});
+    case GRD_CC: return f(std::integral_constant<int, A_CC>{});
+    case GRD_SSSP_HOP: return f(std::integral_constant<int, A_SSSP_HOP>{});
+    case GRD_SSSP_W: return f(std::integral_constant<int, A_SSSP_W>{});
+    default: return GRD_E_INVALID;
+  }
+}
+
+int check_ready(grd_ctx* ctx) {
+  if (!ctx) return GRD_E_INVALID;
+  if (ctx->algo < 0) {
+    ctx->err = "no algorithm selected (grd_set_algo)";
+    return GRD_E_INVALID;
+  }
+  if (!ctx->inited) {
+    ctx->err = "grd_init has not been called";
+    return GRD_E_INVALID;
+  }
+  return GRD_OK;
+}
+
+uint32_t grid_for(grd_ctx* ctx, uint32_t blocks_per_sm) { return (uint32_t)ctx->num_sms * blocks_per_sm; }
+
+}  // namespace
+
+int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
+  const uint32_t T = ctx->g.num_tiles;
+  k_fwd_bits<<<T, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+  k_scan_tiles<<<1, 1024, 0, ctx->stream>>>(ctx->g, ctx->st, 1);
+  if (fused) {
+    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdXfer{});
+  } else {
+    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdPack{});
+    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdUnpack{});
+  }
+  CK_LAUNCH();
+  ctx->stats.kernel_launches += fused ? 3 : 4;
+  return GRD_OK;
+}
+
+int grd_enqueue_edge_map(grd_ctx* ctx) {
+  return dispatch(ctx->algo, [&](auto a) -> int {
+    constexpr int A = decltype(a)::value;
+    k_push<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    if (ctx->g.num_hubs)
+      k_hub_push<A><<<std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8)), 256, 0, ctx->stream>>>(ctx->g,
+                                                                                                     ctx->st);
+    CK_LAUNCH();
+    ctx->stats.push_rounds++;
+    ctx->stats.kernel_launches += ctx->g.num_hubs ? 2 : 1;
+    return GRD_OK;
+  });
+}
+
+// Backward sync; fused = pack and aggregate in one pass per partition group.
+int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate) {
+  const uint32_t T = ctx->g.num_tiles;
+  const Layout& L = ctx->L;
+  return dispatch(ctx->algo, [&](auto a) -> int {
+    constexpr int A = decltype(a)::value;
+    constexpr bool kPR = (A == A_PR_DELTA);
+    if (do_pack) {
+      k_tile_count<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.tile_cnt);
+      k_scan_tiles<<<1, 1024, 0, ctx->stream>>>(ctx->g, ctx->st, 0);
+      if (!fused) k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, nullptr, 0u, ctx->g, ctx->st, OpBwdPack<kPR>{});
+      ctx->stats.kernel_launches += fused ? 2 : 3;
+    }
+    if (do_aggregate) {
+      // PageRank: one launch per partition in ascending order fixes the
+      // per-vertex summation order; min-aggregates run as one launch.
+      const uint32_t groups = kPR ? L.M : 1;
+      for (uint32_t p = 0; p < groups; ++p) {
+        uint32_t t0 = kPR ? L.slot_base[p] / TILE_SLOTS : 0;
+        uint32_t t1 = kPR ? ((p + 1 < L.M) ? L.slot_base[p + 1] / TILE_SLOTS : T) : T;
+        if (fused)
+          k_compact<<<t1 - t0, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.MD, t0, ctx->g, ctx->st, OpBwdXfer<A>{});
+        else
+          k_compact<<<t1 - t0, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.MD, t0, ctx->g, ctx->st,
+                                                      OpAggregate<A>{});
+      }
+      ctx->stats.kernel_launches += groups;
+    }
+    CK_LAUNCH();
+    return GRD_OK;
+  });
+}
+
+int grd_enqueue_update(grd_ctx* ctx) {
+  CK(cudaMemsetAsync(ctx->st.counters + C_FRONTIER, 0, sizeof(unsigned long long), ctx->stream));
+  const uint32_t blocks = std::max<uint32_t>(1, std::min<uint32_t>((ctx->g.V + 255) / 256, grid_for(ctx, 8)));
+  return dispatch(ctx->algo, [&](auto a) -> int {
+    constexpr int A = decltype(a)::value;
+    k_update<A><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance, ctx->params.damping);
+    CK_LAUNCH();
+    ctx->stats.kernel_launches += 1;
+    return GRD_OK;
+  });
+}
+
+// Once per round, after the update: copies the device counters to the host
+// (the only host synchronisation of a round) and folds them into the stats.
+int grd_read_counters(grd_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->h_counters, ctx->st.counters, sizeof(unsigned long long) * NUM_COUNTERS,
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->stats.edges_scanned = ctx->h_counters[C_EDGES];
+  ctx->stats.bytes_synced = ctx->h_counters[C_BYTES];
+  ctx->stats.reference_bytes_moved = ctx->h_counters[C_REFBYTES];
+  ctx->stats.actives_total += ctx->h_counters[C_ACTIVE];
+  if (ctx->h_counters[C_ERR]) {
+    ctx->err = "device-side error code " + std::to_string(ctx->h_counters[C_ERR]);
+    return ctx->h_counters[C_ERR] == 1 ? GRD_E_TIMEOUT : GRD_E_CUDA;
+  }
+  return GRD_OK;
+}
+
+// Stage timing: events 0..4 bracket forward sync, edge-map, backward sync and
+// update of one round; read after the round's synchronisation.
+void grd_prof_mark(grd_ctx* ctx, int i) {
+  if (ctx->profiling) cudaEventRecord(ctx->ev[i], ctx->stream);
+}
+
+void grd_prof_collect(grd_ctx* ctx) {
+  if (!ctx->profiling) return;
+  float ms;
+  for (int i = 0; i < 4; ++i)
+    if (cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]) == cudaSuccess) ctx->stats.stage_ms[i] += ms;
+  if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[4]) == cudaSuccess) ctx->stats.stage_ms[4] += ms;
+  (void)cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ C ABI --
+extern "C" {
+
+const char* grd_version(void) { return "grudon-gb300 0.1 (sm_103a)"; }
+
+int grd_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+const char* grd_create_error(void) { return g_create_error.c_str(); }
+
+const char* grd_last_error(const grd_ctx* ctx) { return ctx ? ctx->err.c_str() : "null ctx"; }
+
+int grd_ctx_create(const grd_csr* graph, const uint32_t* mirror_part, uint32_t num_compute, uint32_t num_memory,
+                   int device, grd_ctx** out) {
+  g_create_error.clear();
+  if (!out) {
+    g_create_error = "out is NULL";
+    return GRD_E_INVALID;
+  }
+  *out = nullptr;
+  if (!graph) {
+    g_create_error = "graph is NULL";
+    return GRD_E_INVALID;
+  }
+  if (num_compute != 1) {
+    g_create_error = "num_compute must be 1";
+    return GRD_E_INVALID;
+  }
+  int ndev = grd_device_count();
+  if (ndev <= 0) {
+    g_create_error = "no CUDA device visible";
+    return GRD_E_CUDA;
+  }
+  if (device < 0 || device >= ndev) {
+    g_create_error = "device index out of range";
+    return GRD_E_INVALID;
+  }
+  grd_ctx* ctx = new (std::nothrow) grd_ctx();
+  if (!ctx) return GRD_E_OOM;
+  ctx->device = device;
+  std::string why = build_layout(graph->num_vertices, graph->num_edges, graph->row_offsets, graph->col_indices,
+                                 graph->weights, mirror_part, num_memory, ctx->L);
+  if (!why.empty()) {
+    g_create_error = why;
+    delete ctx;
+    return GRD_E_INVALID;
+  }
+  int rc = grd_ctx_init_device(ctx);
+  if (rc != GRD_OK) {
+    g_create_error = ctx->err;
+    grd_ctx_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return GRD_OK;
+}
+
+void grd_ctx_destroy(grd_ctx* ctx) {
+  if (!ctx) return;
+  if (ctx->stream) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+  }
+  grd_ctx_release_extras(ctx);
+  for (void* p : ctx->allocs) cudaFree(p);
+  for (void* p : ctx->host_registered) cudaHostUnregister(p);
+  for (cudaEvent_t e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  (void)cudaGetLastError();
+  delete ctx;
+}
+
+int grd_upload(grd_ctx* ctx, uint64_t* bytes_copied) {
+  if (!ctx) return GRD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int rc = grd_upload_layout(ctx);
+  if (bytes_copied) *bytes_copied = ctx->upload_bytes;
+  return rc;
+}
+
+int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
+  if (!ctx) return GRD_E_INVALID;
+  if (algo < GRD_PR_DELTA || algo > GRD_SSSP_W) {
+    ctx->err = "unknown algorithm id";
+    return GRD_E_INVALID;
+  }
+  if (algo == GRD_SSSP_W && !ctx->L.weighted) {
+    ctx->err = "GRD_SSSP_W needs edge weights";
+    return GRD_E_INVALID;
+  }
+  grd_params p{};
+  p.source = 0;
+  p.max_rounds = 1000;
+  p.damping = 0.85;
+  p.tolerance = (algo == GRD_PR_PULL) ? 1e-7 : 1e-6;
+  p.direction = GRD_DIR_AUTO;
+  p.frontier_format = GRD_FMT_AUTO;
+  if (params) p = *params;
+  if ((algo == GRD_SSSP_HOP || algo == GRD_SSSP_W) && p.source >= ctx->L.V) {
+    ctx->err = "SSSP source out of range";
+    return GRD_E_INVALID;
+  }
+  if (p.max_rounds == 0) {
+    ctx->err = "max_rounds must be > 0";
+    return GRD_E_INVALID;
+  }
+  if (!(p.damping > 0.0 && p.damping < 1.0)) {
+    ctx->err = "damping must be in (0,1)";
+    return GRD_E_INVALID;
+  }
+  CK(cudaSetDevice(ctx->device));
+  if (algo == GRD_PR_PULL || p.direction == GRD_DIR_PULL || p.direction == GRD_DIR_AUTO) {
+    int rc = grd_ensure_in_edges(ctx);
+    if (rc != GRD_OK) return rc;
+  }
+  ctx->algo = algo;
+  ctx->params = p;
+  ctx->inited = false;
+  return GRD_OK;
+}
+
+int grd_init(grd_ctx* ctx) {
+  if (!ctx) return GRD_E_INVALID;
+  if (ctx->algo < 0) {
+    ctx->err = "no algorithm selected (grd_set_algo)";
+    return GRD_E_INVALID;
+  }
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemsetAsync(ctx->st.counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, ctx->stream));
+  const uint64_t n = std::max<uint64_t>(ctx->g.S, ctx->g.V);
+  const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)grid_for(ctx, 16));
+  int rc = grd_enqueue_init(ctx, blocks);
+  if (rc != GRD_OK) return rc;
+  CK_LAUNCH();
+  ctx->stats = grd_stats{};
+  ctx->stats.kernel_launches = 1;
+  ctx->inited = true;
+  return GRD_OK;
+}
+
+int grd_sync_fwd(grd_ctx* ctx) {
+  TRY(check_ready(ctx));
+  if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, 0);
+  return grd_enqueue_fwd(ctx, false);
+}
+
+int grd_edge_map(grd_ctx* ctx) {
+  TRY(check_ready(ctx));
+  if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, 1);
+  return grd_enqueue_edge_map(ctx);
+}
+
+int grd_sync_bwd(grd_ctx* ctx) {
+  TRY(check_ready(ctx));
+  if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, 2);
+  return grd_enqueue_bwd(ctx, false, true, false);
+}
+
+int grd_aggregate(grd_ctx* ctx) {
+  TRY(check_ready(ctx));
+  if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, 3);
+  return grd_enqueue_bwd(ctx, false, false, true);
+}
+
+int grd_update(grd_ctx* ctx, uint64_t* frontier_size) {
+  TRY(check_ready(ctx));
+  if (ctx->algo == GRD_PR_PULL) {
+    TRY(grd_pull_stage(ctx, 4));
+  } else {
+    TRY(grd_enqueue_update(ctx));
+  }
+  TRY(grd_read_counters(ctx));
+  ctx->stats.rounds++;
+  const uint64_t f = ctx->h_counters[C_FRONTIER];
+  ctx->stats.converged = (f == 0);
+  if (frontier_size) *frontier_size = f;
+  return GRD_OK;
+}
+
+int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
+  TRY(check_ready(ctx));
+  CK(cudaSetDevice(ctx->device));
+  if (ctx->algo == GRD_PR_PULL) {
+    TRY(grd_pull_run(ctx));
+  } else {
+    uint64_t f = 1;
+    while (ctx->stats.rounds < ctx->params.max_rounds) {
+      grd_prof_mark(ctx, 0);
+      TRY(grd_enqueue_fwd(ctx, true));
+      grd_prof_mark(ctx, 1);
+      TRY(grd_enqueue_edge_map(ctx));
+      grd_prof_mark(ctx, 2);
+      TRY(grd_enqueue_bwd(ctx, true, true, true));
+      grd_prof_mark(ctx, 3);
+      TRY(grd_enqueue_update(ctx));
+      grd_prof_mark(ctx, 4);
+      TRY(grd_read_counters(ctx));
+      grd_prof_collect(ctx);
+      ctx->stats.rounds++;
+      f = ctx->h_counters[C_FRONTIER];
+      if (f == 0) break;
+    }
+    ctx->stats.converged = (f == 0);
+  }
+  if (stats) *stats = ctx->stats;
+  if ((flags & GRD_RUN_STRICT) && !ctx->stats.converged) {
+    ctx->err = "round cap reached with a non-empty frontier";
+    return GRD_E_ROUND_CAP;
+  }
+  return GRD_OK;
+}
+
+int grd_get_stats(const grd_ctx* ctx, grd_stats* stats) {
+  if (!ctx || !stats) return GRD_E_INVALID;
+  *stats = ctx->stats;
+  return GRD_OK;
+}
+
+int grd_set_profiling(grd_ctx* ctx, int enable) {
+  if (!ctx) return GRD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  if (enable && !ctx->ev[0])
+    for (cudaEvent_t& e : ctx->ev) CK(cudaEventCreate(&e));
+  ctx->profiling = enable != 0;
+  return GRD_OK;
+}
+
+static int read_dev(grd_ctx* ctx, void* host, const void* dev, size_t bytes, size_t need) {
+  if (!ctx || !host) return GRD_E_INVALID;
+  if (bytes < need) {
+    ctx->err = "host buffer too small: need " + std::to_string(need) + " bytes";
+    return GRD_E_INVALID;
+  }
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpyAsync(host, dev, need, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GRD_OK;
+}
+
+int grd_read_props(grd_ctx* ctx, void* host, size_t bytes) {
+  if (!ctx) return GRD_E_INVALID;
+  return read_dev(ctx, host, ctx->st.prop, bytes, sizeof(uint32_t) * ctx->L.V);
+}
+
+int grd_read_ranks(grd_ctx* ctx, float* host, size_t count) {
+  if (!ctx) return GRD_E_INVALID;
+  return read_dev(ctx, host, ctx->st.ranks, count * sizeof(float), sizeof(float) * ctx->L.V);
+}
+
+int grd_read_updates(grd_ctx* ctx, void* host, size_t bytes) {
+  if (!ctx) return GRD_E_INVALID;
+  return read_dev(ctx, host, ctx->st.upd, bytes, sizeof(uint32_t) * ctx->L.V);
+}
+
+int grd_read_frontier(grd_ctx* ctx, uint32_t* host, size_t words) {
+  if (!ctx) return GRD_E_INVALID;
+  return read_dev(ctx, host, ctx->st.F, words * 4, sizeof(uint32_t) * ((ctx->L.V + 31) / 32));
+}
+
+int grd_layout_info(const grd_ctx* ctx, uint32_t part, uint32_t* n_owned, uint32_t* n_proxy, uint64_t* num_edges) {
+  if (!ctx || part >= ctx->L.M) return GRD_E_INVALID;
+  if (n_owned) *n_owned = ctx->L.n_owned[part];
+  if (n_proxy) *n_proxy = ctx->L.n_proxy[part];
+  if (num_edges) *num_edges = ctx->L.part_edges[part];
+  return GRD_OK;
+}
+
+int grd_layout_slots(const grd_ctx* ctx, uint32_t part, uint32_t* host, size_t count) {
+  if (!ctx || part >= ctx->L.M || !host) return GRD_E_INVALID;
+  const uint32_t T = ctx->L.T(part);
+  if (count < T) return GRD_E_INVALID;
+  std::memcpy(host, ctx->L.slot_gid.data() + ctx->L.slot_base[part], sizeof(uint32_t) * T);
+  return GRD_OK;
+}
+
+int grd_layout_preview(const grd_csr* graph, const uint32_t* mirror_part, uint32_t num_memory, uint32_t part,
+                       uint32_t* slots, size_t cap, uint32_t* n_owned, uint32_t* n_proxy) {
+  g_create_error.clear();
+  if (!graph || part >= num_memory) return GRD_E_INVALID;
+  Layout L;
+  std::string why = build_layout(graph->num_vertices, graph->num_edges, graph->row_offsets, graph->col_indices,
+                                 graph->weights, mirror_part, num_memory, L);
+  if (!why.empty()) {
+    g_create_error = why;
+    return GRD_E_INVALID;
+  }
+  if (n_owned) *n_owned = L.n_owned[part];
+  if (n_proxy) *n_proxy = L.n_proxy[part];
+  if (slots) std::memcpy(slots, L.slot_gid.data() + L.slot_base[part], sizeof(uint32_t) * std::min<size_t>(cap, L.T(part)));
+  return GRD_OK;
+}
+
+int grd_device_props(grd_ctx* ctx, void** dptr) {
+  if (!ctx || !dptr) return GRD_E_INVALID;
+  *dptr = ctx->st.prop;
+  return GRD_OK;
+}
+
+int grd_device_ranks(grd_ctx* ctx, float** dptr) {
+  if (!ctx || !dptr) return GRD_E_INVALID;
+  *dptr = ctx->st.ranks;
+  return GRD_OK;
+}
+
+void* grd_stream(grd_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int grd_synchronize(grd_ctx* ctx) {
+  if (!ctx) return GRD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GRD_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ device setup --
+int grd_ctx_init_device(grd_ctx* ctx) {
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaMallocHost((void**)&ctx->h_counters, sizeof(unsigned long long) * NUM_COUNTERS));
+  std::memset(ctx->h_counters, 0, sizeof(unsigned long long) * NUM_COUNTERS);
+  TRY(alloc_and_upload(ctx));
+  // Pin the large host layout arrays so grd_upload copies run at full
+  // host->device bandwidth; pageable copies still work if pinning fails.
+  for (auto* v : {&ctx->L.col, &ctx->L.wgt, &ctx->L.row_off, &ctx->L.slot_gid}) {
+    if (v->size() * sizeof(uint32_t) < (1u << 20)) continue;
+    if (cudaHostRegister(v->data(), v->size() * sizeof(uint32_t), cudaHostRegisterDefault) == cudaSuccess)
+      ctx->host_registered.push_back(v->data());
+    else
+      (void)cudaGetLastError();
+  }
+  return grd_upload_layout(ctx);
+}
+
+int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks) {
+  const double d = ctx->params.damping;
+  const uint32_t src = ctx->params.source;
+  switch (ctx->algo) {
+    case GRD_PR_DELTA: k_init<A_PR_DELTA><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->st, src, d); break;
+    case GRD_PR_PULL: k_init<A_PR_PULL><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->st, src, d); break;
+    case GRD_CC: k_init<A_CC><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->st, src, d); break;
+    case GRD_SSSP_HOP: k_init<A_SSSP_HOP><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->st, src, d); break;
+    case GRD_SSSP_W: k_init<A_SSSP_W><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->st, src, d); break;
+    default: return GRD_E_INVALID;
+  }
+  CK_LAUNCH();
+  if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, -1);  // pull-specific init
+  return GRD_OK;
+}

@@ -1,0 +1,232 @@
+/*
+ * grudon_gpu.h — C ABI of the GB300 (sm_103a) per-round graph operator.
+ *
+ * One opaque grd_ctx owns every device buffer of one partitioned graph: the
+ * compute partition (master copies, gid-indexed) and the M memory partitions
+ * (out-edge CSR over owned vertices plus proxy slots), all resident in one
+ * GPU's HBM.  Every call is stream-ordered on the ctx's own CUDA stream; a ctx
+ * is single-threaded, distinct ctxs may be used concurrently.
+ *
+ * Reference interfaces replaced (paths relative to the Grudon project):
+ *   grd_ctx_create      DistributedGraph ctor, src/DistributedGraph.cpp:13-785
+ *                       (layout, proxies, translation tables, bitCommVector)
+ *   grd_set_algo        choice of plugin class, src/main.cpp:133-134
+ *   grd_init            GraphAlgorithm::init overrides: pr.cpp:20-61,
+ *                       cc.cpp:18-40, sssp.cpp:18-47
+ *   grd_sync_fwd        compute->memory frontier pack + unpack,
+ *                       src/GraphAlgorithm.cpp:199-343
+ *   grd_edge_map        TraverseWorker::traverse -> gen_updates,
+ *                       src/Workers.cpp:109-113, pr.cpp:91-121, cc.cpp:54-84,
+ *                       sssp.cpp:61-90
+ *   grd_sync_bwd        memory->compute dirty pack, src/GraphAlgorithm.cpp:356-424
+ *   grd_aggregate       compute-side aggregate, src/GraphAlgorithm.cpp:478-581
+ *                       + pr.cpp:149-153, cc.cpp:109-113, sssp.cpp:115-119
+ *   grd_update          UpdateWorker::update (update_frontier + apply_updates)
+ *                       + termination_check, src/GraphAlgorithm.cpp:643-662
+ *   grd_run             GraphAlgorithm::run, src/GraphAlgorithm.cpp:145-701
+ *   grd_read_*          PageRank/CC/SSSP::printState output, pr.cpp:162-176
+ *
+ * Status convention: every int-returning call returns GRD_OK (0) or a negative
+ * GRD_E_* code; grd_last_error(ctx) gives a one-line reason.
+ */
+#ifndef GRUDON_GPU_H
+#define GRUDON_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GRD_OK            0
+#define GRD_E_INVALID   (-1) /* bad argument, size or state                   */
+#define GRD_E_OOM       (-2) /* device or host allocation failed              */
+#define GRD_E_CUDA      (-3) /* CUDA runtime error (incl. no device)          */
+#define GRD_E_TIMEOUT   (-4) /* a bounded device wait gave up                 */
+#define GRD_E_ROUND_CAP (-5) /* grd_run hit max_rounds with a live frontier
+                                and GRD_RUN_STRICT was requested              */
+#define GRD_E_IO        (-6) /* file could not be read/written or is corrupt  */
+
+/* ---- algorithms (GraphAlgorithm plugins) -------------------------------- */
+#define GRD_PR_DELTA  0 /* reference delta-push PageRank, float, TOL 1e-6    */
+#define GRD_PR_PULL   1 /* Jacobi PageRank, FP32 Kahan sums, FP64 residual   */
+#define GRD_CC        2 /* min-label propagation along out-edges, uint32     */
+#define GRD_SSSP_HOP  3 /* reference unit-weight SSSP (hop count), uint32    */
+#define GRD_SSSP_W    4 /* weighted SSSP: prop[u] + w(u,v), uint32 weights   */
+
+/* ---- traversal direction / frontier format (per-round policy) ----------- */
+#define GRD_DIR_AUTO  0
+#define GRD_DIR_PUSH  1
+#define GRD_DIR_PULL  2
+#define GRD_FMT_AUTO    0
+#define GRD_FMT_BITVEC  1
+#define GRD_FMT_LIST    2
+
+#define GRD_RUN_STRICT  1u /* flag: return GRD_E_ROUND_CAP at the round cap */
+
+/* Host CSR as handed to the library: row_offsets has num_vertices+1 entries
+ * (u64, like the reference's LC_CSR_Graph row ends), col_indices num_edges
+ * u32 global ids, weights num_edges u32 or NULL. */
+typedef struct grd_csr {
+  uint32_t num_vertices;
+  uint64_t num_edges;
+  const uint64_t* row_offsets;
+  const uint32_t* col_indices;
+  const uint32_t* weights;
+} grd_csr;
+
+typedef struct grd_params {
+  uint32_t source;      /* SSSP source gid (reference: gid 0)                */
+  uint32_t max_rounds;  /* round cap (reference MAX_ITERATIONS = 1000)       */
+  double damping;       /* PageRank damping (reference 0.85)                 */
+  double tolerance;     /* PR_DELTA: activation threshold (reference 1e-6);
+                           PR_PULL: stop when L1 residual / V < tolerance    */
+  int direction;        /* GRD_DIR_*                                          */
+  int frontier_format;  /* GRD_FMT_*                                          */
+} grd_params;
+
+typedef struct grd_stats {
+  uint32_t rounds;            /* reference "Iterations" statistic          */
+  uint32_t converged;         /* 1 if the frontier emptied before the cap  */
+  uint64_t edges_scanned;     /* out-edges (push) / in-edges (pull) read   */
+  uint64_t bytes_synced;      /* bitvector words + packed values, both
+                                 directions, all partitions (true size)    */
+  uint64_t reference_bytes_moved; /* the reference's TotalBytesMoved
+                                 formula (bitvector count inflated x8,
+                                 src/GraphAlgorithm.cpp:251-265)           */
+  double last_residual;       /* PR_PULL: last L1 residual / V (FP64)      */
+  uint32_t push_rounds;       /* rounds that ran the push edge-map         */
+  uint32_t pull_rounds;       /* rounds that ran the pull edge-map         */
+  uint64_t actives_total;     /* sum over rounds of unpacked active slots  */
+  uint64_t kernel_launches;   /* kernels this ctx launched since grd_init  */
+  /* With grd_set_profiling(ctx,1): CUDA-event milliseconds per stage, summed
+   * over rounds: [0] forward sync, [1] edge-map, [2] backward sync +
+   * aggregate, [3] update, [4] whole rounds. */
+  double stage_ms[5];
+} grd_stats;
+
+typedef struct grd_ctx grd_ctx;
+
+/* Library / device info ----------------------------------------------------*/
+const char* grd_version(void);
+/* Returns number of CUDA devices visible (0 when none); never faults. */
+int grd_device_count(void);
+
+/* Context lifetime ---------------------------------------------------------*/
+/* Builds the 1-compute + num_memory-partition layout from a host CSR and a
+ * mirror (memory) partition id per vertex (NULL => gid % num_memory, the
+ * reference's NaivePartitioner), and uploads it to device `device`.
+ * num_compute must be 1 (every configuration of this operator uses one). */
+int grd_ctx_create(const grd_csr* graph, const uint32_t* mirror_part,
+                   uint32_t num_compute, uint32_t num_memory, int device,
+                   grd_ctx** out);
+void grd_ctx_destroy(grd_ctx* ctx);
+const char* grd_last_error(const grd_ctx* ctx);
+/* Error text of the most recent failed grd_ctx_create on this thread. */
+const char* grd_create_error(void);
+
+/* Re-uploads the layout arrays from the host copy kept at create time
+ * (timed host->device traffic for end-to-end runs). Returns bytes copied. */
+int grd_upload(grd_ctx* ctx, uint64_t* bytes_copied);
+
+/* Algorithm selection and per-stage round API -----------------------------*/
+int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params);
+int grd_init(grd_ctx* ctx);
+int grd_sync_fwd(grd_ctx* ctx);
+int grd_edge_map(grd_ctx* ctx);
+int grd_sync_bwd(grd_ctx* ctx);
+int grd_aggregate(grd_ctx* ctx);
+/* Applies update_frontier + apply_updates; *frontier_size = |frontier|. */
+int grd_update(grd_ctx* ctx, uint64_t* frontier_size);
+
+/* Full run: init() already called; loops rounds until the frontier is empty
+ * or params.max_rounds.  flags: GRD_RUN_STRICT. */
+int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats);
+int grd_get_stats(const grd_ctx* ctx, grd_stats* stats);
+/* Per-stage CUDA-event timing inside grd_run (off by default). */
+int grd_set_profiling(grd_ctx* ctx, int enable);
+
+/* Results (blocking device->host copies) -----------------------------------*/
+/* Compute-side vertex_properties, gid order (uint32 for CC/SSSP, float for PR
+ * contributions). */
+int grd_read_props(grd_ctx* ctx, void* host, size_t bytes);
+/* PageRank values (pr_vals for PR_DELTA, ranks for PR_PULL), float[V]. */
+int grd_read_ranks(grd_ctx* ctx, float* host, size_t count);
+/* Compute-side vertex_updates, gid order. */
+int grd_read_updates(grd_ctx* ctx, void* host, size_t bytes);
+/* Current compute frontier bitmap, ceil(V/32) uint32 words. */
+int grd_read_frontier(grd_ctx* ctx, uint32_t* host, size_t words);
+
+/* Layout introspection (translation-slot index space, reference
+ * src/DistributedGraph.cpp:630-775) ---------------------------------------*/
+int grd_layout_info(const grd_ctx* ctx, uint32_t part, uint32_t* n_owned,
+                    uint32_t* n_proxy, uint64_t* num_edges);
+/* slot -> gid of memory partition `part` (owned slots, then proxy slots). */
+int grd_layout_slots(const grd_ctx* ctx, uint32_t part, uint32_t* host,
+                     size_t count);
+
+/* Host-only preview of the same slot space without a device: writes the
+ * slot -> gid order of partition `part` (up to cap entries) and its sizes. */
+int grd_layout_preview(const grd_csr* graph, const uint32_t* mirror_part,
+                       uint32_t num_memory, uint32_t part, uint32_t* slots,
+                       size_t cap, uint32_t* n_owned, uint32_t* n_proxy);
+
+/* Device pointers of the compute-side arrays (for zero-copy callers). */
+int grd_device_props(grd_ctx* ctx, void** dptr);
+int grd_device_ranks(grd_ctx* ctx, float** dptr);
+/* CUDA stream the ctx launches on (cudaStream_t as void*). */
+void* grd_stream(grd_ctx* ctx);
+/* Blocks until all work on the ctx stream is done. */
+int grd_synchronize(grd_ctx* ctx);
+
+/* ---- host graph tools (seeded generators, formats, partition files) ----- */
+typedef struct grd_host_graph {
+  uint32_t num_vertices;
+  uint64_t num_edges;
+  uint64_t* row_offsets; /* V+1 */
+  uint32_t* col_indices; /* E, ascending within each row, no dups/loops */
+  uint32_t* weights;     /* E or NULL */
+  uint64_t seed;
+} grd_host_graph;
+
+/* RMAT: 2^scale vertices, edge_factor*2^scale draws, quadrant probabilities
+ * a,b,c (d = 1-a-b-c); self-loops and duplicates removed; no relabelling.
+ * symmetrize: add reverse edges before dedupe.  weighted: u32 weights in
+ * [1,255] keyed by the final sorted edge index.  threads<=0: all cores. */
+int grd_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b,
+                 double c, uint64_t seed, int symmetrize, int weighted,
+                 int threads, grd_host_graph** out);
+/* Erdos-Renyi G(n, m = edge_factor*n) uniform pairs, deduped. */
+int grd_gen_er(uint32_t num_vertices, uint32_t edge_factor, uint64_t seed,
+               int symmetrize, int weighted, int threads,
+               grd_host_graph** out);
+/* k x k 4-neighbour grid, both directions, weights in [1,255]. */
+int grd_gen_grid(uint32_t k, uint64_t seed, int weighted, int threads,
+                 grd_host_graph** out);
+/* Host graph from caller arrays (copied). */
+int grd_graph_from_csr(const grd_csr* csr, grd_host_graph** out);
+void grd_graph_free(grd_host_graph* g);
+/* Default seed of the RMAT workloads: 0x6772756E ^ (scale<<8) ^ ef. */
+uint64_t grd_rmat_seed(uint32_t scale, uint32_t edge_factor);
+
+/* Galois binary .gr (version 1) and MatrixMarket .mtx I/O. */
+int grd_write_gr(const grd_host_graph* g, const char* path);
+int grd_read_gr(const char* path, grd_host_graph** out);
+int grd_write_mtx(const grd_host_graph* g, const char* path);
+int grd_read_mtx(const char* path, grd_host_graph** out);
+
+/* Edge-balanced contiguous mirror partitioning (one id per vertex). */
+int grd_partition_edge_balanced(const grd_host_graph* g, uint32_t num_memory,
+                                uint32_t* mirror_part);
+/* Partition file: one integer per line (include/partitioning_engine/
+ * Partitioner.hpp:98-102 format). */
+int grd_write_partition_file(const uint32_t* part, uint32_t n, const char* path);
+int grd_read_partition_file(const char* path, uint32_t n, uint32_t num_memory,
+                            uint32_t* part);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRUDON_GPU_H */

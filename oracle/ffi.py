@@ -1,0 +1,133 @@
+"""ctypes wrapper of the oracle library (test infrastructure only).
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg;
+never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+ORC_PR_DELTA, ORC_PR_PULL, ORC_CC, ORC_SSSP_HOP, ORC_SSSP_W = 0, 1, 2, 3, 4
+
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+
+
+class orc_stats(C.Structure):
+    _fields_ = [("rounds", C.c_uint32), ("converged", C.c_uint32), ("edges_scanned", C.c_uint64),
+                ("bytes_synced", C.c_uint64), ("reference_bytes_moved", C.c_uint64)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.OUT
+        if not path.exists():
+            path = _build.build()
+        L = C.CDLL(os.fspath(path))
+        L.orc_run.restype = C.c_int
+        L.orc_run.argtypes = [C.c_int, C.c_uint32, C.c_uint64, u64p, u32p, u32p, u32p, C.c_uint32, C.c_uint32,
+                              C.c_uint32, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.POINTER(orc_stats)]
+        L.orc_layout_slots.restype = C.c_uint32
+        L.orc_layout_slots.argtypes = [C.c_uint32, u64p, u32p, u32p, C.c_uint32, C.c_uint32, u32p, C.c_uint32, u32p]
+        L.orc_bfs.restype = None
+        L.orc_bfs.argtypes = [C.c_uint32, u64p, u32p, C.c_uint32, u32p]
+        L.orc_dijkstra.restype = None
+        L.orc_dijkstra.argtypes = [C.c_uint32, u64p, u32p, u32p, C.c_uint32, u32p]
+        L.orc_cc_union_find.restype = None
+        L.orc_cc_union_find.argtypes = [C.c_uint32, u64p, u32p, u32p]
+        L.orc_pr_jacobi_fp64.restype = C.c_uint32
+        L.orc_pr_jacobi_fp64.argtypes = [C.c_uint32, u64p, u32p, C.c_double, C.c_uint32, C.c_double,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def _csr(ro, col, w=None):
+    ro = np.ascontiguousarray(ro, dtype=np.uint64)
+    col = np.ascontiguousarray(col, dtype=np.uint32)
+    if len(col) == 0:
+        col = np.zeros(1, dtype=np.uint32)
+    w = None if w is None else np.ascontiguousarray(w, dtype=np.uint32)
+    return ro, col, w
+
+
+def _p32(a):
+    return None if a is None else a.ctypes.data_as(u32p)
+
+
+def run(algo: int, ro, col, w=None, mirror=None, num_memory: int = 1, source: int = 0, max_rounds: int = 1000,
+        damping: float = 0.85, tol: float = 1e-6, threads: int = 1) -> dict:
+    """Restated reference round protocol; returns props/updates/ranks/stats."""
+    ro, col, w = _csr(ro, col, w)
+    V = len(ro) - 1
+    mir = None if mirror is None else np.ascontiguousarray(mirror, dtype=np.uint32)
+    dt = np.float32 if algo == ORC_PR_DELTA else np.uint32
+    props = np.zeros(V, dtype=dt)
+    upd = np.zeros(V, dtype=dt)
+    ranks = np.zeros(V, dtype=np.float32)
+    st = orc_stats()
+    rc = lib().orc_run(algo, V, int(ro[-1]), ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), _p32(w), _p32(mir),
+                       num_memory, source, max_rounds, damping, tol, threads, props.ctypes.data_as(C.c_void_p),
+                       ranks.ctypes.data_as(C.c_void_p), upd.ctypes.data_as(C.c_void_p), C.byref(st))
+    if rc != 0:
+        raise ValueError("oracle rejected the arguments")
+    out = {"props": props, "updates": upd, "stats": {f: getattr(st, f) for f, _ in orc_stats._fields_}}
+    if algo == ORC_PR_DELTA:
+        out["ranks"] = ranks
+    return out
+
+
+def layout_slots(ro, col, mirror, num_memory: int, part: int):
+    ro, col, _ = _csr(ro, col)
+    V = len(ro) - 1
+    mir = None if mirror is None else np.ascontiguousarray(mirror, dtype=np.uint32)
+    cap = V * 2 + 1
+    out = np.zeros(cap, dtype=np.uint32)
+    n_owned = C.c_uint32()
+    T = lib().orc_layout_slots(V, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), _p32(mir), num_memory, part,
+                               out.ctypes.data_as(u32p), cap, C.byref(n_owned))
+    return out[:T].copy(), int(n_owned.value)
+
+
+def bfs(ro, col, src: int) -> np.ndarray:
+    ro, col, _ = _csr(ro, col)
+    d = np.zeros(len(ro) - 1, dtype=np.uint32)
+    lib().orc_bfs(len(ro) - 1, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), src, d.ctypes.data_as(u32p))
+    return d
+
+
+def dijkstra(ro, col, w, src: int) -> np.ndarray:
+    ro, col, w = _csr(ro, col, w)
+    if len(w) == 0:
+        w = np.zeros(1, dtype=np.uint32)
+    d = np.zeros(len(ro) - 1, dtype=np.uint32)
+    lib().orc_dijkstra(len(ro) - 1, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), w.ctypes.data_as(u32p), src,
+                       d.ctypes.data_as(u32p))
+    return d
+
+
+def cc_union_find(ro, col) -> np.ndarray:
+    ro, col, _ = _csr(ro, col)
+    lab = np.zeros(len(ro) - 1, dtype=np.uint32)
+    lib().orc_cc_union_find(len(ro) - 1, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), lab.ctypes.data_as(u32p))
+    return lab
+
+
+def pr_jacobi_fp64(ro, col, damping: float = 0.85, iters: int = 100, tol: float = 0.0):
+    ro, col, _ = _csr(ro, col)
+    V = len(ro) - 1
+    pr = np.zeros(V, dtype=np.float64)
+    res = C.c_double()
+    it = lib().orc_pr_jacobi_fp64(V, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), damping, iters, tol,
+                                  pr.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res))
+    return pr, int(it), float(res.value)

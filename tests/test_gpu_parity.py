@@ -1,0 +1,129 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+CC and SSSP are compared bit-exactly (labels, distances, round counts, wire
+statistics); delta PageRank within an absolute 2e-5 + relative 1e-4 bound on
+pr_vals (float atomics make the per-vertex summation order nondeterministic,
+exactly as the reference's concurrent atomicAdd does).
+"""
+import numpy as np
+import pytest
+
+import grudon_gb300 as g
+from oracle import ffi as O
+
+pytestmark = pytest.mark.gpu
+
+ALGOS = [(g.GRD_CC, O.ORC_CC), (g.GRD_SSSP_HOP, O.ORC_SSSP_HOP), (g.GRD_SSSP_W, O.ORC_SSSP_W)]
+
+
+GRAPHS = {
+    "rmat12_sym": lambda: g.Graph.rmat(12, 8, symmetrize=True, weighted=True),
+    "rmat13_dir": lambda: g.Graph.rmat(13, 16, weighted=True),
+    "er4k": lambda: g.Graph.er(4000, 4, seed=7, symmetrize=True, weighted=True),
+    "grid40": lambda: g.Graph.grid(40, seed=3),
+}
+
+
+@pytest.mark.parametrize("num_memory", [1, 3])
+@pytest.mark.parametrize("name", list(GRAPHS))
+def test_min_algorithms_bit_exact(gpu, name, num_memory):
+    G = GRAPHS[name]()
+    ro, ci, w = G.row_offsets, G.col_indices, G.weights
+    part = G.partition_edge_balanced(num_memory) if num_memory > 1 else None
+    with g.Context(G, part, num_memory=num_memory) as ctx:
+        for algo, oalgo in ALGOS:
+            ctx.set_algo(algo)
+            ctx.init()
+            st = ctx.run()
+            ref = O.run(oalgo, ro, ci, w, mirror=part, num_memory=num_memory)
+            np.testing.assert_array_equal(ctx.read_props(), ref["props"])
+            np.testing.assert_array_equal(ctx.read_updates(), ref["updates"])
+            assert st["rounds"] == ref["stats"]["rounds"]
+            assert st["converged"] == 1
+            assert st["edges_scanned"] == ref["stats"]["edges_scanned"]
+            assert st["bytes_synced"] == ref["stats"]["bytes_synced"]
+            assert st["reference_bytes_moved"] == ref["stats"]["reference_bytes_moved"]
+
+
+@pytest.mark.parametrize("num_memory", [1, 3])
+def test_stage_api_matches_oracle_round_by_round(gpu, num_memory):
+    G = g.Graph.rmat(11, 8, symmetrize=True, weighted=True)
+    ro, ci, w = G.row_offsets, G.col_indices, G.weights
+    part = G.partition_edge_balanced(num_memory) if num_memory > 1 else None
+    with g.Context(G, part, num_memory=num_memory) as ctx:
+        for algo, oalgo in ALGOS:
+            ctx.set_algo(algo)
+            ctx.init()
+            r = 0
+            while True:
+                f = ctx.round()
+                r += 1
+                ref = O.run(oalgo, ro, ci, w, mirror=part, num_memory=num_memory, max_rounds=r)
+                np.testing.assert_array_equal(ctx.read_props(), ref["props"])
+                np.testing.assert_array_equal(ctx.read_updates(), ref["updates"])
+                if f == 0:
+                    break
+            assert r == ref["stats"]["rounds"]
+
+
+@pytest.mark.parametrize("num_memory", [1, 3])
+def test_pr_delta_close_to_oracle(gpu, num_memory):
+    G = g.Graph.rmat(14, 16)
+    ro, ci = G.row_offsets, G.col_indices
+    part = G.partition_edge_balanced(num_memory) if num_memory > 1 else None
+    with g.Context(G, part, num_memory=num_memory) as ctx:
+        ctx.set_algo(g.GRD_PR_DELTA)
+        ctx.init()
+        st = ctx.run()
+        ref = O.run(O.ORC_PR_DELTA, ro, ci, mirror=part, num_memory=num_memory)
+        got = ctx.read_ranks()
+        exp = ref["ranks"]
+        assert np.all(np.abs(got - exp) <= 2e-5 + 1e-4 * np.abs(exp))
+        assert abs(st["rounds"] - ref["stats"]["rounds"]) <= 2
+
+
+def test_cc_sssp_full_size_properties(gpu):
+    """RMAT-18 symmetric: CC against union-find, SSSP against BFS / Dijkstra."""
+    G = g.Graph.rmat(18, 16, symmetrize=True, weighted=True)
+    ro, ci, w = G.row_offsets, G.col_indices, G.weights
+    part = G.partition_edge_balanced(3)
+    with g.Context(G, part, num_memory=3) as ctx:
+        ctx.set_algo(g.GRD_CC)
+        ctx.init()
+        ctx.run()
+        np.testing.assert_array_equal(ctx.read_props(), O.cc_union_find(ro, ci))
+        ctx.set_algo(g.GRD_SSSP_HOP)
+        ctx.init()
+        ctx.run()
+        np.testing.assert_array_equal(ctx.read_props(), O.bfs(ro, ci, 0))
+        ctx.set_algo(g.GRD_SSSP_W)
+        ctx.init()
+        ctx.run()
+        np.testing.assert_array_equal(ctx.read_props(), O.dijkstra(ro, ci, w, 0))
+
+
+def test_edge_cases(gpu):
+    # single vertex, no edges
+    G = g.Graph.from_csr([0, 0], [])
+    with g.Context(G) as ctx:
+        ctx.set_algo(g.GRD_CC)
+        ctx.init()
+        st = ctx.run()
+        assert st["rounds"] == 1 and list(ctx.read_props()) == [0]
+    # isolated vertices + one edge; unreachable SSSP stays UINT32_MAX
+    G = g.Graph.from_edges(5, [1], [3], [7])
+    with g.Context(G) as ctx:
+        ctx.set_algo(g.GRD_SSSP_W, source=1)
+        ctx.init()
+        ctx.run()
+        assert list(ctx.read_props()) == [0xFFFFFFFF, 0, 0xFFFFFFFF, 7, 0xFFFFFFFF]
+    # round cap
+    G = g.Graph.grid(20)
+    with g.Context(G) as ctx:
+        ctx.set_algo(g.GRD_SSSP_HOP, max_rounds=3)
+        ctx.init()
+        st = ctx.run()
+        assert st["rounds"] == 3 and st["converged"] == 0
+        ctx.init()
+        with pytest.raises(g.GrdError):
+            ctx.run(strict=True)
