@@ -1,0 +1,387 @@
+"""Benchmark of the per-round graph operator on one GB300 (replicas for N>1).
+
+Workload (one step): connected components on the symmetrised graph and
+weighted SSSP (uint32 weights in [1,255], source 0) on the directed graph,
+both seeded RMAT scale 22 (4.19M vertices, edge factor 16, a/b/c/d =
+0.57/0.19/0.19/0.05, self-loops and duplicates removed), laid out as 1
+compute + 3 memory partitions (edge-balanced contiguous ranges) in HBM with
+bitvector-compacted sync.  Every step runs both algorithms to convergence
+from init().  The graphs are synthetic (no dataset is involved).
+
+value: Graph500-style GTEPS = (E_cc + E_sssp) / step time, inputs resident in
+HBM, CUDA events on the ctx streams.  e2e: the same through the C ABI with
+host buffers: every step uploads the partitioned CSR (pinned host memory),
+runs, and reads the results back.
+
+`--impl reference` times the reference algorithm on the host cores: the
+reference project cannot be built (its Galois/MPI dependencies are absent),
+so the arm runs the oracle's restatement of its round protocol with all host
+threads ("kind": "port").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GTEPS (PR/CC/SSSP, RMAT-24) & % HBM roofline; learned+batched vs plain GPU"
+SCALE, EF, NUM_MEMORY = 22, 16, 3
+RMAT_ABC = (0.57, 0.19, 0.19)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--scale", type=int, default=SCALE)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-pagerank", action="store_true")
+    ap.add_argument("--pr-scale", type=int, default=24)
+    return ap.parse_args()
+
+
+def bench_pagerank(g, args, local, hbm_peak, barrier, ws) -> dict:
+    """PageRank, RMAT-24 (ef16), 1C+3M: Jacobi with FP32 Kahan sums and an FP64
+    residual, until L1 residual / V < 1e-7 or 100 iterations."""
+    threads = max(1, (os.cpu_count() or 1) // ws)
+    a, b, c = RMAT_ABC
+    G = g.Graph.rmat(args.pr_scale, EF, a, b, c, seed=g.rmat_seed(args.pr_scale, EF), threads=threads)
+    part = G.partition_edge_balanced(NUM_MEMORY)
+    ctx = g.Context(G, part, num_memory=NUM_MEMORY, device=local)
+    ctx.set_algo(g.GRD_PR_PULL, max_rounds=100, tolerance=1e-7)
+    ctx.init()
+    ctx.run()  # warm-up
+    ctx.set_profiling(True)
+    reps = 2
+    stats = []
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx.init()
+        stats.append(ctx.run())
+    barrier()
+    dt = (time.perf_counter() - t0) / reps
+    st = stats[-1]
+    it = st["rounds"]
+    pull_ms = sum(s["stage_ms"][1] for s in stats) / reps
+    rounds_ms = sum(s["stage_ms"][4] for s in stats) / reps
+    S = sum(ctx.layout_info(p)[0] + ctx.layout_info(p)[1] for p in range(NUM_MEMORY))
+    # pull edge-map bytes per iteration: in_off + partial writes + dirty bits
+    # over the slots, index + contribution gather per in-edge
+    alg = it * (S * 8 + S / 8 + G.num_edges * 8)
+    ach = alg / (pull_ms / 1e3) / 1e9 if pull_ms else 0.0
+    ranks = ctx.read_ranks()
+    ctx.close()
+    return {
+        "workload": f"PageRank Jacobi (FP32 Kahan, FP64 residual), RMAT-{args.pr_scale} ef{EF}, 1C+{NUM_MEMORY}M, "
+                    "stop at L1 residual/V < 1e-7 or 100 iterations",
+        "num_vertices": G.num_vertices, "num_edges": G.num_edges, "iterations": it,
+        "converged": st["converged"], "last_residual_per_vertex": st["last_residual"],
+        "seconds_per_run": dt, "gteps": G.num_edges * it / dt / 1e9,
+        "ms_per_iteration": rounds_ms / max(it, 1),
+        "roofline": {"bound": "hbm", "kernel": "pull edge-map (k_pull_pr + k_pull_hub)", "achieved": ach,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None},
+        "_graph": G, "_ranks": ranks,
+    }
+
+
+def pr_fp64_check(pr: dict, cpu: dict) -> None:
+    """FP64 Jacobi on the host for the same iteration count (CPU-baseline
+    leg): reports its time and the GPU's max relative error against it."""
+    import numpy as np
+    from oracle import ffi as O
+    G = pr["_graph"]
+    t0 = time.perf_counter()
+    ref, it, _ = O.pr_jacobi_fp64_mt(G.row_offsets, G.col_indices, iters=pr["iterations"])
+    secs = time.perf_counter() - t0
+    got = pr["_ranks"].astype(np.float64)
+    both0 = (got == 0) & (ref == 0)
+    rel = np.where(both0, 0.0, np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300))
+    pr["max_rel_err_vs_fp64"] = float(rel.max())
+    cpu["pagerank_fp64"] = {"seconds": secs, "iterations": it, "threads": os.cpu_count(),
+                            "gteps": G.num_edges * it / secs / 1e9,
+                            "kind": "FP64 Jacobi restatement (oracle), all host threads"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_graphs(scale: int, threads: int):
+    import grudon_gb300 as g
+    a, b, c = RMAT_ABC
+    seed = g.rmat_seed(scale, EF)
+    G_cc = g.Graph.rmat(scale, EF, a, b, c, seed=seed, symmetrize=True, threads=threads)
+    G_ss = g.Graph.rmat(scale, EF, a, b, c, seed=seed, weighted=True, threads=threads)
+    return seed, G_cc, G_ss
+
+
+def cpu_baseline(G_cc, G_ss, p_cc, p_ss, steps: int = 1) -> dict:
+    """The oracle's restated round protocol, all host threads, run() only."""
+    from oracle import ffi as O
+    threads = os.cpu_count() or 1
+    L_cc = O.Layout(G_cc.row_offsets, G_cc.col_indices, mirror=p_cc, num_memory=NUM_MEMORY)
+    L_ss = O.Layout(G_ss.row_offsets, G_ss.col_indices, G_ss.weights, mirror=p_ss, num_memory=NUM_MEMORY)
+    t_total = 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        L_cc.run(O.ORC_CC, threads=threads)
+        L_ss.run(O.ORC_SSSP_W, threads=threads)
+        t_total += time.perf_counter() - t0
+    E = G_cc.num_edges + G_ss.num_edges
+    return {"value": steps * E / t_total / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
+            "seconds": t_total,
+            "sample": f"{steps} full step(s): CC + weighted SSSP to convergence on the same RMAT-{SCALE} graphs, "
+                      f"1C+{NUM_MEMORY}M, oracle restatement of the reference round protocol (reference "
+                      "unbuildable: Galois/MPI absent), {threads} host threads"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    seed, G_cc, G_ss = make_graphs(args.scale, 0)
+    p_cc = G_cc.partition_edge_balanced(NUM_MEMORY)
+    p_ss = G_ss.partition_edge_balanced(NUM_MEMORY)
+    from oracle import ffi as O
+    threads = os.cpu_count() or 1
+    L_cc = O.Layout(G_cc.row_offsets, G_cc.col_indices, mirror=p_cc, num_memory=NUM_MEMORY)
+    L_ss = O.Layout(G_ss.row_offsets, G_ss.col_indices, G_ss.weights, mirror=p_ss, num_memory=NUM_MEMORY)
+    for _ in range(args.warmup):
+        L_cc.run(O.ORC_CC, threads=threads)
+        L_ss.run(O.ORC_SSSP_W, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L_cc.run(O.ORC_CC, threads=threads)
+        L_ss.run(O.ORC_SSSP_W, threads=threads)
+    dt = time.perf_counter() - t0
+    E = G_cc.num_edges + G_ss.num_edges
+    value = args.steps * E / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": workload_config(args.scale, seed, G_cc, G_ss),
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
+                         "sample": f"each step: CC + weighted SSSP to convergence (full workload), "
+                                   f"{threads} host threads; reference itself unbuildable (Galois/MPI absent)"},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(scale, seed, G_cc, G_ss) -> dict:
+    return {
+        "workload": f"CC (symmetrised) + weighted SSSP (w in [1,255], source 0) to convergence, RMAT-{scale} "
+                    f"ef{EF} a/b/c/d .57/.19/.19/.05, 1 compute + {NUM_MEMORY} memory partitions, bitvector sync",
+        "scale": scale, "edge_factor": EF, "seed": seed, "num_vertices": G_cc.num_vertices,
+        "E_cc_symmetrised": G_cc.num_edges, "E_sssp": G_ss.num_edges,
+        "partitions": f"1C+{NUM_MEMORY}M edge-balanced contiguous",
+        "l2": "inputs larger than L2 (CSR indices 0.27-0.5 GB > 129 MB), no flush",
+    }
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import grudon_gb300 as g
+
+    threads = max(1, (os.cpu_count() or 1) // ws)
+    seed, G_cc, G_ss = make_graphs(args.scale, threads)
+    p_cc = G_cc.partition_edge_balanced(NUM_MEMORY)
+    p_ss = G_ss.partition_edge_balanced(NUM_MEMORY)
+    ctx_cc = g.Context(G_cc, p_cc, num_memory=NUM_MEMORY, device=local)
+    ctx_ss = g.Context(G_ss, p_ss, num_memory=NUM_MEMORY, device=local)
+    ctx_cc.set_algo(g.GRD_CC, direction=g.GRD_DIR_PUSH)
+    ctx_ss.set_algo(g.GRD_SSSP_W, direction=g.GRD_DIR_PUSH)
+    E = G_cc.num_edges + G_ss.num_edges
+
+    def step():
+        out = []
+        for c in (ctx_cc, ctx_ss):
+            c.init()
+            out.append(c.run())
+        return out
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    for c in (ctx_cc, ctx_ss):
+        c.set_profiling(True)
+
+    s_cc = torch.cuda.ExternalStream(ctx_cc.stream())
+    s_ss = torch.cuda.ExternalStream(ctx_ss.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    ev0.record(s_cc)
+    agg = {"edge_map_ms": 0.0, "fwd_ms": 0.0, "bwd_ms": 0.0, "update_ms": 0.0, "rounds_ms": 0.0,
+           "actives": 0, "edges": 0, "launches": 0, "rounds": [], "bytes_synced": 0}
+    for _ in range(args.steps):
+        for st, weighted in zip(step(), (False, True)):
+            agg["fwd_ms"] += st["stage_ms"][0]
+            agg["edge_map_ms"] += st["stage_ms"][1]
+            agg["bwd_ms"] += st["stage_ms"][2]
+            agg["update_ms"] += st["stage_ms"][3]
+            agg["rounds_ms"] += st["stage_ms"][4]
+            agg["actives"] += st["actives_total"]
+            agg["edges"] += st["edges_scanned"]
+            agg["launches"] += st["kernel_launches"]
+            agg["bytes_synced"] += st["bytes_synced"]
+            agg.setdefault("alg_bytes", 0)
+            agg["alg_bytes"] += st["actives_total"] * 12 + st["edges_scanned"] * (16 if weighted else 12)
+            agg["rounds"].append(st["rounds"])
+    ev1.record(s_ss)
+    barrier()
+    clk = clocks.stop()
+    dt_ms = ev0.elapsed_time(ev1)
+    if ws > 1:
+        t = torch.tensor([dt_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt_ms = float(t.item())
+    value = ws * args.steps * E / (dt_ms / 1e3) / 1e9
+
+    # End to end through the C ABI with host buffers.
+    for c in (ctx_cc, ctx_ss):
+        c.set_profiling(False)
+    barrier()
+    h2d = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for c in (ctx_cc, ctx_ss):
+            h2d += c.upload()
+            c.init()
+            c.run()
+            c.read_props()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": ws * args.steps * E / e2e_s / 1e9, "unit": "GTEPS",
+           "h2d_bytes_per_step": h2d // args.steps,
+           "d2h_bytes_per_step": 4 * (G_cc.num_vertices + G_ss.num_vertices)}
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = agg["alg_bytes"] / (agg["edge_map_ms"] / 1e3) / 1e9 if agg["edge_map_ms"] > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": "edge-map stage (k_push + k_hub_push)", "achieved": achieved,
+                "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None,
+                "edge_map_share_of_rounds": agg["edge_map_ms"] / agg["rounds_ms"] if agg["rounds_ms"] else None,
+                "stage_ms_per_step": {k: agg[k] / args.steps for k in
+                                      ("fwd_ms", "edge_map_ms", "bwd_ms", "update_ms", "rounds_ms")}}
+    pr = None
+    if not args.no_pagerank:
+        pr = bench_pagerank(g, args, local, hbm_peak, barrier, ws)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": workload_config(args.scale, seed, G_cc, G_ss) | {"parallelism": f"replicas x{ws}"},
+            "e2e": e2e, "gpu_launches": agg["launches"], "roofline": roofline, "clocks": clk,
+            "rounds_per_step": agg["rounds"][:2],
+            "edges_scanned_gteps": ws * agg["edges"] / (dt_ms / 1e3) / 1e9,
+        }
+        if ws == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(G_cc, G_ss, p_cc, p_ss)
+            if pr is not None:
+                pr_fp64_check(pr, line["cpu_baseline"])
+        if pr is not None:
+            pr.pop("_graph", None)
+            pr.pop("_ranks", None)
+            line["pagerank_rmat24"] = pr
+        print(json.dumps(line), flush=True)
+    ctx_cc.close()
+    ctx_ss.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -81,7 +81,24 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     if res.returncode != 0:
         raise RuntimeError(f"link failed\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    build_cli(verbose)
     return LIB
+
+
+CLI = BUILD / "grudon"
+
+
+def build_cli(verbose: bool = False) -> Path:
+    """The flag-compatible driver over the C++ plugin API (links the .so)."""
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, *CXX_FLAGS, "-I", str(INCLUDE), str(CSRC / "cli.cpp"), "-o", str(CLI), f"-L{BUILD}", "-lgrudon_gpu",
+           "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"cli build failed\n{res.stdout}\n{res.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -18,39 +18,27 @@ using namespace grd;
 
 static thread_local std::string g_create_error;
 
-#define CK(call)                                                                       \
-  do {                                                                                 \
-    cudaError_t e_ = (call);                                                           \
-    if (e_ != cudaSuccess) {                                                           \
-      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                   \
-      return GRD_E_CUDA;                                                               \
-    }                                                                                  \
-  } while (0)
-
-#define CK_LAUNCH()                                                                    \
-  do {                                                                                 \
-    cudaError_t e_ = cudaGetLastError();                                               \
-    if (e_ != cudaSuccess) {                                                           \
-      ctx->err = std::string("kernel launch: ") + cudaGetErrorString(e_);              \
-      return GRD_E_CUDA;                                                               \
-    }                                                                                  \
-  } while (0)
-
-namespace {
-
-template <class T>
-int dev_alloc(grd_ctx* ctx, T** p, size_t count) {
-  size_t bytes = sizeof(T) * std::max<size_t>(count, 1);
+int grd_dev_alloc_bytes(grd_ctx* ctx, void** p, size_t bytes) {
   void* d = nullptr;
-  cudaError_t e = cudaMalloc(&d, bytes);
+  cudaError_t e = cudaMalloc(&d, std::max<size_t>(bytes, 4));
   if (e != cudaSuccess) {
     ctx->err = "cudaMalloc(" + std::to_string(bytes) + " B): " + cudaGetErrorString(e);
     (void)cudaGetLastError();
     return e == cudaErrorMemoryAllocation ? GRD_E_OOM : GRD_E_CUDA;
   }
   ctx->allocs.push_back(d);
-  *p = static_cast<T*>(d);
+  *p = d;
   return GRD_OK;
+}
+
+namespace {
+
+template <class T>
+int dev_alloc(grd_ctx* ctx, T** p, size_t count) {
+  void* d = nullptr;
+  int rc = grd_dev_alloc_bytes(ctx, &d, sizeof(T) * std::max<size_t>(count, 1));
+  if (rc == GRD_OK) *p = static_cast<T*>(d);
+  return rc;
 }
 
 template <class T>
@@ -61,11 +49,8 @@ int upload(grd_ctx* ctx, T* dst, const std::vector<T>& src) {
   return GRD_OK;
 }
 
-#define TRY(x)                 \
-  do {                         \
-    int r_ = (x);              \
-    if (r_ != GRD_OK) return r_; \
-  } while (0)
+// Blocks of the degree-scan kernels (fixed grid, segments sized on device).
+uint32_t lbs_blocks(const grd_ctx* ctx) { return (uint32_t)ctx->num_sms * 4; }
 
 int alloc_and_upload(grd_ctx* ctx) {
   const Layout& L = ctx->L;
@@ -95,6 +80,7 @@ int alloc_and_upload(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, &st.UD, VW));
   TRY(dev_alloc(ctx, &st.mprop, S));
   TRY(dev_alloc(ctx, &st.mupd, S));
+  TRY(dev_alloc(ctx, &st.snap, S));
   TRY(dev_alloc(ctx, &st.FB, SW));
   TRY(dev_alloc(ctx, &st.MD, SW));
   TRY(dev_alloc(ctx, &st.FV, S));
@@ -104,6 +90,12 @@ int alloc_and_upload(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, &st.tile_off, T));
   TRY(dev_alloc(ctx, &st.tile_goff, T));
   TRY(dev_alloc(ctx, &st.part_cnt, M));
+  TRY(dev_alloc(ctx, &st.DP, S + 1));
+  TRY(dev_alloc(ctx, &st.RB, S));
+  TRY(dev_alloc(ctx, &st.SV, S));
+  TRY(dev_alloc(ctx, &st.chunk_start, E / LBS_CHUNK + 2));
+  TRY(dev_alloc(ctx, &st.blk_sum, lbs_blocks(ctx)));
+  TRY(dev_alloc(ctx, &st.blk_off, lbs_blocks(ctx)));
   TRY(dev_alloc(ctx, &st.counters, NUM_COUNTERS));
   CK(cudaMemsetAsync(st.counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, ctx->stream));
   return GRD_OK;
@@ -185,6 +177,16 @@ int check_ready(grd_ctx* ctx) {
 
 uint32_t grid_for(grd_ctx* ctx, uint32_t blocks_per_sm) { return (uint32_t)ctx->num_sms * blocks_per_sm; }
 
+// Dense rounds (reductions only, dirty set rebuilt by one linear pass) pay an
+// O(S) pass; sparse rounds pay a returned atomic per improving edge.  The
+// fixed rule takes the dense form when the frontier entering the round is at
+// least 1/32 of the slot space.  GRD_FMT_BITVEC / GRD_FMT_LIST force it.
+bool use_dense(const grd_ctx* ctx) {
+  if (ctx->params.frontier_format == GRD_FMT_BITVEC) return true;
+  if (ctx->params.frontier_format == GRD_FMT_LIST) return false;
+  return ctx->last_frontier * 32 >= ctx->g.S;
+}
+
 }  // namespace
 
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
@@ -205,13 +207,23 @@ int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
 int grd_enqueue_edge_map(grd_ctx* ctx) {
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
-    k_push<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-    if (ctx->g.num_hubs)
-      k_hub_push<A><<<std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8)), 256, 0, ctx->stream>>>(ctx->g,
-                                                                                                     ctx->st);
+    const uint32_t B = lbs_blocks(ctx);
+    k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(ctx->st, B);
+    k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
+    const bool dense = use_dense(ctx);
+    if (dense) {
+      k_push_lbs<A, true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      k_diff_dirty<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    } else {
+      k_push_lbs<A, false><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ctx->g.num_hubs) k_hub_push<A, false><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    }
     CK_LAUNCH();
     ctx->stats.push_rounds++;
-    ctx->stats.kernel_launches += ctx->g.num_hubs ? 2 : 1;
+    ctx->stats.kernel_launches += 4 + (ctx->g.num_hubs ? 1 : 0) + (dense ? 1 : 0);
     return GRD_OK;
   });
 }
@@ -226,7 +238,7 @@ int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate) {
     if (do_pack) {
       k_tile_count<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.tile_cnt);
       k_scan_tiles<<<1, 1024, 0, ctx->stream>>>(ctx->g, ctx->st, 0);
-      if (!fused) k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, nullptr, 0u, ctx->g, ctx->st, OpBwdPack<kPR>{});
+      if (!fused) k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, nullptr, 0u, ctx->g, ctx->st, OpBwdPack<A>{});
       ctx->stats.kernel_launches += fused ? 2 : 3;
     }
     if (do_aggregate) {
@@ -271,6 +283,7 @@ int grd_read_counters(grd_ctx* ctx) {
   ctx->stats.bytes_synced = ctx->h_counters[C_BYTES];
   ctx->stats.reference_bytes_moved = ctx->h_counters[C_REFBYTES];
   ctx->stats.actives_total += ctx->h_counters[C_ACTIVE];
+  ctx->last_frontier = ctx->h_counters[C_FRONTIER];
   if (ctx->h_counters[C_ERR]) {
     ctx->err = "device-side error code " + std::to_string(ctx->h_counters[C_ERR]);
     return ctx->h_counters[C_ERR] == 1 ? GRD_E_TIMEOUT : GRD_E_CUDA;
@@ -435,6 +448,7 @@ int grd_init(grd_ctx* ctx) {
   int rc = grd_enqueue_init(ctx, blocks);
   if (rc != GRD_OK) return rc;
   CK_LAUNCH();
+  TRY(grd_read_counters(ctx));  // initial |frontier| for the first round's mode
   ctx->stats = grd_stats{};
   ctx->stats.kernel_launches = 1;
   ctx->inited = true;
@@ -467,15 +481,20 @@ int grd_aggregate(grd_ctx* ctx) {
 
 int grd_update(grd_ctx* ctx, uint64_t* frontier_size) {
   TRY(check_ready(ctx));
+  uint64_t f;
+  ctx->stats.rounds++;
   if (ctx->algo == GRD_PR_PULL) {
+    // Every non-dangling vertex stays active; the run is over when the
+    // residual drops below the tolerance, reported as an empty frontier.
     TRY(grd_pull_stage(ctx, 4));
+    ctx->stats.converged = ctx->stats.last_residual < ctx->params.tolerance;
+    f = ctx->stats.converged ? 0 : ctx->h_counters[C_FRONTIER];
   } else {
     TRY(grd_enqueue_update(ctx));
+    TRY(grd_read_counters(ctx));
+    f = ctx->h_counters[C_FRONTIER];
+    ctx->stats.converged = (f == 0);
   }
-  TRY(grd_read_counters(ctx));
-  ctx->stats.rounds++;
-  const uint64_t f = ctx->h_counters[C_FRONTIER];
-  ctx->stats.converged = (f == 0);
   if (frontier_size) *frontier_size = f;
   return GRD_OK;
 }
@@ -510,6 +529,41 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
     ctx->err = "round cap reached with a non-empty frontier";
     return GRD_E_ROUND_CAP;
   }
+  return GRD_OK;
+}
+
+int grd_aggregate_values(grd_ctx* ctx, const uint32_t* gids, const uint32_t* values, size_t n) {
+  TRY(check_ready(ctx));
+  if (n == 0) return GRD_OK;
+  if (!gids || !values) return GRD_E_INVALID;
+  if (n > 0xFFFFFFFFull) {
+    ctx->err = "too many values in one call";
+    return GRD_E_INVALID;
+  }
+  for (size_t i = 0; i < n; ++i)
+    if (gids[i] >= ctx->L.V) {
+      ctx->err = "gid " + std::to_string(gids[i]) + " out of range";
+      return GRD_E_INVALID;
+    }
+  CK(cudaSetDevice(ctx->device));
+  if (ctx->agg_cap < n) {
+    void* p = nullptr;
+    TRY(grd_dev_alloc_bytes(ctx, &p, sizeof(uint32_t) * 2 * n));
+    ctx->agg_buf = static_cast<uint32_t*>(p);
+    ctx->agg_cap = n;
+  }
+  CK(cudaMemcpyAsync(ctx->agg_buf, gids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->agg_buf + n, values, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+  const uint32_t blocks = (uint32_t)std::min<size_t>((n + 255) / 256, grid_for(ctx, 8));
+  const int algo = ctx->algo == GRD_PR_PULL ? GRD_PR_DELTA : ctx->algo;
+  TRY(dispatch(algo, [&](auto a) -> int {
+    constexpr int A = decltype(a)::value;
+    k_aggregate_values<A><<<blocks, 256, 0, ctx->stream>>>(ctx->st, ctx->agg_buf, ctx->agg_buf + n, (uint32_t)n);
+    CK_LAUNCH();
+    return GRD_OK;
+  }));
+  ctx->stats.kernel_launches += 1;
+  CK(cudaStreamSynchronize(ctx->stream));  // caller's buffers may be reused
   return GRD_OK;
 }
 

@@ -15,6 +15,7 @@ struct PullState {
   double* h_residual = nullptr;   // pinned mirror
   grd::HubChunkD* in_hubs = nullptr;  // destination slots with long in-lists
   uint32_t num_in_hubs = 0;
+  uint64_t edges = 0;                 // in-edges read since init
 };
 
 struct grd_ctx {
@@ -34,12 +35,43 @@ struct grd_ctx {
   uint64_t upload_bytes = 0;
   bool in_edges_alloc = false;
   PullState pull;
+  uint64_t last_frontier = 0;  // |frontier| entering the next round
+  uint32_t* agg_buf = nullptr; // staging of grd_aggregate_values (gids, values)
+  size_t agg_cap = 0;
   bool profiling = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<void*> host_registered;  // layout arrays pinned for H2D uploads
 };
 
+// Error plumbing shared by the host translation units (expects a `ctx`).
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                   \
+      return GRD_E_CUDA;                                                               \
+    }                                                                                  \
+  } while (0)
+
+#define CK_LAUNCH()                                                                    \
+  do {                                                                                 \
+    cudaError_t e_ = cudaGetLastError();                                               \
+    if (e_ != cudaSuccess) {                                                           \
+      ctx->err = std::string("kernel launch: ") + cudaGetErrorString(e_);              \
+      return GRD_E_CUDA;                                                               \
+    }                                                                                  \
+  } while (0)
+
+#define TRY(x)                   \
+  do {                           \
+    int r_ = (x);                \
+    if (r_ != GRD_OK) return r_; \
+  } while (0)
+
 int grd_ctx_init_device(grd_ctx* ctx);
+int grd_dev_alloc_bytes(grd_ctx* ctx, void** p, size_t bytes);
+void grd_prof_mark(grd_ctx* ctx, int i);
+void grd_prof_collect(grd_ctx* ctx);
 void grd_ctx_release_extras(grd_ctx* ctx);
 int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks);
 int grd_upload_layout(grd_ctx* ctx);

@@ -19,7 +19,7 @@
 namespace grd {
 
 constexpr uint32_t FULL = 0xFFFFFFFFu;
-constexpr uint32_t K_TILE_SLOTS = 32768;
+constexpr uint32_t K_TILE_SLOTS = 8192;
 constexpr uint32_t K_TILE_WORDS = K_TILE_SLOTS / 32;
 constexpr uint32_t K_HUB_DEGREE = 2048;
 
@@ -34,6 +34,7 @@ enum Counter : int {
   C_TOTAL = 5,     // total set bits of the last compaction scan
   C_ERR = 6,       // first device-side error code (0 = none)
   C_PULL_EDGES = 7,
+  C_MEDGES = 8,    // edges of the load-balanced push this round (non-hub rows)
   NUM_COUNTERS = 16
 };
 
@@ -68,6 +69,7 @@ struct DevState {
   uint32_t* UD;
   uint32_t* mprop;
   uint32_t* mupd;
+  uint32_t* snap;  // [S] mupd as of its last send (dense-mode dirty detection)
   uint32_t* FB;
   uint32_t* FV;
   uint32_t* MD;
@@ -77,6 +79,12 @@ struct DevState {
   uint32_t* tile_off;
   uint32_t* tile_goff;
   uint32_t* part_cnt;
+  uint32_t* DP;           // [S+1] exclusive degree prefix over the active list
+  uint32_t* RB;           // [S] row start of each active (active-list order)
+  uint32_t* SV;           // [S] property of each active (active-list order)
+  uint32_t* chunk_start;  // [E/256+2] first active of each 256-edge chunk
+  uint32_t* blk_sum;      // [LBS blocks]
+  uint32_t* blk_off;      // [LBS blocks]
   unsigned long long* counters;
 };
 
@@ -164,11 +172,13 @@ __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t 
     if (lane_id() == 0 && i < g.V) {
       st.F[i >> 5] = m;
       st.UD[i >> 5] = 0;
+      if (m) atomicAdd(&st.counters[C_FRONTIER], (unsigned long long)__popc(m));
     }
     if (i < g.S) {
       const uint32_t x = (A == A_PR_DELTA || A == A_PR_PULL) ? 0u : 0xFFFFFFFFu;
       st.mprop[i] = x;
       st.mupd[i] = x;
+      st.snap[i] = x;
       if ((i & 31) == 0) {
         st.FB[i >> 5] = 0;
         st.MD[i >> 5] = 0;
@@ -187,18 +197,26 @@ static __global__ void __launch_bounds__(256) k_fwd_bits(DevGraph g, DevState st
   const uint32_t p = g.tile_part[t];
   const uint32_t base = g.part_base[p], nown = g.part_owned[p];
   const uint32_t t0 = t * K_TILE_SLOTS;
+  constexpr int U = 4;  // independent gathers in flight per thread
   uint32_t cnt = 0;
-  for (uint32_t i = threadIdx.x; i < K_TILE_SLOTS; i += blockDim.x) {
-    const uint32_t s = t0 + i;
-    uint32_t bit = 0;
-    if (s - base < nown) {
-      const uint32_t gid = __ldg(&g.slot_gid[s]);
-      bit = test_bit(st.F, gid);
+  for (uint32_t i = threadIdx.x; i < K_TILE_SLOTS; i += blockDim.x * U) {
+    uint32_t gid[U], fw[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t s = t0 + i + u * blockDim.x;
+      gid[u] = (s - base < nown) ? __ldg(&g.slot_gid[s]) : 0xFFFFFFFFu;
     }
-    const uint32_t m = __ballot_sync(FULL, bit);
-    if (lane_id() == 0) {
-      st.FB[s >> 5] = m;
-      cnt += __popc(m);
+#pragma unroll
+    for (int u = 0; u < U; ++u) fw[u] = gid[u] != 0xFFFFFFFFu ? st.F[gid[u] >> 5] : 0u;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t s = t0 + i + u * blockDim.x;
+      const uint32_t bit = gid[u] != 0xFFFFFFFFu ? (fw[u] >> (gid[u] & 31)) & 1u : 0u;
+      const uint32_t m = __ballot_sync(FULL, bit);
+      if (lane_id() == 0) {
+        st.FB[s >> 5] = m;
+        cnt += __popc(m);
+      }
     }
   }
   cnt = block_sum(cnt);
@@ -269,25 +287,47 @@ static __global__ void __launch_bounds__(1024) k_scan_tiles(DevGraph g, DevState
 }
 
 // ------------------------------------------------------------- compaction --
+// Fire-and-forget reductions (no returned value, so no round trip).
+__device__ __forceinline__ void red_or(uint32_t* a, uint32_t v) {
+  asm volatile("red.global.or.b32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_min(uint32_t* a, uint32_t v) {
+  asm volatile("red.global.min.u32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_add_f32(float* a, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(a), "f"(v) : "memory");
+}
+
 // Visits every set bit of `bits` over the tiles [tile_begin, tile_begin +
-// gridDim.x) in ascending slot order and calls op(p, slot, j, jg) where j is
-// the bit's rank inside its partition (packed value index) and jg its rank
-// over all partitions.  One warp owns 128 words; 32 words are loaded
-// coalesced, warp-scanned by popcount, then expanded one word at a time so
-// that lane l handles slot 32*word + l (coalesced value traffic).
+// gridDim.x) in ascending slot order with j = the bit's rank inside its
+// partition (packed value index) and jg = its rank over all partitions.
+// Phase A: each of the 8 warps loads its K_TILE_WORDS/8 words (coalesced),
+// scans their popcounts and writes the slot of every set bit to a warp-private
+// shared buffer in rank order (shuffles and shared stores only).  Phase B:
+// lanes walk the buffer 32 apart, U = 4 items per lane at a time, issuing all
+// loads of an item group (Op::gather) before any store (Op::scatter), so each
+// lane keeps 4 independent memory chains in flight.
+struct Payload {
+  uint32_t v, gid, cur, cmp;
+};
+
 template <class Op>
 __global__ void __launch_bounds__(256)
     k_compact(const uint32_t* __restrict__ bits, uint32_t* clear_bits, uint32_t tile_begin, DevGraph g,
               DevState st, Op op) {
+  constexpr int KW = K_TILE_WORDS / 256;  // 32-word groups per warp
+  constexpr int CAP = 32 * 32 * KW;       // slots owned by one warp
+  constexpr int U = 4;
   __shared__ uint32_t s_wsum[8];
+  __shared__ uint32_t s_slot[8][CAP];
   const uint32_t t = tile_begin + blockIdx.x;
   const uint32_t p = g.tile_part[t];
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-  const size_t wbase = (size_t)t * K_TILE_WORDS + warp * 128;
-  uint32_t x[4];
+  const size_t wbase = (size_t)t * K_TILE_WORDS + warp * (32 * KW);
+  uint32_t x[KW];
   uint32_t c = 0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < KW; ++k) {
     x[k] = __ldcg(&bits[wbase + k * 32 + lane]);
     c += __popc(x[k]);
   }
@@ -296,11 +336,13 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   uint32_t wb = 0;
   for (uint32_t i = 0; i < warp; ++i) wb += s_wsum[i];
-  uint32_t run = st.tile_off[t] + wb;
-  uint32_t grun = st.tile_goff[t] + wb;
+  const uint32_t run = st.tile_off[t] + wb;
+  const uint32_t grun = st.tile_goff[t] + wb;
   const uint32_t lt = (1u << lane) - 1u;
+  uint32_t* buf = s_slot[warp];
+  uint32_t n = 0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < KW; ++k) {
     const uint32_t xc = __popc(x[k]);
     const uint32_t incl = warp_incl_scan(xc);
     const uint32_t excl = incl - xc;
@@ -310,19 +352,32 @@ __global__ void __launch_bounds__(256)
         const uint32_t wj = __shfl_sync(FULL, x[k], j);
         if (wj == 0) continue;
         const uint32_t ej = __shfl_sync(FULL, excl, j);
-        if ((wj >> lane) & 1u) {
-          const uint32_t r = ej + __popc(wj & lt);
-          const uint32_t slot = t * K_TILE_SLOTS + (warp * 128 + k * 32 + j) * 32 + lane;
-          op(g, st, p, slot, run + r, grun + r);
-        }
+        if ((wj >> lane) & 1u) buf[n + ej + __popc(wj & lt)] = (uint32_t)(wbase + k * 32 + j) * 32 + lane;
       }
     }
-    run += ctot;
-    grun += ctot;
+    n += ctot;
+  }
+  __syncwarp();
+  for (uint32_t q0 = 0; q0 < n; q0 += 32 * U) {
+    uint32_t sl[U];
+    Payload pv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t q = q0 + u * 32 + lane;
+      if (q < n) {
+        sl[u] = buf[q];
+        pv[u] = op.gather(g, st, p, sl[u], run + q);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t q = q0 + u * 32 + lane;
+      if (q < n) op.scatter(g, st, p, sl[u], run + q, grun + q, pv[u]);
+    }
   }
   if (clear_bits) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < KW; ++k)
       if (x[k]) clear_bits[wbase + k * 32 + lane] = 0;
   }
 }
@@ -330,94 +385,163 @@ __global__ void __launch_bounds__(256)
 // Forward pack (compute side): packed value j of partition p is
 // vertex_properties of the j-th set bit (src/GraphAlgorithm.cpp:233-235).
 struct OpFwdPack {
-  __device__ __forceinline__ void operator()(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
-                                             uint32_t j, uint32_t) const {
-    st.FV[g.part_base[p] + j] = st.prop[g.slot_gid[slot]];
+  __device__ __forceinline__ Payload gather(const DevGraph& g, const DevState& st, uint32_t, uint32_t slot,
+                                            uint32_t) const {
+    return Payload{st.prop[__ldg(&g.slot_gid[slot])], 0, 0};
+  }
+  __device__ __forceinline__ void scatter(const DevGraph& g, const DevState& st, uint32_t p, uint32_t, uint32_t j,
+                                          uint32_t, const Payload& v) const {
+    st.FV[g.part_base[p] + j] = v.v;
   }
 };
 // Forward unpack (memory side, src/GraphAlgorithm.cpp:316-334): set() the
 // slot's property (the bitvector itself is the dirty set) and append the
 // slot to the active list.
 struct OpFwdUnpack {
-  __device__ __forceinline__ void operator()(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
-                                             uint32_t j, uint32_t jg) const {
-    st.mprop[slot] = st.FV[g.part_base[p] + j];
+  __device__ __forceinline__ Payload gather(const DevGraph& g, const DevState& st, uint32_t p, uint32_t,
+                                            uint32_t j) const {
+    return Payload{st.FV[g.part_base[p] + j], 0, 0};
+  }
+  __device__ __forceinline__ void scatter(const DevGraph&, const DevState& st, uint32_t, uint32_t slot, uint32_t,
+                                          uint32_t jg, const Payload& v) const {
+    st.mprop[slot] = v.v;
     st.AL[jg] = slot;
   }
 };
 // Fused forward pack + unpack (one pass; the wire buffer is still written).
 struct OpFwdXfer {
-  __device__ __forceinline__ void operator()(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
-                                             uint32_t j, uint32_t jg) const {
-    const uint32_t v = st.prop[g.slot_gid[slot]];
-    st.FV[g.part_base[p] + j] = v;
-    st.mprop[slot] = v;
+  __device__ __forceinline__ Payload gather(const DevGraph& g, const DevState& st, uint32_t, uint32_t slot,
+                                            uint32_t) const {
+    return Payload{st.prop[__ldg(&g.slot_gid[slot])], 0, 0};
+  }
+  __device__ __forceinline__ void scatter(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
+                                          uint32_t j, uint32_t jg, const Payload& v) const {
+    st.FV[g.part_base[p] + j] = v.v;
+    st.mprop[slot] = v.v;
     st.AL[jg] = slot;
   }
 };
+
 // Backward pack (memory side, src/GraphAlgorithm.cpp:388-393); PageRank
-// zeroes the sent entry (vertex_updates.clear(), :674-677).
-template <bool kClear>
+// zeroes the sent entry (vertex_updates.clear(), :674-677); the min
+// algorithms record the sent value as the dirty-detection snapshot.
+template <int A>
+__device__ __forceinline__ void retire_update(const DevState& st, uint32_t slot, uint32_t v) {
+  if (A == A_PR_DELTA)
+    st.mupd[slot] = 0;
+  else
+    st.snap[slot] = v;
+}
+
+template <int A>
 struct OpBwdPack {
-  __device__ __forceinline__ void operator()(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
-                                             uint32_t j, uint32_t) const {
-    st.BV[g.part_base[p] + j] = st.mupd[slot];
-    if (kClear) st.mupd[slot] = 0;
+  __device__ __forceinline__ Payload gather(const DevGraph&, const DevState& st, uint32_t, uint32_t slot,
+                                            uint32_t) const {
+    return Payload{st.mupd[slot], 0, 0};
+  }
+  __device__ __forceinline__ void scatter(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
+                                          uint32_t j, uint32_t, const Payload& v) const {
+    st.BV[g.part_base[p] + j] = v.v;
+    retire_update<A>(st, slot, v.v);
   }
 };
 
-// Compute-side aggregate of one received value (plugin aggregate()).
+// Compute-side aggregate of one received value (plugin aggregate()):
+// PageRank addUpdate, CC/SSSP minUpdate, marking the vertex_updates dirty bit.
 template <int A>
-__device__ __forceinline__ void aggregate_one(const DevState& st, uint32_t gid, uint32_t v) {
+__device__ __forceinline__ void aggregate_one(const DevState& st, uint32_t gid, uint32_t v, uint32_t cur) {
   if (A == A_PR_DELTA || A == A_PR_PULL) {
     // Partitions are aggregated by ordered launches and a gid occurs at most
     // once per partition, so this read-modify-write is race free and the
     // per-vertex summation order is partition 0, 1, ..., M-1.
-    st.upd[gid] = __float_as_uint(__fadd_rn(__uint_as_float(st.upd[gid]), __uint_as_float(v)));
-    set_dirty(st.UD, gid);
-  } else {
-    if (v < __ldcg(&st.upd[gid])) {
-      const uint32_t old = atomicMin(&st.upd[gid], v);
-      if (v < old) set_dirty(st.UD, gid);
-    }
+    st.upd[gid] = __float_as_uint(__fadd_rn(__uint_as_float(cur), __uint_as_float(v)));
+    red_or(st.UD + (gid >> 5), 1u << (gid & 31));
+  } else if (v < cur) {
+    const uint32_t old = atomicMin(&st.upd[gid], v);
+    if (v < old) red_or(st.UD + (gid >> 5), 1u << (gid & 31));
   }
 }
 
 template <int A>
+__device__ __forceinline__ uint32_t aggregate_peek(const DevState& st, uint32_t gid) {
+  return (A == A_PR_DELTA || A == A_PR_PULL) ? st.upd[gid] : __ldcg(&st.upd[gid]);
+}
+
+template <int A>
 struct OpAggregate {
-  __device__ __forceinline__ void operator()(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
-                                             uint32_t j, uint32_t) const {
-    aggregate_one<A>(st, g.slot_gid[slot], st.BV[g.part_base[p] + j]);
+  __device__ __forceinline__ Payload gather(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
+                                            uint32_t j) const {
+    const uint32_t gid = __ldg(&g.slot_gid[slot]);
+    return Payload{st.BV[g.part_base[p] + j], gid, aggregate_peek<A>(st, gid)};
+  }
+  __device__ __forceinline__ void scatter(const DevGraph&, const DevState& st, uint32_t, uint32_t, uint32_t,
+                                          uint32_t, const Payload& v) const {
+    aggregate_one<A>(st, v.gid, v.v, v.cur);
   }
 };
 // Fused backward pack + aggregate.
 template <int A>
 struct OpBwdXfer {
-  __device__ __forceinline__ void operator()(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
-                                             uint32_t j, uint32_t) const {
-    const uint32_t v = st.mupd[slot];
-    st.BV[g.part_base[p] + j] = v;
-    if (A == A_PR_DELTA) st.mupd[slot] = 0;
-    aggregate_one<A>(st, g.slot_gid[slot], v);
+  __device__ __forceinline__ Payload gather(const DevGraph& g, const DevState& st, uint32_t, uint32_t slot,
+                                            uint32_t) const {
+    const uint32_t gid = __ldg(&g.slot_gid[slot]);
+    return Payload{st.mupd[slot], gid, aggregate_peek<A>(st, gid)};
+  }
+  __device__ __forceinline__ void scatter(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
+                                          uint32_t j, uint32_t, const Payload& v) const {
+    st.BV[g.part_base[p] + j] = v.v;
+    retire_update<A>(st, slot, v.v);
+    aggregate_one<A>(st, v.gid, v.v, v.cur);
   }
 };
+
+// Host-supplied (gid, value) pairs (grd_aggregate_values).  A gid may repeat
+// within one call, so PageRank adds atomically here.
+template <int A>
+__global__ void __launch_bounds__(256) k_aggregate_values(DevState st, const uint32_t* gids, const uint32_t* vals,
+                                                          uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t gid = gids[i], v = vals[i];
+    if (A == A_PR_DELTA || A == A_PR_PULL) {
+      atomicAdd(reinterpret_cast<float*>(st.upd) + gid, __uint_as_float(v));
+      red_or(st.UD + (gid >> 5), 1u << (gid & 31));
+    } else {
+      const uint32_t old = atomicMin(&st.upd[gid], v);
+      if (v < old) red_or(st.UD + (gid >> 5), 1u << (gid & 31));
+    }
+  }
+}
 
 // -------------------------------------------------------------- edge map --
 // One relaxation (PropertyList::minUpdate / addUpdate,
 // include/DistributedGraph.hpp:103-130): the dirty bit is set when a min
-// lowers the value, and always for an add.
-template <int A>
-__device__ __forceinline__ void relax(const DevState& st, uint32_t d, uint32_t sval, uint32_t w) {
+// lowers the value, and always for an add.  `cur` is a prior read of
+// mupd[d] (a stale read is only ever larger, values never grow in a round).
+// Dense mode (kDense) issues reductions only and leaves the dirty set to
+// k_diff_dirty; sparse mode marks dirty bits as it goes.
+template <int A, bool kDense>
+__device__ __forceinline__ void relax_apply(const DevState& st, uint32_t d, uint32_t cand, uint32_t cur) {
   if (A == A_PR_DELTA) {
-    atomicAdd(reinterpret_cast<float*>(st.mupd) + d, __uint_as_float(sval));
-    set_dirty(st.MD, d);
-  } else {
-    const uint32_t cand = (A == A_SSSP_W) ? sat_add(sval, w) : sval;
-    if (cand < __ldcg(&st.mupd[d])) {
+    red_add_f32(reinterpret_cast<float*>(st.mupd) + d, __uint_as_float(cand));
+    if (!kDense) red_or(st.MD + (d >> 5), 1u << (d & 31));
+  } else if (cand < cur) {
+    if (kDense) {
+      red_min(st.mupd + d, cand);
+    } else {
       const uint32_t old = atomicMin(&st.mupd[d], cand);
-      if (cand < old) set_dirty(st.MD, d);
+      if (cand < old) red_or(st.MD + (d >> 5), 1u << (d & 31));
     }
   }
+}
+
+template <int A>
+__device__ __forceinline__ uint32_t relax_cand(uint32_t sval, uint32_t w) {
+  return A == A_SSSP_W ? sat_add(sval, w) : sval;
+}
+
+template <int A>
+__device__ __forceinline__ uint32_t relax_peek(const DevState& st, uint32_t d) {
+  return A == A_PR_DELTA ? 0u : __ldcg(&st.mupd[d]);
 }
 
 // Source value after the per-source transform (sssp.cpp:69: prop + 1).
@@ -426,59 +550,184 @@ __device__ __forceinline__ uint32_t source_value(uint32_t v) {
   return A == A_SSSP_HOP ? v + 1u : v;
 }
 
-// Push edge-map over the compacted active list (gen_updates).  Each warp
-// takes 32 actives, scans their degrees and walks the concatenation of their
-// rows 32 edges at a time; a lane locates its source by a 5-step binary search
-// over the scanned offsets, so consecutive lanes read consecutive edges.
-// Rows longer than K_HUB_DEGREE are skipped here and run by k_hub_push.
-template <int A>
-__global__ void __launch_bounds__(256) k_push(DevGraph g, DevState st) {
+// ---- load-balanced push (gen_updates over the compacted active list) ------
+// The edge-map runs in three steps so that every warp gets the same number of
+// edges whatever the degree skew: (1) per-block sums of the (hub-capped)
+// degrees of the active list, (2) one block scans those sums, (3) each block
+// writes the exclusive degree prefix DP[i] of its actives and, for every
+// 256-edge chunk boundary that falls inside a row, the chunk's first active
+// (chunk_start).  k_push_lbs then hands one 256-edge chunk to a warp.
+// Rows longer than K_HUB_DEGREE count as 0 here and run in k_hub_push.
+constexpr uint32_t LBS_CHUNK = 256;
+
+__device__ __forceinline__ uint32_t capped_degree(const DevGraph& g, uint32_t s) {
+  const uint32_t d = __ldg(&g.row_off[s + 1]) - __ldg(&g.row_off[s]);
+  return d > K_HUB_DEGREE ? 0u : d;
+}
+
+// Fixed grid: block b owns actives [b*seg, min(K,(b+1)*seg)), seg = ceil(K/B).
+__device__ __forceinline__ void lbs_segment(uint64_t K, uint32_t& b0, uint32_t& b1) {
+  const uint64_t seg = (K + gridDim.x - 1) / gridDim.x;
+  const uint64_t a = (uint64_t)blockIdx.x * seg;
+  b0 = (uint32_t)(a < K ? a : K);
+  b1 = (uint32_t)(a + seg < K ? a + seg : K);
+}
+
+static __global__ void __launch_bounds__(256) k_deg_reduce(DevGraph g, DevState st) {
   const uint64_t K = __ldcg(&st.counters[C_ACTIVE]);
-  const uint32_t lane = lane_id();
-  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-  unsigned long long scanned = 0;
-  for (uint64_t c = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; c < K;
-       c += warps * 32) {
-    const uint64_t i = c + lane;
-    uint32_t b = 0, deg = 0, sv = 0;
-    if (i < K) {
-      const uint32_t s = st.AL[i];
-      b = __ldg(&g.row_off[s]);
-      deg = __ldg(&g.row_off[s + 1]) - b;
-      if (deg > K_HUB_DEGREE) deg = 0;
-      sv = source_value<A>(st.mprop[s]);
+  uint32_t b0, b1;
+  lbs_segment(K, b0, b1);
+  uint32_t sum = 0;
+  for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) sum += capped_degree(g, st.AL[i]);
+  sum = block_sum(sum);
+  if (threadIdx.x == 0) st.blk_sum[blockIdx.x] = sum;
+}
+
+// One block: exclusive scan of the nb block sums; DP[K] = total edges m.
+static __global__ void __launch_bounds__(1024) k_scan_blocks(DevState st, uint32_t nb) {
+  __shared__ uint32_t s_w[32];
+  __shared__ uint32_t s_carry;
+  const uint32_t tid = threadIdx.x, lane = lane_id(), w = tid >> 5;
+  if (tid == 0) s_carry = 0;
+  __syncthreads();
+  for (uint32_t c0 = 0; c0 < nb; c0 += blockDim.x) {
+    const uint32_t i = c0 + tid;
+    const uint32_t v = i < nb ? st.blk_sum[i] : 0;
+    uint32_t incl = warp_incl_scan(v);
+    if (lane == 31) s_w[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+      const uint32_t x = s_w[lane];
+      s_w[lane] = warp_incl_scan(x) - x;
     }
-    const uint32_t incl = warp_incl_scan(deg);
-    const uint32_t excl = incl - deg;
-    const uint32_t total = __shfl_sync(FULL, incl, 31);
-    scanned += total;
-    for (uint32_t e0 = 0; e0 < total; e0 += 32) {
-      const uint32_t eid = e0 + lane;
-      uint32_t lo = 0;
+    __syncthreads();
+    incl += s_w[w];
+    const uint32_t carry = s_carry;
+    if (i < nb) st.blk_off[i] = carry + incl - v;
+    __syncthreads();
+    if (tid == blockDim.x - 1) s_carry = carry + incl;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const uint64_t K = __ldcg(&st.counters[C_ACTIVE]);
+    st.DP[K] = s_carry;
+    st.counters[C_MEDGES] = s_carry;
+    st.counters[C_EDGES] += s_carry;
+  }
+}
+
+static __global__ void __launch_bounds__(256) k_deg_down(DevGraph g, DevState st) {
+  __shared__ uint32_t s_w[8];
+  const uint64_t K = __ldcg(&st.counters[C_ACTIVE]);
+  uint32_t b0, b1;
+  lbs_segment(K, b0, b1);
+  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+  uint32_t run = st.blk_off[blockIdx.x];
+  for (uint32_t base = b0; base < b1; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t d = 0;
+    if (i < b1) {
+      const uint32_t s = st.AL[i];
+      const uint32_t r0 = __ldg(&g.row_off[s]);
+      d = __ldg(&g.row_off[s + 1]) - r0;
+      if (d > K_HUB_DEGREE) d = 0;
+      st.RB[i] = r0;                 // row start and source value in active
+      st.SV[i] = st.mprop[s];        // order: one-level loads in k_push_lbs
+    }
+    const uint32_t incl = warp_incl_scan(d);
+    if (lane == 31) s_w[w] = incl;
+    __syncthreads();
+    uint32_t wb = 0, tot = 0;
+    for (uint32_t k = 0; k < 8; ++k) {
+      const uint32_t x = s_w[k];
+      if (k < w) wb += x;
+      tot += x;
+    }
+    const uint32_t ex = run + wb + incl - d;
+    if (i < b1) {
+      st.DP[i] = ex;
+      if (d) {
+        const uint32_t c0 = (ex + LBS_CHUNK - 1) / LBS_CHUNK, c1 = (ex + d + LBS_CHUNK - 1) / LBS_CHUNK;
+        for (uint32_t c = c0; c < c1; ++c) st.chunk_start[c] = i;
+      }
+    }
+    run += tot;
+    __syncthreads();
+  }
+}
+
+// One warp per 256-edge chunk.  The warp loads a window of 32 consecutive
+// actives (their DP, row start and source value); each lane finds the source
+// of each of its edges by a 5-step shuffle binary search over the window, so
+// lanes read consecutive edge slots.  All 8 edges of a lane are loaded (index,
+// weight, current value) before any update is issued, keeping 8 independent
+// memory chains in flight per lane; the window slides until the chunk is done.
+template <int A, bool kDense>
+__global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
+  constexpr int B = LBS_CHUNK / 32;
+  const uint32_t K = (uint32_t)__ldcg(&st.counters[C_ACTIVE]);
+  const uint32_t m = (uint32_t)__ldcg(&st.counters[C_MEDGES]);
+  const uint32_t lane = lane_id();
+  const uint32_t nchunks = (m + LBS_CHUNK - 1) / LBS_CHUNK;
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
+    uint32_t e = c * LBS_CHUNK;
+    const uint32_t e_end = min(m, e + LBS_CHUNK);
+    uint32_t i0 = st.chunk_start[c];
+    while (e < e_end) {
+      const uint32_t idx = i0 + lane;
+      uint32_t dpl = m, dpe = m, rb = 0, sv = 0;
+      if (idx < K) {
+        dpl = st.DP[idx];
+        dpe = st.DP[idx + 1];
+        rb = st.RB[idx];
+        sv = source_value<A>(st.SV[idx]);
+      }
+      const uint32_t wend = min(e_end, __shfl_sync(FULL, dpe, 31));
+      uint32_t dst[B], cand[B], cur[B];
 #pragma unroll
-      for (uint32_t step = 16; step; step >>= 1) {
-        const uint32_t cand = lo + step;
-        const uint32_t xe = __shfl_sync(FULL, excl, cand & 31);
-        if (cand < 32 && xe <= eid) lo = cand;
+      for (int k = 0; k < B; ++k) {
+        const uint32_t eid = e + k * 32 + lane;
+        uint32_t lo = 0;
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1) {
+          const uint32_t cnd = lo + step;
+          const uint32_t x = __shfl_sync(FULL, dpl, cnd);
+          if (x <= eid) lo = cnd;
+        }
+        const uint32_t sd = __shfl_sync(FULL, dpl, lo);
+        const uint32_t sr = __shfl_sync(FULL, rb, lo);
+        const uint32_t ssv = __shfl_sync(FULL, sv, lo);
+        dst[k] = 0xFFFFFFFFu;
+        cand[k] = ssv;
+        if (eid < wend) {
+          const uint32_t ed = sr + (eid - sd);
+          dst[k] = __ldg(&g.col[ed]);
+          if (A == A_SSSP_W) cand[k] = relax_cand<A>(ssv, __ldg(&g.wgt[ed]));
+        }
       }
-      const uint32_t sb = __shfl_sync(FULL, b, lo);
-      const uint32_t se = __shfl_sync(FULL, excl, lo);
-      const uint32_t ssv = __shfl_sync(FULL, sv, lo);
-      if (eid < total) {
-        const uint32_t e = sb + (eid - se);
-        const uint32_t d = __ldg(&g.col[e]);
-        const uint32_t w = (A == A_SSSP_W) ? __ldg(&g.wgt[e]) : 0u;
-        relax<A>(st, d, ssv, w);
-      }
+#pragma unroll
+      for (int k = 0; k < B; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek<A>(st, dst[k]) : 0u;
+#pragma unroll
+      for (int k = 0; k < B; ++k)
+        if (dst[k] != 0xFFFFFFFFu) relax_apply<A, kDense>(st, dst[k], cand[k], cur[k]);
+      e = wend;
+      i0 += 32;
     }
   }
-  if (lane == 0 && scanned) atomicAdd(&st.counters[C_EDGES], scanned);
 }
 
 // Hub rows: static work items of at most 4096 edges; a block runs an item
 // when its row is active this round (bit set in the forward bitvector) and
 // reads the aligned interior of the row with 128-bit loads.
-template <int A>
+template <int A, bool kDense>
+__device__ __forceinline__ void hub_edge(const DevGraph& g, const DevState& st, uint32_t e, uint32_t sv) {
+  const uint32_t d = __ldg(&g.col[e]);
+  const uint32_t c = relax_cand<A>(sv, A == A_SSSP_W ? __ldg(&g.wgt[e]) : 0u);
+  relax_apply<A, kDense>(st, d, c, relax_peek<A>(st, d));
+}
+
+template <int A, bool kDense>
 __global__ void __launch_bounds__(256) k_hub_push(DevGraph g, DevState st) {
   unsigned long long scanned = 0;
   for (uint32_t c = blockIdx.x; c < g.num_hubs; c += gridDim.x) {
@@ -487,24 +736,46 @@ __global__ void __launch_bounds__(256) k_hub_push(DevGraph g, DevState st) {
     const uint32_t sv = source_value<A>(st.mprop[h.slot]);
     const uint32_t a0 = min(h.e1, (h.e0 + 3u) & ~3u);
     const uint32_t a1 = max(a0, h.e1 & ~3u);
-    for (uint32_t e = h.e0 + threadIdx.x; e < a0; e += blockDim.x)
-      relax<A>(st, __ldg(&g.col[e]), sv, A == A_SSSP_W ? __ldg(&g.wgt[e]) : 0u);
+    for (uint32_t e = h.e0 + threadIdx.x; e < a0; e += blockDim.x) hub_edge<A, kDense>(g, st, e, sv);
     const uint4* c4 = reinterpret_cast<const uint4*>(g.col);
     const uint4* w4 = reinterpret_cast<const uint4*>(g.wgt);
     for (uint32_t q = (a0 >> 2) + threadIdx.x; q < (a1 >> 2); q += blockDim.x) {
       const uint4 d = __ldg(&c4[q]);
       uint4 w = make_uint4(0, 0, 0, 0);
       if (A == A_SSSP_W) w = __ldg(&w4[q]);
-      relax<A>(st, d.x, sv, w.x);
-      relax<A>(st, d.y, sv, w.y);
-      relax<A>(st, d.z, sv, w.z);
-      relax<A>(st, d.w, sv, w.w);
+      const uint32_t c0 = relax_cand<A>(sv, w.x), c1 = relax_cand<A>(sv, w.y);
+      const uint32_t c2 = relax_cand<A>(sv, w.z), c3 = relax_cand<A>(sv, w.w);
+      const uint32_t p0 = relax_peek<A>(st, d.x), p1 = relax_peek<A>(st, d.y);
+      const uint32_t p2 = relax_peek<A>(st, d.z), p3 = relax_peek<A>(st, d.w);
+      relax_apply<A, kDense>(st, d.x, c0, p0);
+      relax_apply<A, kDense>(st, d.y, c1, p1);
+      relax_apply<A, kDense>(st, d.z, c2, p2);
+      relax_apply<A, kDense>(st, d.w, c3, p3);
     }
-    for (uint32_t e = a1 + threadIdx.x; e < h.e1; e += blockDim.x)
-      relax<A>(st, __ldg(&g.col[e]), sv, A == A_SSSP_W ? __ldg(&g.wgt[e]) : 0u);
+    for (uint32_t e = a1 + threadIdx.x; e < h.e1; e += blockDim.x) hub_edge<A, kDense>(g, st, e, sv);
     if (threadIdx.x == 0) scanned += h.e1 - h.e0;
   }
   if (threadIdx.x == 0 && scanned) atomicAdd(&st.counters[C_EDGES], scanned);
+}
+
+// Dense-mode dirty set: a slot is dirty when its running min dropped below
+// the snapshot taken at its last send (CC/SSSP), or when it received any
+// PageRank contribution (the entry is zeroed after every send and every
+// contribution is positive).  Rebuilds every word of MD.
+template <int A>
+__global__ void __launch_bounds__(256) k_diff_dirty(DevGraph g, DevState st) {
+  for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.S; s += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = st.mupd[s];
+    bool dirty;
+    if (A == A_PR_DELTA) {
+      dirty = a != 0u;
+    } else {
+      const uint32_t b = st.snap[s];
+      dirty = a < b;
+    }
+    const uint32_t m = __ballot_sync(FULL, dirty);
+    if (lane_id() == 0) st.MD[s >> 5] = m;
+  }
 }
 
 // ------------------------------------------------------------------ update --

@@ -210,6 +210,9 @@ void build_in_edges(Layout& L) {
       if (L.weighted) L.in_wgt[o] = L.wgt[i];
     }
   }
+  L.in_hubs.clear();
+  for (uint64_t s = 0; s < S; ++s)
+    if (L.in_off[s + 1] - L.in_off[s] > PULL_HUB) L.in_hubs.push_back(HubChunk{(uint32_t)s, L.in_off[s], L.in_off[s + 1]});
 }
 
 }  // namespace grd

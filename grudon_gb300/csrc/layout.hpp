@@ -19,11 +19,12 @@
 
 namespace grd {
 
-constexpr uint32_t TILE_SLOTS = 32768;      // slots per compaction tile
+constexpr uint32_t TILE_SLOTS = 8192;       // slots per compaction tile
 constexpr uint32_t TILE_WORDS = TILE_SLOTS / 32;  // u32 bitvector words
 constexpr uint32_t INVALID = 0xFFFFFFFFu;
 constexpr uint32_t HUB_DEGREE = 2048;       // rows above this go to hub chunks
 constexpr uint32_t HUB_CHUNK = 4096;        // edges per hub work item
+constexpr uint32_t PULL_HUB = 1024;         // in-lists above this pull per block
 
 struct HubChunk {
   uint32_t slot;   // global slot of the hub row
@@ -52,6 +53,7 @@ struct Layout {
   std::vector<uint32_t> in_off;  // [S+1]
   std::vector<uint32_t> in_src;  // [E]
   std::vector<uint32_t> in_wgt;  // [E]
+  std::vector<HubChunk> in_hubs; // destinations with more than PULL_HUB in-edges
 
   std::vector<HubChunk> hubs;        // static hub work items (all partitions)
   std::vector<uint32_t> tile_part;   // [S/TILE_SLOTS] partition of each tile

@@ -140,6 +140,13 @@ int grd_sync_bwd(grd_ctx* ctx);
 int grd_aggregate(grd_ctx* ctx);
 /* Applies update_frontier + apply_updates; *frontier_size = |frontier|. */
 int grd_update(grd_ctx* ctx, uint64_t* frontier_size);
+/* Aggregates n caller-supplied (gid, value) pairs into the compute-side
+ * vertex_updates with the algorithm's aggregate operator (PR add, CC/SSSP
+ * min), marking them dirty for the next grd_update — the batch form of the
+ * plugin's aggregate(lid, value) (pr.cpp:149-153, cc.cpp:109-113,
+ * sssp.cpp:115-119).  Values are 32-bit (float bits for PageRank). */
+int grd_aggregate_values(grd_ctx* ctx, const uint32_t* gids,
+                         const uint32_t* values, size_t n);
 
 /* Full run: init() already called; loops rounds until the frontier is empty
  * or params.max_rounds.  flags: GRD_RUN_STRICT. */

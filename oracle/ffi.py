@@ -37,6 +37,13 @@ def lib() -> C.CDLL:
         L.orc_run.argtypes = [C.c_int, C.c_uint32, C.c_uint64, u64p, u32p, u32p, u32p, C.c_uint32, C.c_uint32,
                               C.c_uint32, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.POINTER(orc_stats)]
+        L.orc_layout_create.restype = C.c_void_p
+        L.orc_layout_create.argtypes = [C.c_uint32, u64p, u32p, u32p, u32p, C.c_uint32]
+        L.orc_layout_free.restype = None
+        L.orc_layout_free.argtypes = [C.c_void_p]
+        L.orc_run_layout.restype = C.c_int
+        L.orc_run_layout.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_int,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(orc_stats)]
         L.orc_layout_slots.restype = C.c_uint32
         L.orc_layout_slots.argtypes = [C.c_uint32, u64p, u32p, u32p, C.c_uint32, C.c_uint32, u32p, C.c_uint32, u32p]
         L.orc_bfs.restype = None
@@ -48,6 +55,9 @@ def lib() -> C.CDLL:
         L.orc_pr_jacobi_fp64.restype = C.c_uint32
         L.orc_pr_jacobi_fp64.argtypes = [C.c_uint32, u64p, u32p, C.c_double, C.c_uint32, C.c_double,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_pr_jacobi_fp64_mt.restype = C.c_uint32
+        L.orc_pr_jacobi_fp64_mt.argtypes = [C.c_uint32, u64p, u32p, C.c_double, C.c_uint32, C.c_double, C.c_int,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -85,6 +95,40 @@ def run(algo: int, ro, col, w=None, mirror=None, num_memory: int = 1, source: in
     if algo == ORC_PR_DELTA:
         out["ranks"] = ranks
     return out
+
+
+class Layout:
+    """Prebuilt restated layout, so timing covers run() only."""
+
+    def __init__(self, ro, col, w=None, mirror=None, num_memory: int = 1):
+        ro, col, w = _csr(ro, col, w)
+        self.V = len(ro) - 1
+        self._keep = (ro, col, w)
+        mir = None if mirror is None else np.ascontiguousarray(mirror, dtype=np.uint32)
+        self._h = lib().orc_layout_create(self.V, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), _p32(w),
+                                          _p32(mir), num_memory)
+        if not self._h:
+            raise ValueError("oracle rejected the layout arguments")
+
+    def run(self, algo: int, source: int = 0, max_rounds: int = 1000, damping: float = 0.85, tol: float = 1e-6,
+            threads: int = 1) -> dict:
+        dt = np.float32 if algo == ORC_PR_DELTA else np.uint32
+        props = np.zeros(self.V, dtype=dt)
+        upd = np.zeros(self.V, dtype=dt)
+        ranks = np.zeros(self.V, dtype=np.float32)
+        st = orc_stats()
+        rc = lib().orc_run_layout(self._h, algo, source, max_rounds, damping, tol, threads,
+                                  props.ctypes.data_as(C.c_void_p), ranks.ctypes.data_as(C.c_void_p),
+                                  upd.ctypes.data_as(C.c_void_p), C.byref(st))
+        if rc != 0:
+            raise ValueError("oracle rejected the run arguments")
+        return {"props": props, "updates": upd, "ranks": ranks,
+                "stats": {f: getattr(st, f) for f, _ in orc_stats._fields_}}
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_layout_free(self._h)
+            self._h = None
 
 
 def layout_slots(ro, col, mirror, num_memory: int, part: int):
@@ -130,4 +174,15 @@ def pr_jacobi_fp64(ro, col, damping: float = 0.85, iters: int = 100, tol: float 
     res = C.c_double()
     it = lib().orc_pr_jacobi_fp64(V, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), damping, iters, tol,
                                   pr.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res))
+    return pr, int(it), float(res.value)
+
+
+def pr_jacobi_fp64_mt(ro, col, damping: float = 0.85, iters: int = 100, tol: float = 0.0, threads: int = 0):
+    ro, col, _ = _csr(ro, col)
+    V = len(ro) - 1
+    pr = np.zeros(V, dtype=np.float64)
+    res = C.c_double()
+    it = lib().orc_pr_jacobi_fp64_mt(V, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), damping, iters, tol,
+                                     threads or (os.cpu_count() or 1), pr.ctypes.data_as(C.POINTER(C.c_double)),
+                                     C.byref(res))
     return pr, int(it), float(res.value)

@@ -512,17 +512,33 @@ struct orc_stats {
 // (PR only).  threads == 1 gives the deterministic order (ascending lids,
 // edges in row order, partitions ascending); threads > 1 mirrors the
 // reference's concurrent do_all with atomic CAS updates.
-int orc_run(int algo, uint32_t V, uint64_t E, const uint64_t* ro, const uint32_t* col, const uint32_t* w,
-            const uint32_t* mirror, uint32_t M, uint32_t source, uint32_t max_rounds, double damping, double tol,
-            int threads, void* props_out, float* ranks_out, void* updates_out, orc_stats* st) {
-  (void)E;
-  if (M == 0 || !ro || !st) return -1;
-  if ((algo == ORC_SSSP_W) && !w) return -1;
-  if ((algo == ORC_SSSP_HOP || algo == ORC_SSSP_W) && source >= V) return -1;
-  for (uint32_t g = 0; mirror && g < V; ++g)
-    if (mirror[g] >= M) return -1;
+struct orc_layout {
   Layout L;
-  build(L, V, ro, col, w, mirror, M);
+  bool weighted;
+};
+
+// Builds the partitioned layout once (the reference's setup, excluded from
+// its run() timing); NULL on invalid arguments.
+orc_layout* orc_layout_create(uint32_t V, const uint64_t* ro, const uint32_t* col, const uint32_t* w,
+                              const uint32_t* mirror, uint32_t M) {
+  if (M == 0 || !ro) return nullptr;
+  for (uint32_t g = 0; mirror && g < V; ++g)
+    if (mirror[g] >= M) return nullptr;
+  orc_layout* h = new orc_layout();
+  build(h->L, V, ro, col, w, mirror, M);
+  h->weighted = w != nullptr;
+  return h;
+}
+
+void orc_layout_free(orc_layout* h) { delete h; }
+
+// Runs init() + run() of one algorithm on a prebuilt layout.
+int orc_run_layout(const orc_layout* h, int algo, uint32_t source, uint32_t max_rounds, double damping, double tol,
+                   int threads, void* props_out, float* ranks_out, void* updates_out, orc_stats* st) {
+  if (!h || !st) return -1;
+  const Layout& L = h->L;
+  if ((algo == ORC_SSSP_W) && !h->weighted) return -1;
+  if ((algo == ORC_SSSP_HOP || algo == ORC_SSSP_W) && source >= L.V) return -1;
   Pool pool(threads);
   Stats s{};
   switch (algo) {
@@ -551,6 +567,17 @@ int orc_run(int algo, uint32_t V, uint64_t E, const uint64_t* ro, const uint32_t
   st->bytes_synced = s.bytes_synced;
   st->reference_bytes_moved = s.reference_bytes_moved;
   return 0;
+}
+
+int orc_run(int algo, uint32_t V, uint64_t E, const uint64_t* ro, const uint32_t* col, const uint32_t* w,
+            const uint32_t* mirror, uint32_t M, uint32_t source, uint32_t max_rounds, double damping, double tol,
+            int threads, void* props_out, float* ranks_out, void* updates_out, orc_stats* st) {
+  (void)E;
+  orc_layout* h = orc_layout_create(V, ro, col, w, mirror, M);
+  if (!h) return -1;
+  int rc = orc_run_layout(h, algo, source, max_rounds, damping, tol, threads, props_out, ranks_out, updates_out, st);
+  orc_layout_free(h);
+  return rc;
 }
 
 // Translation-slot order of memory partition p (owned gids ascending, then
@@ -654,6 +681,58 @@ uint32_t orc_pr_jacobi_fp64(uint32_t V, const uint64_t* ro, const uint32_t* col,
       pr[v] = nv;
     }
     res /= (double)V;
+    ++it;
+    if (tol > 0 && res < tol) break;
+  }
+  if (residual_out) *residual_out = res;
+  return it;
+}
+
+// Same iteration as orc_pr_jacobi_fp64, parallel over destinations (in-edge
+// lists, each summed in ascending source order, so the result does not
+// depend on the thread count).  Used as the FP64 reference at full size.
+uint32_t orc_pr_jacobi_fp64_mt(uint32_t V, const uint64_t* ro, const uint32_t* col, double d, uint32_t iters,
+                               double tol, int threads, double* pr, double* residual_out) {
+  std::vector<uint64_t> in_off((size_t)V + 1, 0);
+  for (uint64_t i = 0; i < ro[V]; ++i) in_off[col[i] + 1]++;
+  for (uint32_t v = 0; v < V; ++v) in_off[v + 1] += in_off[v];
+  std::vector<uint32_t> in_src(ro[V] ? ro[V] : 1);
+  {
+    std::vector<uint64_t> cur(in_off.begin(), in_off.end() - 1);
+    for (uint32_t u = 0; u < V; ++u)
+      for (uint64_t i = ro[u]; i < ro[u + 1]; ++i) in_src[cur[col[i]]++] = u;
+  }
+  Pool pool(threads);
+  std::vector<double> contrib(V);
+  for (uint32_t v = 0; v < V; ++v) pr[v] = (ro[v + 1] > ro[v]) ? (1.0 - d) : 0.0;
+  uint32_t it = 0;
+  double res = 0;
+  const int nt = pool.size();
+  std::vector<double> part(nt > 0 ? 1024 : 1);
+  while (it < iters) {
+    pool.run(V, 65536, [&](uint64_t b, uint64_t e) {
+      for (uint64_t v = b; v < e; ++v) {
+        uint64_t deg = ro[v + 1] - ro[v];
+        contrib[v] = deg ? d * pr[v] / (double)deg : 0.0;
+      }
+    });
+    std::atomic<uint64_t> res_bits{0};
+    std::mutex mu;
+    double res_acc = 0;
+    pool.run(V, 65536, [&](uint64_t b, uint64_t e) {
+      double local = 0;
+      for (uint64_t v = b; v < e; ++v) {
+        double acc = 0;
+        for (uint64_t i = in_off[v]; i < in_off[v + 1]; ++i) acc += contrib[in_src[i]];
+        double nv = ((ro[v + 1] > ro[v]) ? (1.0 - d) : 0.0) + acc;
+        local += std::fabs(nv - pr[v]);
+        pr[v] = nv;
+      }
+      std::lock_guard<std::mutex> g(mu);
+      res_acc += local;
+    });
+    (void)res_bits;
+    res = res_acc / (double)V;
     ++it;
     if (tol > 0 && res < tol) break;
   }

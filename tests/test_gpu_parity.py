@@ -24,15 +24,19 @@ GRAPHS = {
 }
 
 
+FORMATS = [g.GRD_FMT_AUTO, g.GRD_FMT_BITVEC, g.GRD_FMT_LIST]
+
+
 @pytest.mark.parametrize("num_memory", [1, 3])
 @pytest.mark.parametrize("name", list(GRAPHS))
-def test_min_algorithms_bit_exact(gpu, name, num_memory):
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_min_algorithms_bit_exact(gpu, name, num_memory, fmt):
     G = GRAPHS[name]()
     ro, ci, w = G.row_offsets, G.col_indices, G.weights
     part = G.partition_edge_balanced(num_memory) if num_memory > 1 else None
     with g.Context(G, part, num_memory=num_memory) as ctx:
         for algo, oalgo in ALGOS:
-            ctx.set_algo(algo)
+            ctx.set_algo(algo, frontier_format=fmt)
             ctx.init()
             st = ctx.run()
             ref = O.run(oalgo, ro, ci, w, mirror=part, num_memory=num_memory)
@@ -67,12 +71,13 @@ def test_stage_api_matches_oracle_round_by_round(gpu, num_memory):
 
 
 @pytest.mark.parametrize("num_memory", [1, 3])
-def test_pr_delta_close_to_oracle(gpu, num_memory):
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_pr_delta_close_to_oracle(gpu, num_memory, fmt):
     G = g.Graph.rmat(14, 16)
     ro, ci = G.row_offsets, G.col_indices
     part = G.partition_edge_balanced(num_memory) if num_memory > 1 else None
     with g.Context(G, part, num_memory=num_memory) as ctx:
-        ctx.set_algo(g.GRD_PR_DELTA)
+        ctx.set_algo(g.GRD_PR_DELTA, frontier_format=fmt)
         ctx.init()
         st = ctx.run()
         ref = O.run(O.ORC_PR_DELTA, ro, ci, mirror=part, num_memory=num_memory)
@@ -127,3 +132,49 @@ def test_edge_cases(gpu):
         ctx.init()
         with pytest.raises(g.GrdError):
             ctx.run(strict=True)
+
+
+def _max_rel_err(got, exp):
+    got = np.asarray(got, dtype=np.float64)
+    both_zero = (got == 0) & (exp == 0)
+    rel = np.abs(got - exp) / np.maximum(np.abs(exp), 1e-300)
+    return float(np.max(np.where(both_zero, 0.0, rel)))
+
+
+@pytest.mark.parametrize("num_memory", [1, 3])
+def test_pr_pull_vs_fp64_oracle(gpu, num_memory):
+    """FP32 Kahan pull PageRank within max relative error 1e-5 of FP64 Jacobi
+    run for the same number of iterations (the config-3 accuracy bar)."""
+    G = g.Graph.rmat(15, 16)
+    ro, ci = G.row_offsets, G.col_indices
+    part = G.partition_edge_balanced(num_memory) if num_memory > 1 else None
+    with g.Context(G, part, num_memory=num_memory) as ctx:
+        ctx.set_algo(g.GRD_PR_PULL, max_rounds=40, tolerance=0.0)
+        ctx.init()
+        st = ctx.run()
+        assert st["rounds"] == 40 and st["converged"] == 0
+        ref, it, res = O.pr_jacobi_fp64(ro, ci, iters=40)
+        assert it == 40
+        assert _max_rel_err(ctx.read_ranks(), ref) <= 1e-5
+        assert abs(st["last_residual"] - res) <= 1e-3 * res + 1e-12
+        assert st["edges_scanned"] == 40 * G.num_edges
+
+
+def test_pr_pull_converges_and_stage_api(gpu):
+    G = g.Graph.rmat(12, 8)
+    ro, ci = G.row_offsets, G.col_indices
+    part = G.partition_edge_balanced(3)
+    with g.Context(G, part, num_memory=3) as ctx:
+        ctx.set_algo(g.GRD_PR_PULL, max_rounds=100, tolerance=1e-7)
+        ctx.init()
+        st = ctx.run()
+        ref, it, _ = O.pr_jacobi_fp64(ro, ci, iters=100, tol=1e-7)
+        assert st["converged"] == 1 and abs(st["rounds"] - it) <= 1
+        full = ctx.read_ranks()
+        # the same iterations through the per-stage API
+        ctx.init()
+        r = 0
+        while ctx.round() != 0:
+            r += 1
+        assert r + 1 == st["rounds"]
+        np.testing.assert_array_equal(ctx.read_ranks(), full)
