@@ -314,12 +314,11 @@ def main():
     ev1.record(s_ss)
     barrier()
     clk = clocks.stop()
-    dt_ms = ev0.elapsed_time(ev1)
-    if ws > 1:
-        t = torch.tensor([dt_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dt_ms = float(t.item())
-    value = ws * args.steps * E / (dt_ms / 1e3) / 1e9
+    from grudon_gb300.replicas import job_throughput
+    dev = torch.device("cuda", local) if ws > 1 else None
+    thr, secs, _ = job_throughput(args.steps * E, ev0.elapsed_time(ev1) / 1e3, dev)
+    dt_ms = secs * 1e3
+    value = thr / 1e9
 
     # End to end through the C ABI with host buffers.
     for c in (ctx_cc, ctx_ss):
@@ -334,12 +333,8 @@ def main():
             c.run()
             c.read_props()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": ws * args.steps * E / e2e_s / 1e9, "unit": "GTEPS",
+    e2e_thr, _, _ = job_throughput(args.steps * E, time.perf_counter() - t0, dev)
+    e2e = {"value": e2e_thr / 1e9, "unit": "GTEPS",
            "h2d_bytes_per_step": h2d // args.steps,
            "d2h_bytes_per_step": 4 * (G_cc.num_vertices + G_ss.num_vertices)}
 

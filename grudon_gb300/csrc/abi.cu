@@ -144,6 +144,11 @@ int grd_ensure_in_edges(grd_ctx* ctx) {
   TRY(upload(ctx, (uint32_t*)ctx->g.in_off, L.in_off));
   TRY(upload(ctx, (uint32_t*)ctx->g.in_src, L.in_src));
   if (L.weighted) TRY(upload(ctx, (uint32_t*)ctx->g.in_wgt, L.in_wgt));
+  ctx->pull.num_in_hubs = (uint32_t)L.in_hubs.size();
+  TRY(dev_alloc(ctx, &ctx->pull.in_hubs, std::max<size_t>(L.in_hubs.size(), 1)));
+  if (!L.in_hubs.empty())
+    CK(cudaMemcpyAsync(ctx->pull.in_hubs, L.in_hubs.data(), sizeof(HubChunkD) * L.in_hubs.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return GRD_OK;
 }
@@ -187,6 +192,16 @@ bool use_dense(const grd_ctx* ctx) {
   return ctx->last_frontier * 32 >= ctx->g.S;
 }
 
+// Direction: the pull map reads every in-edge once; the push map reads only
+// the frontier's out-edges but needs atomics.  The fixed rule pulls when the
+// frontier entering the round holds at least 1/16 of the vertices.
+bool use_pull(const grd_ctx* ctx) {
+  if (!ctx->in_edges_alloc) return false;
+  if (ctx->params.direction == GRD_DIR_PULL) return true;
+  if (ctx->params.direction == GRD_DIR_PUSH) return false;
+  return ctx->last_frontier * 16 >= ctx->g.V;
+}
+
 }  // namespace
 
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
@@ -207,6 +222,17 @@ int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
 int grd_enqueue_edge_map(grd_ctx* ctx) {
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
+    if (use_pull(ctx)) {
+      k_pull<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ctx->pull.num_in_hubs)
+        k_pull_hub<A><<<std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8)), 256, 0, ctx->stream>>>(
+            ctx->g, ctx->st, ctx->pull.in_hubs, ctx->pull.num_in_hubs);
+      CK_LAUNCH();
+      ctx->stats.pull_rounds++;
+      ctx->stats.kernel_launches += ctx->pull.num_in_hubs ? 2 : 1;
+      ctx->pull.edges += ctx->L.E;
+      return GRD_OK;
+    }
     const uint32_t B = lbs_blocks(ctx);
     k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(ctx->st, B);
@@ -279,7 +305,7 @@ int grd_read_counters(grd_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->h_counters, ctx->st.counters, sizeof(unsigned long long) * NUM_COUNTERS,
                      cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  ctx->stats.edges_scanned = ctx->h_counters[C_EDGES];
+  ctx->stats.edges_scanned = ctx->h_counters[C_EDGES] + ctx->pull.edges;
   ctx->stats.bytes_synced = ctx->h_counters[C_BYTES];
   ctx->stats.reference_bytes_moved = ctx->h_counters[C_REFBYTES];
   ctx->stats.actives_total += ctx->h_counters[C_ACTIVE];
@@ -451,6 +477,7 @@ int grd_init(grd_ctx* ctx) {
   TRY(grd_read_counters(ctx));  // initial |frontier| for the first round's mode
   ctx->stats = grd_stats{};
   ctx->stats.kernel_launches = 1;
+  ctx->pull.edges = 0;
   ctx->inited = true;
   return GRD_OK;
 }

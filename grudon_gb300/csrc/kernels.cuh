@@ -778,6 +778,167 @@ __global__ void __launch_bounds__(256) k_diff_dirty(DevGraph g, DevState st) {
   }
 }
 
+// -------------------------------------------------------------- pull map --
+// Pull edge-map over each partition's in-edge lists (sources in ascending
+// slot order).  Min algorithms fold every in-edge: a source that is not in
+// this round's frontier still holds the value it last sent, whose
+// relaxation has already been applied, so it cannot lower anything — the
+// values and the dirty set equal those of the push over the frontier, with no
+// atomics.  Delta PageRank adds only frontier sources (bit test in FB), in
+// ascending source order, so its sums are reproducible.  PR_PULL folds every
+// source with a Kahan sum.
+constexpr uint32_t K_PULL_HUB = 1024;  // = PULL_HUB of the layout
+constexpr uint32_t PULL_CH = 256;      // staged in-edges per warp step
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+// Value contributed by one in-edge (bit pattern), and the fold identity.
+template <int A>
+__device__ __forceinline__ uint32_t pull_value(const DevState& st, uint32_t src, uint32_t w) {
+  const uint32_t v = st.mprop[src];
+  if (A == A_SSSP_HOP) return v == 0xFFFFFFFFu ? v : v + 1u;
+  if (A == A_SSSP_W) return sat_add(v, w);
+  if (A == A_PR_DELTA) return test_bit(st.FB, src) ? v : 0u;
+  return v;  // CC, PR_PULL
+}
+
+template <int A>
+struct PullAcc {
+  uint32_t best = 0xFFFFFFFFu;  // min algorithms
+  float s = 0.0f, c = 0.0f;     // sums (c: Kahan compensation, PR_PULL)
+  __device__ __forceinline__ void fold(uint32_t v) {
+    if (A == A_PR_PULL)
+      kahan_add(s, c, __uint_as_float(v));
+    else if (A == A_PR_DELTA)
+      s = __fadd_rn(s, __uint_as_float(v));
+    else
+      best = min(best, v);
+  }
+};
+
+// Writes the pulled value of destination slot d; returns its dirty bit.
+template <int A>
+__device__ __forceinline__ bool pull_commit(const DevState& st, uint32_t d, const PullAcc<A>& a, bool has) {
+  if (A == A_PR_PULL) {
+    if (has) st.mupd[d] = __float_as_uint(__fsub_rn(a.s, a.c));
+    return has;
+  }
+  if (A == A_PR_DELTA) {  // every frontier contribution is > 0
+    if (a.s > 0.0f) {
+      st.mupd[d] = __float_as_uint(a.s);
+      return true;
+    }
+    return false;
+  }
+  if (a.best < st.mupd[d]) {
+    st.mupd[d] = a.best;
+    return true;
+  }
+  return false;
+}
+
+// One warp per 32 consecutive destination slots.  Their in-edges are
+// concatenated (warp scan of in-degrees) and staged 256 at a time: lanes load
+// consecutive in_src entries (coalesced), gather the source values into
+// shared memory, then every lane folds its own slot's part of the stage in
+// ascending source order.  In-lists longer than K_PULL_HUB go to k_pull_hub.
+// The warp writes its 32 dirty bits as one word.
+template <int A>
+__global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
+  __shared__ uint32_t s_val[8][PULL_CH];
+  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+  const uint64_t nwarps = (uint64_t)gridDim.x * 8;
+  for (uint64_t base = ((uint64_t)blockIdx.x * 8 + warp) * 32; base < g.S; base += nwarps * 32) {
+    const uint32_t d = (uint32_t)base + lane;
+    const uint32_t b = __ldg(&g.in_off[d]);
+    uint32_t deg = __ldg(&g.in_off[d + 1]) - b;
+    const bool has = deg > 0;
+    const bool hub = deg > K_PULL_HUB;
+    if (hub) deg = 0;
+    const uint32_t incl = warp_incl_scan(deg);
+    const uint32_t excl = incl - deg;
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    PullAcc<A> acc;
+    for (uint32_t c0 = 0; c0 < total; c0 += PULL_CH) {
+      uint32_t src[PULL_CH / 32], wt[PULL_CH / 32];
+#pragma unroll
+      for (int k = 0; k < (int)(PULL_CH / 32); ++k) {
+        const uint32_t q = c0 + k * 32 + lane;
+        uint32_t lo = 0;
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1) {
+          const uint32_t cand = lo + step;
+          if (__shfl_sync(FULL, excl, cand) <= q) lo = cand;
+        }
+        const uint32_t sb = __shfl_sync(FULL, b, lo);
+        const uint32_t se = __shfl_sync(FULL, excl, lo);
+        const uint32_t e = sb + (q - se);
+        src[k] = q < total ? __ldg(&g.in_src[e]) : 0xFFFFFFFFu;
+        wt[k] = (A == A_SSSP_W && q < total) ? __ldg(&g.in_wgt[e]) : 0u;
+      }
+#pragma unroll
+      for (int k = 0; k < (int)(PULL_CH / 32); ++k)
+        s_val[warp][k * 32 + lane] = src[k] != 0xFFFFFFFFu ? pull_value<A>(st, src[k], wt[k]) : 0u;
+      __syncwarp();
+      const uint32_t q0 = max(excl, c0), q1 = min(excl + deg, c0 + PULL_CH);
+      for (uint32_t q = q0; q < q1; ++q) acc.fold(s_val[warp][q - c0]);
+      __syncwarp();
+    }
+    bool dirty = false;
+    if (!hub) dirty = pull_commit<A>(st, d, acc, has);
+    else if (A == A_PR_PULL) dirty = true;  // the hub kernel writes the value
+    const uint32_t m = __ballot_sync(FULL, dirty);
+    if (lane == 0) st.MD[d >> 5] = m;
+  }
+}
+
+// Long in-lists: one block per destination; thread t folds the elements t,
+// t+256, ... (coalesced), then thread 0 folds the 256 partials in thread
+// order (a fixed order, so sums are reproducible).  Runs after k_pull, whose
+// dirty word for the slot is already written: a dirty hub ORs its bit in.
+template <int A>
+__global__ void __launch_bounds__(256) k_pull_hub(DevGraph g, DevState st, const HubChunkD* hubs, uint32_t n) {
+  __shared__ uint32_t s_part[256];
+  for (uint32_t h = blockIdx.x; h < n; h += gridDim.x) {
+    const HubChunkD hc = hubs[h];
+    PullAcc<A> acc;
+    uint32_t q = hc.e0 + threadIdx.x;
+    for (; q + 3 * 256 < hc.e1; q += 4 * 256) {
+      uint32_t v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t e = q + u * 256;
+        v[u] = pull_value<A>(st, __ldg(&g.in_src[e]), A == A_SSSP_W ? __ldg(&g.in_wgt[e]) : 0u);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc.fold(v[u]);
+    }
+    for (; q < hc.e1; q += 256)
+      acc.fold(pull_value<A>(st, __ldg(&g.in_src[q]), A == A_SSSP_W ? __ldg(&g.in_wgt[q]) : 0u));
+    uint32_t part;
+    if (A == A_PR_PULL)
+      part = __float_as_uint(__fsub_rn(acc.s, acc.c));
+    else if (A == A_PR_DELTA)
+      part = __float_as_uint(acc.s);
+    else
+      part = acc.best;
+    s_part[threadIdx.x] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      PullAcc<A> tot;
+      for (int i = 0; i < 256; ++i) tot.fold(s_part[i]);
+      if (pull_commit<A>(st, hc.slot, tot, true) && A != A_PR_PULL)
+        red_or(st.MD + (hc.slot >> 5), 1u << (hc.slot & 31));
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------ update --
 // UpdateWorker::update = update_frontier() then apply_updates()
 // (src/Workers.cpp:77-82), over the vertex_updates dirty set; rebuilds the

@@ -23,99 +23,6 @@ using namespace grd;
 
 namespace {
 
-constexpr uint32_t K_PULL_HUB = 1024;  // = PULL_HUB in layout.hpp
-constexpr uint32_t PULL_CH = 256;      // staged in-edges per warp step
-
-__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
-  const float y = __fsub_rn(x, c);
-  const float t = __fadd_rn(s, y);
-  c = __fsub_rn(__fsub_rn(t, s), y);
-  s = t;
-}
-
-// One warp per 32 consecutive destination slots.  The in-edges of the 32
-// slots are concatenated (warp scan of in-degrees) and staged 256 at a time:
-// lanes load consecutive in_src entries (coalesced) and gather the source
-// contributions into shared memory, then every lane folds its own slot's
-// part of the stage into a Kahan sum in ascending source order.  In-lists
-// longer than K_PULL_HUB are summed by k_pull_hub.  The dirty (sent) set is
-// every slot with at least one in-edge; the warp writes its word by ballot.
-__global__ void __launch_bounds__(256) k_pull_pr(DevGraph g, DevState st) {
-  __shared__ float s_val[8][PULL_CH];
-  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-  const uint64_t nwarps = (uint64_t)gridDim.x * 8;
-  const float* contrib = reinterpret_cast<const float*>(st.mprop);
-  for (uint64_t base = ((uint64_t)blockIdx.x * 8 + warp) * 32; base < g.S; base += nwarps * 32) {
-    const uint32_t d = (uint32_t)base + lane;
-    const uint32_t b = __ldg(&g.in_off[d]);
-    uint32_t deg = __ldg(&g.in_off[d + 1]) - b;
-    const bool has = deg > 0;
-    const bool hub = deg > K_PULL_HUB;
-    if (hub) deg = 0;
-    const uint32_t incl = warp_incl_scan(deg);
-    const uint32_t excl = incl - deg;
-    const uint32_t total = __shfl_sync(FULL, incl, 31);
-    float s = 0.0f, c = 0.0f;
-    for (uint32_t c0 = 0; c0 < total; c0 += PULL_CH) {
-      uint32_t src[PULL_CH / 32];
-#pragma unroll
-      for (int k = 0; k < (int)(PULL_CH / 32); ++k) {
-        const uint32_t q = c0 + k * 32 + lane;
-        uint32_t lo = 0;
-#pragma unroll
-        for (uint32_t step = 16; step; step >>= 1) {
-          const uint32_t cand = lo + step;
-          if (__shfl_sync(FULL, excl, cand) <= q) lo = cand;
-        }
-        const uint32_t sb = __shfl_sync(FULL, b, lo);
-        const uint32_t se = __shfl_sync(FULL, excl, lo);
-        src[k] = q < total ? __ldg(&g.in_src[sb + (q - se)]) : 0xFFFFFFFFu;
-      }
-#pragma unroll
-      for (int k = 0; k < (int)(PULL_CH / 32); ++k)
-        s_val[warp][k * 32 + lane] = src[k] != 0xFFFFFFFFu ? contrib[src[k]] : 0.0f;
-      __syncwarp();
-      const uint32_t q0 = max(excl, c0), q1 = min(excl + deg, c0 + PULL_CH);
-      for (uint32_t q = q0; q < q1; ++q) kahan_add(s, c, s_val[warp][q - c0]);
-      __syncwarp();
-    }
-    if (has && !hub) st.mupd[d] = __float_as_uint(__fsub_rn(s, c));
-    const uint32_t m = __ballot_sync(FULL, has);
-    if (lane == 0) st.MD[d >> 5] = m;
-  }
-}
-
-// Long in-lists: one block per destination; thread t sums the elements
-// t, t+256, ... (coalesced) with Kahan, then thread 0 merges the 256 partial
-// sums in thread order — a fixed order, so the result is reproducible.
-__global__ void __launch_bounds__(256) k_pull_hub(DevGraph g, DevState st, const HubChunkD* hubs, uint32_t n) {
-  __shared__ float s_part[256];
-  const float* contrib = reinterpret_cast<const float*>(st.mprop);
-  for (uint32_t h = blockIdx.x; h < n; h += gridDim.x) {
-    const HubChunkD hc = hubs[h];
-    float s = 0.0f, c = 0.0f;
-    uint32_t q = hc.e0 + threadIdx.x;
-    for (; q + 3 * 256 < hc.e1; q += 4 * 256) {
-      const uint32_t a0 = __ldg(&g.in_src[q]), a1 = __ldg(&g.in_src[q + 256]);
-      const uint32_t a2 = __ldg(&g.in_src[q + 512]), a3 = __ldg(&g.in_src[q + 768]);
-      const float v0 = contrib[a0], v1 = contrib[a1], v2 = contrib[a2], v3 = contrib[a3];
-      kahan_add(s, c, v0);
-      kahan_add(s, c, v1);
-      kahan_add(s, c, v2);
-      kahan_add(s, c, v3);
-    }
-    for (; q < hc.e1; q += 256) kahan_add(s, c, contrib[__ldg(&g.in_src[q])]);
-    s_part[threadIdx.x] = __fsub_rn(s, c);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      float ts = 0.0f, tc = 0.0f;
-      for (int i = 0; i < 256; ++i) kahan_add(ts, tc, s_part[i]);
-      st.mupd[hc.slot] = __float_as_uint(__fsub_rn(ts, tc));
-    }
-    __syncthreads();
-  }
-}
-
 // Kahan merge of one partition's partial sum into the compute-side
 // accumulator (upd = running sum, comp = compensation).
 struct OpPullXfer {
@@ -181,25 +88,20 @@ int ensure_pull_state(grd_ctx* ctx) {
   TRY(grd_dev_alloc_bytes(ctx, (void**)&ps.comp, sizeof(uint32_t) * ctx->L.V));
   TRY(grd_dev_alloc_bytes(ctx, (void**)&ps.residual, sizeof(double)));
   CK(cudaMallocHost((void**)&ps.h_residual, sizeof(double)));
-  const auto& hubs = ctx->L.in_hubs;
-  ps.num_in_hubs = (uint32_t)hubs.size();
-  TRY(grd_dev_alloc_bytes(ctx, (void**)&ps.in_hubs, sizeof(HubChunkD) * std::max<size_t>(hubs.size(), 1)));
-  if (!hubs.empty())
-    CK(cudaMemcpyAsync(ps.in_hubs, hubs.data(), sizeof(HubChunkD) * hubs.size(), cudaMemcpyHostToDevice,
-                       ctx->stream));
   return GRD_OK;
 }
 
 uint32_t sms(const grd_ctx* ctx, uint32_t per_sm) { return (uint32_t)ctx->num_sms * per_sm; }
 
 int enqueue_pull_edge_map(grd_ctx* ctx) {
-  k_pull_pr<<<sms(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+  k_pull<A_PR_PULL><<<sms(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
   if (ctx->pull.num_in_hubs)
-    k_pull_hub<<<std::min<uint32_t>(ctx->pull.num_in_hubs, sms(ctx, 8)), 256, 0, ctx->stream>>>(
+    k_pull_hub<A_PR_PULL><<<std::min<uint32_t>(ctx->pull.num_in_hubs, sms(ctx, 8)), 256, 0, ctx->stream>>>(
         ctx->g, ctx->st, ctx->pull.in_hubs, ctx->pull.num_in_hubs);
   CK_LAUNCH();
   ctx->stats.kernel_launches += ctx->pull.num_in_hubs ? 2 : 1;
   ctx->stats.pull_rounds++;
+  ctx->pull.edges += ctx->L.E;  // every in-edge is read once per iteration
   return GRD_OK;
 }
 
@@ -241,8 +143,6 @@ int read_residual(grd_ctx* ctx) {
                      ctx->stream));
   TRY(grd_read_counters(ctx));  // synchronises the stream
   ctx->stats.last_residual = *ctx->pull.h_residual / (double)ctx->L.V;
-  ctx->pull.edges += ctx->L.E;  // every in-edge is read once per iteration
-  ctx->stats.edges_scanned = ctx->h_counters[C_EDGES] + ctx->pull.edges;
   return GRD_OK;
 }
 
@@ -257,7 +157,6 @@ int grd_pull_stage(grd_ctx* ctx, int stage) {
   switch (stage) {
     case -1: {  // init: accumulators and compensation start at zero
       TRY(ensure_pull_state(ctx));
-      ctx->pull.edges = 0;
       k_zero_u32<<<sms(ctx, 4), 256, 0, ctx->stream>>>(ctx->pull.comp, ctx->L.V);
       CK_LAUNCH();
       return GRD_OK;

@@ -25,18 +25,23 @@ GRAPHS = {
 
 
 FORMATS = [g.GRD_FMT_AUTO, g.GRD_FMT_BITVEC, g.GRD_FMT_LIST]
+# (direction, frontier format): push with sparse / dense dirty tracking, pull,
+# and the fixed heuristic choosing per round.
+MODES = [(g.GRD_DIR_PUSH, g.GRD_FMT_LIST), (g.GRD_DIR_PUSH, g.GRD_FMT_BITVEC), (g.GRD_DIR_PULL, g.GRD_FMT_AUTO),
+         (g.GRD_DIR_AUTO, g.GRD_FMT_AUTO)]
 
 
 @pytest.mark.parametrize("num_memory", [1, 3])
 @pytest.mark.parametrize("name", list(GRAPHS))
-@pytest.mark.parametrize("fmt", FORMATS)
-def test_min_algorithms_bit_exact(gpu, name, num_memory, fmt):
+@pytest.mark.parametrize("mode", MODES, ids=["push-list", "push-bitvec", "pull", "auto"])
+def test_min_algorithms_bit_exact(gpu, name, num_memory, mode):
     G = GRAPHS[name]()
     ro, ci, w = G.row_offsets, G.col_indices, G.weights
     part = G.partition_edge_balanced(num_memory) if num_memory > 1 else None
+    direction, fmt = mode
     with g.Context(G, part, num_memory=num_memory) as ctx:
         for algo, oalgo in ALGOS:
-            ctx.set_algo(algo, frontier_format=fmt)
+            ctx.set_algo(algo, direction=direction, frontier_format=fmt)
             ctx.init()
             st = ctx.run()
             ref = O.run(oalgo, ro, ci, w, mirror=part, num_memory=num_memory)
@@ -44,7 +49,11 @@ def test_min_algorithms_bit_exact(gpu, name, num_memory, fmt):
             np.testing.assert_array_equal(ctx.read_updates(), ref["updates"])
             assert st["rounds"] == ref["stats"]["rounds"]
             assert st["converged"] == 1
-            assert st["edges_scanned"] == ref["stats"]["edges_scanned"]
+            if direction == g.GRD_DIR_PUSH:
+                assert st["edges_scanned"] == ref["stats"]["edges_scanned"]
+                assert st["pull_rounds"] == 0
+            if direction == g.GRD_DIR_PULL:
+                assert st["push_rounds"] == 0 and st["edges_scanned"] == st["rounds"] * G.num_edges
             assert st["bytes_synced"] == ref["stats"]["bytes_synced"]
             assert st["reference_bytes_moved"] == ref["stats"]["reference_bytes_moved"]
 
@@ -71,13 +80,13 @@ def test_stage_api_matches_oracle_round_by_round(gpu, num_memory):
 
 
 @pytest.mark.parametrize("num_memory", [1, 3])
-@pytest.mark.parametrize("fmt", FORMATS)
-def test_pr_delta_close_to_oracle(gpu, num_memory, fmt):
+@pytest.mark.parametrize("mode", MODES, ids=["push-list", "push-bitvec", "pull", "auto"])
+def test_pr_delta_close_to_oracle(gpu, num_memory, mode):
     G = g.Graph.rmat(14, 16)
     ro, ci = G.row_offsets, G.col_indices
     part = G.partition_edge_balanced(num_memory) if num_memory > 1 else None
     with g.Context(G, part, num_memory=num_memory) as ctx:
-        ctx.set_algo(g.GRD_PR_DELTA, frontier_format=fmt)
+        ctx.set_algo(g.GRD_PR_DELTA, direction=mode[0], frontier_format=mode[1])
         ctx.init()
         st = ctx.run()
         ref = O.run(O.ORC_PR_DELTA, ro, ci, mirror=part, num_memory=num_memory)
