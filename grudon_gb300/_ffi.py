@@ -75,6 +75,7 @@ SIGNATURES = {
     "grd_aggregate": (C.c_int, [C.c_void_p]),
     "grd_update": (C.c_int, [C.c_void_p, u64p]),
     "grd_aggregate_values": (C.c_int, [C.c_void_p, u32p, u32p, C.c_size_t]),
+    "grd_aggregate_values_noalloc": (C.c_int, [C.c_void_p, u32p, u32p, C.c_size_t]),
     "grd_run": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(grd_stats)]),
     "grd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(grd_stats)]),
     "grd_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),

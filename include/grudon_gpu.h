@@ -148,6 +148,23 @@ int grd_update(grd_ctx* ctx, uint64_t* frontier_size);
 int grd_aggregate_values(grd_ctx* ctx, const uint32_t* gids,
                          const uint32_t* values, size_t n);
 
+/* grd_aggregate_values for callers that cannot allocate device memory — a
+ * serving process whose memory is already reserved for its own pool, a
+ * latency-bound caller that must not take the allocator's device
+ * synchronisation, or a thread in the middle of capturing other work into a
+ * CUDA graph.  No counterpart in the reference.  Same arguments and result as
+ * grd_aggregate_values, but the pairs are staged in a fixed device array
+ * inside the library (2 MiB, held by every GPU that loads the library until
+ * exit) instead of an allocated buffer, so at most GRD_NOALLOC_MAX_VALUES
+ * pairs per call (larger n returns GRD_E_INVALID).  The first call on a
+ * device looks the array's address up for that device: make it before any
+ * stream capture.  All calls share the one array: calls whose work overlaps on
+ * the GPU (several ctxs on different streams) race; each call waits for its
+ * own work before returning. */
+#define GRD_NOALLOC_MAX_VALUES (1u << 18)
+int grd_aggregate_values_noalloc(grd_ctx* ctx, const uint32_t* gids,
+                                 const uint32_t* values, size_t n);
+
 /* Full run: init() already called; loops rounds until the frontier is empty
  * or params.max_rounds.  flags: GRD_RUN_STRICT. */
 int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats);
