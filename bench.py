@@ -267,15 +267,16 @@ def main():
     p_ss = G_ss.partition_edge_balanced(NUM_MEMORY)
     ctx_cc = g.Context(G_cc, p_cc, num_memory=NUM_MEMORY, device=local)
     ctx_ss = g.Context(G_ss, p_ss, num_memory=NUM_MEMORY, device=local)
-    ctx_cc.set_algo(g.GRD_CC, direction=g.GRD_DIR_PUSH)
-    ctx_ss.set_algo(g.GRD_SSSP_W, direction=g.GRD_DIR_PUSH)
+    ctx_cc.set_algo(g.GRD_CC)
+    ctx_ss.set_algo(g.GRD_SSSP_W)
     E = G_cc.num_edges + G_ss.num_edges
+    slots = {id(c): sum(sum(c.layout_info(p)[:2]) for p in range(NUM_MEMORY)) for c in (ctx_cc, ctx_ss)}
 
-    def step():
+    def step(host_loop=False):
         out = []
         for c in (ctx_cc, ctx_ss):
             c.init()
-            out.append(c.run())
+            out.append(c.run(host_loop=host_loop))
         return out
 
     def barrier():
@@ -285,9 +286,9 @@ def main():
 
     for _ in range(args.warmup):
         step()
-    for c in (ctx_cc, ctx_ss):
-        c.set_profiling(True)
 
+    # Timed region: every step runs both algorithms to convergence, each as
+    # one device-driven CUDA-graph launch.
     s_cc = torch.cuda.ExternalStream(ctx_cc.stream())
     s_ss = torch.cuda.ExternalStream(ctx_ss.stream())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -295,22 +296,13 @@ def main():
     clocks.start()
     barrier()
     ev0.record(s_cc)
-    agg = {"edge_map_ms": 0.0, "fwd_ms": 0.0, "bwd_ms": 0.0, "update_ms": 0.0, "rounds_ms": 0.0,
-           "actives": 0, "edges": 0, "launches": 0, "rounds": [], "bytes_synced": 0}
+    agg = {"edges": 0, "launches": 0, "rounds": [], "device_loop": []}
     for _ in range(args.steps):
-        for st, weighted in zip(step(), (False, True)):
-            agg["fwd_ms"] += st["stage_ms"][0]
-            agg["edge_map_ms"] += st["stage_ms"][1]
-            agg["bwd_ms"] += st["stage_ms"][2]
-            agg["update_ms"] += st["stage_ms"][3]
-            agg["rounds_ms"] += st["stage_ms"][4]
-            agg["actives"] += st["actives_total"]
+        for st in step():
             agg["edges"] += st["edges_scanned"]
             agg["launches"] += st["kernel_launches"]
-            agg["bytes_synced"] += st["bytes_synced"]
-            agg.setdefault("alg_bytes", 0)
-            agg["alg_bytes"] += st["actives_total"] * 12 + st["edges_scanned"] * (16 if weighted else 12)
             agg["rounds"].append(st["rounds"])
+            agg["device_loop"].append(st["device_loop"])
     ev1.record(s_ss)
     barrier()
     clk = clocks.stop()
@@ -320,9 +312,29 @@ def main():
     dt_ms = secs * 1e3
     value = thr / 1e9
 
-    # End to end through the C ABI with host buffers.
+    # Stage timing for the roofline: the same steps driven from the host with
+    # CUDA events around every stage of every round (same kernels, same
+    # per-round choices).
+    for c in (ctx_cc, ctx_ss):
+        c.set_profiling(True)
+    prof = {"edge_map_ms": 0.0, "fwd_ms": 0.0, "bwd_ms": 0.0, "update_ms": 0.0, "rounds_ms": 0.0, "alg_bytes": 0.0,
+            "push_rounds": 0, "pull_rounds": 0}
+    for _ in range(args.steps):
+        for st, c, weighted, Eg in zip(step(host_loop=True), (ctx_cc, ctx_ss), (False, True),
+                                        (G_cc.num_edges, G_ss.num_edges)):
+            for i, k in enumerate(("fwd_ms", "edge_map_ms", "bwd_ms", "update_ms", "rounds_ms")):
+                prof[k] += st["stage_ms"][i]
+            wb = 4 if weighted else 0
+            push_edges = st["edges_scanned"] - st["pull_rounds"] * Eg
+            S = slots[id(c)]
+            prof["alg_bytes"] += (st["push_actives"] * 12 + push_edges * (12 + wb) +
+                                  st["pull_rounds"] * (Eg * (8 + wb) + S * 8 + S / 8))
+            prof["push_rounds"] += st["push_rounds"]
+            prof["pull_rounds"] += st["pull_rounds"]
     for c in (ctx_cc, ctx_ss):
         c.set_profiling(False)
+
+    # End to end through the C ABI with host buffers.
     barrier()
     h2d = 0
     t0 = time.perf_counter()
@@ -343,12 +355,16 @@ def main():
     if pk.exists():
         peaks = json.loads(pk.read_text())
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = agg["alg_bytes"] / (agg["edge_map_ms"] / 1e3) / 1e9 if agg["edge_map_ms"] > 0 else 0.0
-    roofline = {"bound": "hbm", "kernel": "edge-map stage (k_push + k_hub_push)", "achieved": achieved,
-                "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+    achieved = prof["alg_bytes"] / (prof["edge_map_ms"] / 1e3) / 1e9 if prof["edge_map_ms"] > 0 else 0.0
+    roofline = {"bound": "hbm",
+                "kernel": "edge-map stage: push (k_deg_*, k_push_lbs, k_hub_push, k_diff_dirty) or pull "
+                          "(k_pull, k_pull_hub) per round",
+                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None,
-                "edge_map_share_of_rounds": agg["edge_map_ms"] / agg["rounds_ms"] if agg["rounds_ms"] else None,
-                "stage_ms_per_step": {k: agg[k] / args.steps for k in
+                "edge_map_share_of_rounds": prof["edge_map_ms"] / prof["rounds_ms"] if prof["rounds_ms"] else None,
+                "push_rounds_per_step": prof["push_rounds"] / args.steps,
+                "pull_rounds_per_step": prof["pull_rounds"] / args.steps,
+                "stage_ms_per_step": {k: prof[k] / args.steps for k in
                                       ("fwd_ms", "edge_map_ms", "bwd_ms", "update_ms", "rounds_ms")}}
     pr = None
     if not args.no_pagerank:
@@ -360,7 +376,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": workload_config(args.scale, seed, G_cc, G_ss) | {"parallelism": f"replicas x{ws}"},
             "e2e": e2e, "gpu_launches": agg["launches"], "roofline": roofline, "clocks": clk,
-            "rounds_per_step": agg["rounds"][:2],
+            "rounds_per_step": agg["rounds"][:2], "device_loop": all(agg["device_loop"]),
             "edges_scanned_gteps": ws * agg["edges"] / (dt_ms / 1e3) / 1e9,
         }
         if ws == 1 and not args.no_cpu_baseline:

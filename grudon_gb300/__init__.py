@@ -277,9 +277,13 @@ class Context:
             out[f] = list(v) if isinstance(v, C.Array) else v
         return out
 
-    def run(self, strict: bool = False) -> dict:
+    def run(self, strict: bool = False, host_loop: bool = False) -> dict:
+        """Runs to convergence (or the round cap).  By default the rounds run
+        as one device-driven CUDA-graph launch; host_loop=True drives them
+        from the host instead."""
         s = _ffi.grd_stats()
-        self._check(self._lib.grd_run(self._ctx, GRD_RUN_STRICT if strict else 0, C.byref(s)))
+        flags = (GRD_RUN_STRICT if strict else 0) | (_ffi.GRD_RUN_HOST_LOOP if host_loop else 0)
+        self._check(self._lib.grd_run(self._ctx, flags, C.byref(s)))
         return self._stats_dict(s)
 
     def stats(self) -> dict:

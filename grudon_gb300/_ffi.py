@@ -25,6 +25,7 @@ GRD_SSSP_W = 4
 GRD_DIR_AUTO, GRD_DIR_PUSH, GRD_DIR_PULL = 0, 1, 2
 GRD_FMT_AUTO, GRD_FMT_BITVEC, GRD_FMT_LIST = 0, 1, 2
 GRD_RUN_STRICT = 1
+GRD_RUN_HOST_LOOP = 2
 
 ERROR_NAMES = {
     GRD_E_INVALID: "GRD_E_INVALID", GRD_E_OOM: "GRD_E_OOM", GRD_E_CUDA: "GRD_E_CUDA",
@@ -50,7 +51,8 @@ class grd_stats(C.Structure):
     _fields_ = [("rounds", C.c_uint32), ("converged", C.c_uint32), ("edges_scanned", C.c_uint64),
                 ("bytes_synced", C.c_uint64), ("reference_bytes_moved", C.c_uint64),
                 ("last_residual", C.c_double), ("push_rounds", C.c_uint32), ("pull_rounds", C.c_uint32),
-                ("actives_total", C.c_uint64), ("kernel_launches", C.c_uint64), ("stage_ms", C.c_double * 5)]
+                ("actives_total", C.c_uint64), ("kernel_launches", C.c_uint64), ("stage_ms", C.c_double * 5),
+                ("device_loop", C.c_uint32), ("push_actives", C.c_uint64)]
 
 
 class grd_host_graph(C.Structure):

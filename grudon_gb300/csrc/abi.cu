@@ -193,13 +193,15 @@ bool use_dense(const grd_ctx* ctx) {
 }
 
 // Direction: the pull map reads every in-edge once; the push map reads only
-// the frontier's out-edges but needs atomics.  The fixed rule pulls when the
-// frontier entering the round holds at least 1/16 of the vertices.
+// the frontier's out-edges (load-balanced, fire-and-forget reductions in
+// dense rounds).  Measured on RMAT, push wins even for full frontiers, so the
+// fixed rule pulls only when at least half the vertices are active and the
+// in-edge view already exists (it is built when pull is requested).
 bool use_pull(const grd_ctx* ctx) {
   if (!ctx->in_edges_alloc) return false;
   if (ctx->params.direction == GRD_DIR_PULL) return true;
   if (ctx->params.direction == GRD_DIR_PUSH) return false;
-  return ctx->last_frontier * 16 >= ctx->g.V;
+  return ctx->last_frontier * 2 >= ctx->g.V;
 }
 
 }  // namespace
@@ -219,18 +221,36 @@ int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
   return GRD_OK;
 }
 
+// Kernels one edge-map round launches in each mode (push sparse / push
+// dense / pull).
+uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
+  if (mode == MODE_PULL) return ctx->pull.num_in_hubs ? 2 : 1;
+  return 4 + (ctx->g.num_hubs ? 1 : 0) + (mode == MODE_PUSH_DENSE ? 1 : 0);
+}
+
 int grd_enqueue_edge_map(grd_ctx* ctx) {
+  const int mode = use_pull(ctx) ? MODE_PULL : (use_dense(ctx) ? MODE_PUSH_DENSE : MODE_PUSH_SPARSE);
+  TRY(grd_enqueue_edge_map_mode(ctx, mode));
+  ctx->last_mode = mode;
+  if (mode == MODE_PULL) {
+    ctx->stats.pull_rounds++;
+    ctx->pull.edges += ctx->L.E;
+  } else {
+    ctx->stats.push_rounds++;
+  }
+  ctx->stats.kernel_launches += grd_edge_map_launches(ctx, mode);
+  return GRD_OK;
+}
+
+int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
-    if (use_pull(ctx)) {
+    if (mode == MODE_PULL) {
       k_pull<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       if (ctx->pull.num_in_hubs)
         k_pull_hub<A><<<std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8)), 256, 0, ctx->stream>>>(
             ctx->g, ctx->st, ctx->pull.in_hubs, ctx->pull.num_in_hubs);
       CK_LAUNCH();
-      ctx->stats.pull_rounds++;
-      ctx->stats.kernel_launches += ctx->pull.num_in_hubs ? 2 : 1;
-      ctx->pull.edges += ctx->L.E;
       return GRD_OK;
     }
     const uint32_t B = lbs_blocks(ctx);
@@ -238,7 +258,7 @@ int grd_enqueue_edge_map(grd_ctx* ctx) {
     k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(ctx->st, B);
     k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
-    const bool dense = use_dense(ctx);
+    const bool dense = mode == MODE_PUSH_DENSE;
     if (dense) {
       k_push_lbs<A, true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
@@ -248,8 +268,6 @@ int grd_enqueue_edge_map(grd_ctx* ctx) {
       if (ctx->g.num_hubs) k_hub_push<A, false><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     }
     CK_LAUNCH();
-    ctx->stats.push_rounds++;
-    ctx->stats.kernel_launches += 4 + (ctx->g.num_hubs ? 1 : 0) + (dense ? 1 : 0);
     return GRD_OK;
   });
 }
@@ -309,6 +327,8 @@ int grd_read_counters(grd_ctx* ctx) {
   ctx->stats.bytes_synced = ctx->h_counters[C_BYTES];
   ctx->stats.reference_bytes_moved = ctx->h_counters[C_REFBYTES];
   ctx->stats.actives_total += ctx->h_counters[C_ACTIVE];
+  if (ctx->last_mode >= 0 && ctx->last_mode != MODE_PULL) ctx->stats.push_actives += ctx->h_counters[C_ACTIVE];
+  ctx->last_mode = -1;
   ctx->last_frontier = ctx->h_counters[C_FRONTIER];
   if (ctx->h_counters[C_ERR]) {
     ctx->err = "device-side error code " + std::to_string(ctx->h_counters[C_ERR]);
@@ -402,6 +422,7 @@ void grd_ctx_destroy(grd_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
   }
   grd_ctx_release_extras(ctx);
+  grd_graph_release(ctx);
   for (void* p : ctx->allocs) cudaFree(p);
   for (void* p : ctx->host_registered) cudaHostUnregister(p);
   for (cudaEvent_t e : ctx->ev)
@@ -451,10 +472,12 @@ int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
     return GRD_E_INVALID;
   }
   CK(cudaSetDevice(ctx->device));
-  if (algo == GRD_PR_PULL || p.direction == GRD_DIR_PULL || p.direction == GRD_DIR_AUTO) {
+  if (algo == GRD_PR_PULL || p.direction == GRD_DIR_PULL) {
     int rc = grd_ensure_in_edges(ctx);
     if (rc != GRD_OK) return rc;
   }
+  grd_graph_release(ctx);  // a new algorithm or parameter set needs a new loop graph
+  ctx->graph_failed = false;
   ctx->algo = algo;
   ctx->params = p;
   ctx->inited = false;
@@ -529,7 +552,14 @@ int grd_update(grd_ctx* ctx, uint64_t* frontier_size) {
 int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
   TRY(check_ready(ctx));
   CK(cudaSetDevice(ctx->device));
-  if (ctx->algo == GRD_PR_PULL) {
+  bool device_loop = false;
+  if (ctx->algo != GRD_PR_PULL && !ctx->profiling && !(flags & GRD_RUN_HOST_LOOP) &&
+      ctx->stats.rounds < ctx->params.max_rounds)
+    TRY(grd_graph_run(ctx, &device_loop));
+  ctx->stats.device_loop = device_loop ? 1 : 0;
+  if (device_loop) {
+    // the whole loop ran as one graph launch
+  } else if (ctx->algo == GRD_PR_PULL) {
     TRY(grd_pull_run(ctx));
   } else {
     uint64_t f = 1;
@@ -702,8 +732,9 @@ int grd_ctx_init_device(grd_ctx* ctx) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-  CK(cudaMallocHost((void**)&ctx->h_counters, sizeof(unsigned long long) * NUM_COUNTERS));
-  std::memset(ctx->h_counters, 0, sizeof(unsigned long long) * NUM_COUNTERS);
+  CK(cudaMallocHost((void**)&ctx->h_counters, sizeof(unsigned long long) * (NUM_COUNTERS + 8)));
+  std::memset(ctx->h_counters, 0, sizeof(unsigned long long) * (NUM_COUNTERS + 8));
+  ctx->h_seed = ctx->h_counters + NUM_COUNTERS;
   TRY(alloc_and_upload(ctx));
   // Pin the large host layout arrays so grd_upload copies run at full
   // host->device bandwidth; pageable copies still work if pinning fails.

@@ -31,11 +31,17 @@ struct grd_ctx {
   bool inited = false;
   grd_stats stats{};
   std::string err;
-  unsigned long long* h_counters = nullptr;  // pinned
+  unsigned long long* h_counters = nullptr;  // pinned, NUM_COUNTERS + 8 entries
+  unsigned long long* h_seed = nullptr;      // = h_counters + NUM_COUNTERS
   uint64_t upload_bytes = 0;
   bool in_edges_alloc = false;
   PullState pull;
   uint64_t last_frontier = 0;  // |frontier| entering the next round
+  int last_mode = -1;          // edge-map mode of the round in flight (host loop)
+  cudaGraph_t run_graph = nullptr;     // device-driven round loop (graph_run.cu)
+  cudaGraphExec_t run_exec = nullptr;
+  bool graph_failed = false;           // building it failed here: host loop
+  std::string graph_error;
   uint32_t* agg_buf = nullptr; // staging of grd_aggregate_values (gids, values)
   size_t agg_cap = 0;
   bool profiling = false;
@@ -79,6 +85,12 @@ int grd_ensure_in_edges(grd_ctx* ctx);
 int grd_read_counters(grd_ctx* ctx);
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused);
 int grd_enqueue_edge_map(grd_ctx* ctx);
+enum EdgeMapMode { MODE_PUSH_SPARSE = 0, MODE_PUSH_DENSE = 1, MODE_PULL = 2 };
+int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode);
+uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode);
+// Device-driven loop (graph_run.cu).
+int grd_graph_run(grd_ctx* ctx, bool* used);
+void grd_graph_release(grd_ctx* ctx);
 int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate);
 int grd_enqueue_update(grd_ctx* ctx);
 // PR_PULL: stage 0 fwd, 1 pull edge-map, 2 bwd pack, 3 aggregate, 4 update.

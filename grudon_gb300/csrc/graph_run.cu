@@ -1,0 +1,206 @@
+// Device-driven round loop: one CUDA graph per (ctx, algorithm, parameters).
+//
+// Top level: a conditional WHILE node whose body is one round of
+// GraphAlgorithm::run (src/GraphAlgorithm.cpp:177-690):
+//   forward sync -> k_policy -> SWITCH {push sparse, push dense, pull}
+//   -> backward sync + aggregate -> update -> k_round_end
+// k_policy applies the direction / frontier-format rule on the device (the
+// frontier size of the previous update is already there) and selects the
+// switch branch; k_round_end counts the round and keeps the loop going while
+// the frontier is non-empty and the round cap is not reached, so the loop is
+// always bounded.  One graph launch runs the whole algorithm with no host
+// round trip; the host reads the counters once at the end.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+#include "ctx.hpp"
+#include "kernels.cuh"
+
+using namespace grd;
+
+namespace {
+
+struct PolicyArgs {
+  int direction, format, has_in;
+  uint32_t launches[3];  // kernels of one round per edge-map mode
+  unsigned long long edges;
+};
+
+__global__ void k_policy(DevGraph g, DevState st, cudaGraphConditionalHandle sw, PolicyArgs a) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const unsigned long long f = st.counters[C_FRONTIER];
+  const bool pull = a.has_in && (a.direction == GRD_DIR_PULL || (a.direction == GRD_DIR_AUTO && f * 2 >= g.V));
+  const bool dense = a.format == GRD_FMT_BITVEC || (a.format == GRD_FMT_AUTO && f * 32 >= g.S);
+  const int mode = pull ? MODE_PULL : (dense ? MODE_PUSH_DENSE : MODE_PUSH_SPARSE);
+  st.counters[C_MODE] = mode;
+  if (pull) {
+    st.counters[C_PULL_ROUNDS] += 1;
+    st.counters[C_EDGES] += a.edges;
+  } else {
+    st.counters[C_PUSH_ROUNDS] += 1;
+  }
+  st.counters[C_LAUNCHES] += a.launches[mode];
+  cudaGraphSetConditional(sw, (unsigned)mode);
+}
+
+__global__ void k_round_end(DevState st, cudaGraphConditionalHandle wh, uint32_t max_rounds) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const unsigned long long r = st.counters[C_ROUNDS] + 1;
+  st.counters[C_ROUNDS] = r;
+  st.counters[C_ACTIVE_TOTAL] += st.counters[C_ACTIVE];
+  if (st.counters[C_MODE] != MODE_PULL) st.counters[C_PUSH_ACTIVES] += st.counters[C_ACTIVE];
+  cudaGraphSetConditional(wh, (st.counters[C_FRONTIER] > 0 && r < max_rounds) ? 1u : 0u);
+}
+
+// Appends a conditional node to the graph being captured on `s` and returns
+// its body graphs; the capture continues after the node.
+int add_conditional(grd_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                    unsigned size, cudaGraph_t* bodies) {
+  cudaStreamCaptureStatus status;
+  cudaGraph_t graph;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  CK(cudaStreamGetCaptureInfo(s, &status, nullptr, &graph, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = type;
+  p.conditional.size = size;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &p));
+  for (unsigned i = 0; i < size; ++i) bodies[i] = p.conditional.phGraph_out[i];
+  CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return GRD_OK;
+}
+
+int capture_into(grd_ctx* ctx, cudaGraph_t body) {
+  CK(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  return GRD_OK;
+}
+
+int end_capture(grd_ctx* ctx, cudaGraph_t body) {
+  cudaGraph_t out = nullptr;
+  CK(cudaStreamEndCapture(ctx->stream, &out));
+  if (out != body) {
+    ctx->err = "capture returned an unexpected graph";
+    return GRD_E_CUDA;
+  }
+  return GRD_OK;
+}
+
+// Builds the graph; on any error the capture is ended and the error kept.
+int build(grd_ctx* ctx) {
+  const grd_stats saved = ctx->stats;  // enqueue helpers count host-side launches
+  cudaGraph_t top = nullptr;
+  CK(cudaGraphCreate(&top, 0));
+  ctx->run_graph = top;
+  cudaGraphConditionalHandle wh, sw;
+  CK(cudaGraphConditionalHandleCreate(&wh, top, 1, cudaGraphCondAssignDefault));
+  cudaGraph_t loop_body;
+  {
+    // The while node is the only node of the top-level graph.
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = wh;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, top, nullptr, nullptr, 0, &p));
+    loop_body = p.conditional.phGraph_out[0];
+  }
+  CK(cudaGraphConditionalHandleCreate(&sw, loop_body, 0, 0));
+  PolicyArgs pa{};
+  pa.direction = ctx->params.direction;
+  pa.format = ctx->params.frontier_format;
+  pa.has_in = ctx->in_edges_alloc ? 1 : 0;
+  pa.edges = ctx->L.E;
+  const uint32_t base = 3 /*fwd*/ + 1 /*policy*/ + 2 /*bwd pack*/ + (ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1) +
+                        1 /*update*/ + 1 /*round end*/;
+  for (int m = 0; m < 3; ++m) pa.launches[m] = base + grd_edge_map_launches(ctx, m);
+
+  int rc = capture_into(ctx, loop_body);
+  if (rc != GRD_OK) return rc;
+  cudaGraph_t branches[3] = {};
+  rc = grd_enqueue_fwd(ctx, true);
+  if (rc == GRD_OK) {
+    k_policy<<<1, 32, 0, ctx->stream>>>(ctx->g, ctx->st, sw, pa);
+    rc = add_conditional(ctx, ctx->stream, sw, cudaGraphCondTypeSwitch, 3, branches);
+  }
+  if (rc == GRD_OK) rc = grd_enqueue_bwd(ctx, true, true, true);
+  if (rc == GRD_OK) rc = grd_enqueue_update(ctx);
+  if (rc == GRD_OK) k_round_end<<<1, 32, 0, ctx->stream>>>(ctx->st, wh, ctx->params.max_rounds);
+  const int rc_end = end_capture(ctx, loop_body);
+  if (rc != GRD_OK) return rc;
+  if (rc_end != GRD_OK) return rc_end;
+  for (int m = 0; m < 3; ++m) {
+    if (m == MODE_PULL && !ctx->in_edges_alloc) continue;  // never selected
+    TRY(capture_into(ctx, branches[m]));
+    rc = grd_enqueue_edge_map_mode(ctx, m);
+    const int e = end_capture(ctx, branches[m]);
+    if (rc != GRD_OK) return rc;
+    if (e != GRD_OK) return e;
+  }
+  CK(cudaGraphInstantiate(&ctx->run_exec, top, 0));
+  ctx->stats = saved;
+  return GRD_OK;
+}
+
+}  // namespace
+
+void grd_graph_release(grd_ctx* ctx) {
+  if (ctx->run_exec) cudaGraphExecDestroy(ctx->run_exec);
+  if (ctx->run_graph) cudaGraphDestroy(ctx->run_graph);
+  ctx->run_exec = nullptr;
+  ctx->run_graph = nullptr;
+}
+
+// Runs the rest of the algorithm as one graph launch.  Returns GRD_OK with
+// *used = false when the graph cannot be built here (the caller then runs the
+// host-driven loop); the reason is kept in ctx->graph_error.
+int grd_graph_run(grd_ctx* ctx, bool* used) {
+  *used = false;
+  if (ctx->graph_failed) return GRD_OK;
+  if (!ctx->run_exec) {
+    const int rc = build(ctx);
+    if (rc != GRD_OK) {
+      ctx->graph_failed = true;
+      ctx->graph_error = ctx->err;
+      ctx->err.clear();
+      grd_graph_release(ctx);
+      cudaStreamCaptureStatus st;
+      if (cudaStreamIsCapturing(ctx->stream, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(ctx->stream, &g);
+        if (g) cudaGraphDestroy(g);
+      }
+      (void)cudaGetLastError();
+      return GRD_OK;
+    }
+  }
+  // Carry the host-side round statistics into the device counters.
+  // counters C_ROUNDS .. C_PUSH_ACTIVES, in order
+  unsigned long long* seed = ctx->h_seed;
+  seed[0] = ctx->stats.rounds;
+  seed[1] = ctx->stats.push_rounds;
+  seed[2] = ctx->stats.pull_rounds;
+  seed[3] = ctx->stats.actives_total;
+  seed[4] = 0;  // C_MODE
+  seed[5] = 0;  // C_LAUNCHES
+  seed[6] = ctx->stats.push_actives;
+  CK(cudaMemcpyAsync(ctx->st.counters + C_ROUNDS, seed, sizeof(unsigned long long) * 7, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaGraphLaunch(ctx->run_exec, ctx->stream));
+  TRY(grd_read_counters(ctx));
+  const unsigned long long* c = ctx->h_counters;
+  ctx->stats.rounds = (uint32_t)c[C_ROUNDS];
+  ctx->stats.push_rounds = (uint32_t)c[C_PUSH_ROUNDS];
+  ctx->stats.pull_rounds = (uint32_t)c[C_PULL_ROUNDS];
+  ctx->stats.actives_total = c[C_ACTIVE_TOTAL];
+  ctx->stats.push_actives = c[C_PUSH_ACTIVES];
+  ctx->stats.kernel_launches += c[C_LAUNCHES];
+  ctx->stats.converged = c[C_FRONTIER] == 0;
+  *used = true;
+  return GRD_OK;
+}

@@ -35,6 +35,13 @@ enum Counter : int {
   C_ERR = 6,       // first device-side error code (0 = none)
   C_PULL_EDGES = 7,
   C_MEDGES = 8,    // edges of the load-balanced push this round (non-hub rows)
+  C_ROUNDS = 9,         // device-driven loop: rounds run
+  C_PUSH_ROUNDS = 10,   // device-driven loop: rounds that pushed
+  C_PULL_ROUNDS = 11,   // device-driven loop: rounds that pulled
+  C_ACTIVE_TOTAL = 12,  // device-driven loop: sum of C_ACTIVE over rounds
+  C_MODE = 13,          // edge-map mode chosen for the current round
+  C_LAUNCHES = 14,      // device-driven loop: kernels launched
+  C_PUSH_ACTIVES = 15,  // device-driven loop: C_ACTIVE summed over push rounds
   NUM_COUNTERS = 16
 };
 

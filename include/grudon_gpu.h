@@ -65,6 +65,9 @@ extern "C" {
 #define GRD_FMT_LIST    2
 
 #define GRD_RUN_STRICT  1u /* flag: return GRD_E_ROUND_CAP at the round cap */
+#define GRD_RUN_HOST_LOOP 2u /* flag: drive rounds from the host (one
+                                synchronisation per round) instead of the
+                                device-driven CUDA-graph loop */
 
 /* Host CSR as handed to the library: row_offsets has num_vertices+1 entries
  * (u64, like the reference's LC_CSR_Graph row ends), col_indices num_edges
@@ -105,6 +108,10 @@ typedef struct grd_stats {
    * over rounds: [0] forward sync, [1] edge-map, [2] backward sync +
    * aggregate, [3] update, [4] whole rounds. */
   double stage_ms[5];
+  uint32_t device_loop;       /* 1 if the last grd_run ran as one graph
+                                 launch (device-driven loop), 0 if the host
+                                 drove the rounds                          */
+  uint64_t push_actives;      /* actives_total restricted to push rounds   */
 } grd_stats;
 
 typedef struct grd_ctx grd_ctx;

@@ -58,6 +58,44 @@ def test_min_algorithms_bit_exact(gpu, name, num_memory, mode):
             assert st["reference_bytes_moved"] == ref["stats"]["reference_bytes_moved"]
 
 
+@pytest.mark.parametrize("mode", MODES, ids=["push-list", "push-bitvec", "pull", "auto"])
+def test_device_loop_matches_host_loop(gpu, mode):
+    """One CUDA-graph launch (device-side policy + switch + while) gives the
+    same results and statistics as the host-driven loop."""
+    G = g.Graph.rmat(13, 8, symmetrize=True, weighted=True)
+    part = G.partition_edge_balanced(3)
+    with g.Context(G, part, num_memory=3) as ctx:
+        for algo in (g.GRD_CC, g.GRD_SSSP_HOP, g.GRD_SSSP_W, g.GRD_PR_DELTA):
+            ctx.set_algo(algo, direction=mode[0], frontier_format=mode[1])
+            ctx.init()
+            hs = ctx.run(host_loop=True)
+            hp, hr = ctx.read_props(), ctx.read_ranks()
+            ctx.init()
+            ds = ctx.run()
+            assert hs["device_loop"] == 0 and ds["device_loop"] == 1
+            if algo == g.GRD_PR_DELTA:
+                assert abs(ds["rounds"] - hs["rounds"]) <= 1
+                np.testing.assert_allclose(ctx.read_ranks(), hr, rtol=1e-4, atol=2e-5)
+                continue
+            np.testing.assert_array_equal(ctx.read_props(), hp)
+            for k in ("rounds", "converged", "edges_scanned", "bytes_synced", "reference_bytes_moved",
+                      "push_rounds", "pull_rounds", "actives_total", "push_actives"):
+                assert ds[k] == hs[k], k
+            # the device loop adds its policy and round-end kernels each round
+            assert ds["kernel_launches"] == hs["kernel_launches"] + 2 * ds["rounds"]
+
+
+def test_device_loop_respects_round_cap(gpu):
+    G = g.Graph.grid(30)
+    with g.Context(G) as ctx:
+        ctx.set_algo(g.GRD_SSSP_HOP, max_rounds=5)
+        ctx.init()
+        st = ctx.run()
+        assert st["device_loop"] == 1 and st["rounds"] == 5 and st["converged"] == 0
+        ref = O.run(O.ORC_SSSP_HOP, G.row_offsets, G.col_indices, max_rounds=5)
+        np.testing.assert_array_equal(ctx.read_props(), ref["props"])
+
+
 @pytest.mark.parametrize("num_memory", [1, 3])
 def test_stage_api_matches_oracle_round_by_round(gpu, num_memory):
     G = g.Graph.rmat(11, 8, symmetrize=True, weighted=True)
