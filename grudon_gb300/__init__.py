@@ -294,6 +294,19 @@ class Context:
     def set_profiling(self, enable: bool = True) -> None:
         self._check(self._lib.grd_set_profiling(self._ctx, int(enable)))
 
+    def round_log(self) -> list:
+        """Per-round records of profiled host-loop runs since grd_init."""
+        n = C.c_size_t()
+        self._check(self._lib.grd_get_round_log(self._ctx, None, 0, C.byref(n)))
+        recs = (_ffi.grd_round_rec * max(1, n.value))()
+        self._check(self._lib.grd_get_round_log(self._ctx, recs, n.value, C.byref(n)))
+        out = []
+        for r in recs[: n.value]:
+            d = {f: getattr(r, f) for f, _ in _ffi.grd_round_rec._fields_}
+            d["ms"] = list(d["ms"])
+            out.append(d)
+        return out
+
     def upload(self) -> int:
         b = C.c_uint64()
         self._check(self._lib.grd_upload(self._ctx, C.byref(b)))

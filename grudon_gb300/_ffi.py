@@ -55,6 +55,11 @@ class grd_stats(C.Structure):
                 ("device_loop", C.c_uint32), ("push_actives", C.c_uint64)]
 
 
+class grd_round_rec(C.Structure):
+    _fields_ = [("round", C.c_uint32), ("mode", C.c_int32), ("frontier_in", C.c_uint64), ("actives", C.c_uint64),
+                ("edges", C.c_uint64), ("frontier_out", C.c_uint64), ("ms", C.c_double * 5)]
+
+
 class grd_host_graph(C.Structure):
     _fields_ = [("num_vertices", C.c_uint32), ("num_edges", C.c_uint64), ("row_offsets", u64p),
                 ("col_indices", u32p), ("weights", u32p), ("seed", C.c_uint64)]
@@ -81,6 +86,7 @@ SIGNATURES = {
     "grd_run": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(grd_stats)]),
     "grd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(grd_stats)]),
     "grd_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "grd_get_round_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "grd_read_props": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_ranks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_updates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),

@@ -182,6 +182,17 @@ int check_ready(grd_ctx* ctx) {
 
 uint32_t grid_for(grd_ctx* ctx, uint32_t blocks_per_sm) { return (uint32_t)ctx->num_sms * blocks_per_sm; }
 
+// One full wave of a grid-stride kernel: SMs x resident 256-thread blocks.
+template <class Kernel>
+uint32_t resident_grid(grd_ctx* ctx, Kernel k) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, 0) != cudaSuccess || per_sm <= 0) {
+    (void)cudaGetLastError();
+    per_sm = 4;
+  }
+  return (uint32_t)ctx->num_sms * (uint32_t)per_sm;
+}
+
 // Dense rounds (reductions only, dirty set rebuilt by one linear pass) pay an
 // O(S) pass; sparse rounds pay a returned atomic per improving edge.  The
 // fixed rule takes the dense form when the frontier entering the round is at
@@ -260,11 +271,11 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
     const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
     const bool dense = mode == MODE_PUSH_DENSE;
     if (dense) {
-      k_push_lbs<A, true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      k_push_lbs<A, true><<<resident_grid(ctx, k_push_lbs<A, true>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       k_diff_dirty<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     } else {
-      k_push_lbs<A, false><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      k_push_lbs<A, false><<<resident_grid(ctx, k_push_lbs<A, false>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       if (ctx->g.num_hubs) k_hub_push<A, false><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     }
     CK_LAUNCH();
@@ -343,14 +354,19 @@ void grd_prof_mark(grd_ctx* ctx, int i) {
   if (ctx->profiling) cudaEventRecord(ctx->ev[i], ctx->stream);
 }
 
-void grd_prof_collect(grd_ctx* ctx) {
+void grd_prof_collect(grd_ctx* ctx, double* out) {
   if (!ctx->profiling) return;
   float ms;
-  for (int i = 0; i < 4; ++i)
-    if (cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]) == cudaSuccess) ctx->stats.stage_ms[i] += ms;
-  if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[4]) == cudaSuccess) ctx->stats.stage_ms[4] += ms;
+  for (int i = 0; i < 5; ++i) {
+    const cudaEvent_t a = ctx->ev[i < 4 ? i : 0], b = ctx->ev[i < 4 ? i + 1 : 4];
+    const double v = cudaEventElapsedTime(&ms, a, b) == cudaSuccess ? ms : 0.0;
+    ctx->stats.stage_ms[i] += v;
+    if (out) out[i] = v;
+  }
   (void)cudaGetLastError();
 }
+
+void grd_prof_collect(grd_ctx* ctx) { grd_prof_collect(ctx, nullptr); }
 
 // ------------------------------------------------------------------ C ABI --
 extern "C" {
@@ -501,6 +517,7 @@ int grd_init(grd_ctx* ctx) {
   ctx->stats = grd_stats{};
   ctx->stats.kernel_launches = 1;
   ctx->pull.edges = 0;
+  ctx->round_log.clear();
   ctx->inited = true;
   return GRD_OK;
 }
@@ -564,19 +581,31 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
   } else {
     uint64_t f = 1;
     while (ctx->stats.rounds < ctx->params.max_rounds) {
+      const uint64_t f_in = ctx->last_frontier, e_in = ctx->stats.edges_scanned;
       grd_prof_mark(ctx, 0);
       TRY(grd_enqueue_fwd(ctx, true));
       grd_prof_mark(ctx, 1);
       TRY(grd_enqueue_edge_map(ctx));
+      const int mode = ctx->last_mode;
       grd_prof_mark(ctx, 2);
       TRY(grd_enqueue_bwd(ctx, true, true, true));
       grd_prof_mark(ctx, 3);
       TRY(grd_enqueue_update(ctx));
       grd_prof_mark(ctx, 4);
       TRY(grd_read_counters(ctx));
-      grd_prof_collect(ctx);
-      ctx->stats.rounds++;
       f = ctx->h_counters[C_FRONTIER];
+      if (ctx->profiling) {
+        grd_round_rec rec{};
+        rec.round = ctx->stats.rounds;
+        rec.mode = mode;
+        rec.frontier_in = f_in;
+        rec.actives = ctx->h_counters[C_ACTIVE];
+        rec.edges = ctx->stats.edges_scanned - e_in;
+        rec.frontier_out = f;
+        grd_prof_collect(ctx, rec.ms);
+        ctx->round_log.push_back(rec);
+      }
+      ctx->stats.rounds++;
       if (f == 0) break;
     }
     ctx->stats.converged = (f == 0);
@@ -627,6 +656,13 @@ int grd_aggregate_values(grd_ctx* ctx, const uint32_t* gids, const uint32_t* val
 int grd_get_stats(const grd_ctx* ctx, grd_stats* stats) {
   if (!ctx || !stats) return GRD_E_INVALID;
   *stats = ctx->stats;
+  return GRD_OK;
+}
+
+int grd_get_round_log(const grd_ctx* ctx, grd_round_rec* out, size_t cap, size_t* n) {
+  if (!ctx) return GRD_E_INVALID;
+  if (n) *n = ctx->round_log.size();
+  if (out) std::memcpy(out, ctx->round_log.data(), sizeof(grd_round_rec) * std::min(cap, ctx->round_log.size()));
   return GRD_OK;
 }
 

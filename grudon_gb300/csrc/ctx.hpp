@@ -37,6 +37,7 @@ struct grd_ctx {
   bool in_edges_alloc = false;
   PullState pull;
   uint64_t last_frontier = 0;  // |frontier| entering the next round
+  std::vector<grd_round_rec> round_log;  // profiled host-loop rounds
   int last_mode = -1;          // edge-map mode of the round in flight (host loop)
   cudaGraph_t run_graph = nullptr;     // device-driven round loop (graph_run.cu)
   cudaGraphExec_t run_exec = nullptr;

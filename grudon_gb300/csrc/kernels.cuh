@@ -148,6 +148,7 @@ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
 template <int A>
 __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t source, double damping) {
   const uint64_t n = g.S > g.V ? g.S : g.V;
+  uint32_t fcount = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ((n + 31) & ~31ull);
        i += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t fbit = 0;
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t 
     if (lane_id() == 0 && i < g.V) {
       st.F[i >> 5] = m;
       st.UD[i >> 5] = 0;
-      if (m) atomicAdd(&st.counters[C_FRONTIER], (unsigned long long)__popc(m));
+      fcount += __popc(m);
     }
     if (i < g.S) {
       const uint32_t x = (A == A_PR_DELTA || A == A_PR_PULL) ? 0u : 0xFFFFFFFFu;
@@ -192,6 +193,8 @@ __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t 
       }
     }
   }
+  fcount = block_sum(fcount);  // one counter update per block
+  if (threadIdx.x == 0 && fcount) atomicAdd(&st.counters[C_FRONTIER], (unsigned long long)fcount);
 }
 
 // ---------------------------------------------------- forward sync: bits --
@@ -663,54 +666,69 @@ static __global__ void __launch_bounds__(256) k_deg_down(DevGraph g, DevState st
   }
 }
 
-// One warp per 256-edge chunk.  The warp loads a window of 32 consecutive
-// actives (their DP, row start and source value); each lane finds the source
-// of each of its edges by a 5-step shuffle binary search over the window, so
-// lanes read consecutive edge slots.  All 8 edges of a lane are loaded (index,
-// weight, current value) before any update is issued, keeping 8 independent
-// memory chains in flight per lane; the window slides until the chunk is done.
+// One warp per 256-edge chunk.  The warp stages a window of LBS_WIN
+// consecutive actives (their DP, row start and source value) in shared memory
+// with 8 independent coalesced loads per lane — one window covers the whole
+// chunk unless more than LBS_WIN actives fall inside it — then each lane
+// finds the source of each of its 8 edges by an 8-step binary search in
+// shared memory, so lanes read consecutive edge slots.  All 8 edges of a lane
+// are loaded (index, weight, current value) before any update is issued,
+// keeping 8 independent memory chains in flight per lane.
+constexpr uint32_t LBS_WIN = 256;
+
 template <int A, bool kDense>
 __global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
   constexpr int B = LBS_CHUNK / 32;
+  constexpr int SW = LBS_WIN / 32;
+  __shared__ uint32_t s_dp[8][LBS_WIN + 1];
+  __shared__ uint32_t s_rb[8][LBS_WIN];
+  __shared__ uint32_t s_sv[8][LBS_WIN];
   const uint32_t K = (uint32_t)__ldcg(&st.counters[C_ACTIVE]);
   const uint32_t m = (uint32_t)__ldcg(&st.counters[C_MEDGES]);
-  const uint32_t lane = lane_id();
+  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
   const uint32_t nchunks = (m + LBS_CHUNK - 1) / LBS_CHUNK;
   const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
+  uint32_t* dp = s_dp[w];
+  uint32_t* rbs = s_rb[w];
+  uint32_t* svs = s_sv[w];
+  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + w; c < nchunks; c += nwarps) {
     uint32_t e = c * LBS_CHUNK;
     const uint32_t e_end = min(m, e + LBS_CHUNK);
     uint32_t i0 = st.chunk_start[c];
     while (e < e_end) {
-      const uint32_t idx = i0 + lane;
-      uint32_t dpl = m, dpe = m, rb = 0, sv = 0;
-      if (idx < K) {
-        dpl = st.DP[idx];
-        dpe = st.DP[idx + 1];
-        rb = st.RB[idx];
-        sv = source_value<A>(st.SV[idx]);
+      uint32_t a[SW], b[SW], v[SW];
+#pragma unroll
+      for (int k = 0; k < SW; ++k) {
+        const uint32_t idx = i0 + k * 32 + lane;
+        a[k] = idx < K ? st.DP[idx] : m;
+        b[k] = idx < K ? st.RB[idx] : 0u;
+        v[k] = idx < K ? st.SV[idx] : 0u;
       }
-      const uint32_t wend = min(e_end, __shfl_sync(FULL, dpe, 31));
+      const uint32_t tail = (lane == 0) ? (i0 + LBS_WIN < K ? st.DP[i0 + LBS_WIN] : m) : 0u;
+#pragma unroll
+      for (int k = 0; k < SW; ++k) {
+        dp[k * 32 + lane] = a[k];
+        rbs[k * 32 + lane] = b[k];
+        svs[k * 32 + lane] = source_value<A>(v[k]);
+      }
+      if (lane == 0) dp[LBS_WIN] = tail;
+      __syncwarp();
+      const uint32_t wend = min(e_end, dp[LBS_WIN]);
       uint32_t dst[B], cand[B], cur[B];
 #pragma unroll
       for (int k = 0; k < B; ++k) {
         const uint32_t eid = e + k * 32 + lane;
-        uint32_t lo = 0;
-#pragma unroll
-        for (uint32_t step = 16; step; step >>= 1) {
-          const uint32_t cnd = lo + step;
-          const uint32_t x = __shfl_sync(FULL, dpl, cnd);
-          if (x <= eid) lo = cnd;
-        }
-        const uint32_t sd = __shfl_sync(FULL, dpl, lo);
-        const uint32_t sr = __shfl_sync(FULL, rb, lo);
-        const uint32_t ssv = __shfl_sync(FULL, sv, lo);
         dst[k] = 0xFFFFFFFFu;
-        cand[k] = ssv;
+        cand[k] = 0;
         if (eid < wend) {
-          const uint32_t ed = sr + (eid - sd);
+          uint32_t lo = 0;
+#pragma unroll
+          for (uint32_t step = LBS_WIN / 2; step; step >>= 1)
+            if (dp[lo + step] <= eid) lo += step;
+          const uint32_t ed = rbs[lo] + (eid - dp[lo]);
           dst[k] = __ldg(&g.col[ed]);
-          if (A == A_SSSP_W) cand[k] = relax_cand<A>(ssv, __ldg(&g.wgt[ed]));
+          cand[k] = svs[lo];
+          if (A == A_SSSP_W) cand[k] = relax_cand<A>(cand[k], __ldg(&g.wgt[ed]));
         }
       }
 #pragma unroll
@@ -718,8 +736,9 @@ __global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
 #pragma unroll
       for (int k = 0; k < B; ++k)
         if (dst[k] != 0xFFFFFFFFu) relax_apply<A, kDense>(st, dst[k], cand[k], cur[k]);
+      __syncwarp();
       e = wend;
-      i0 += 32;
+      i0 += LBS_WIN;
     }
   }
 }

@@ -176,8 +176,23 @@ int grd_aggregate_values_noalloc(grd_ctx* ctx, const uint32_t* gids,
  * or params.max_rounds.  flags: GRD_RUN_STRICT. */
 int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats);
 int grd_get_stats(const grd_ctx* ctx, grd_stats* stats);
-/* Per-stage CUDA-event timing inside grd_run (off by default). */
+/* Per-stage CUDA-event timing inside grd_run (off by default).  While it is
+ * on, grd_run drives the rounds from the host and records one grd_round_rec
+ * per round (cleared by grd_init). */
 int grd_set_profiling(grd_ctx* ctx, int enable);
+
+typedef struct grd_round_rec {
+  uint32_t round;         /* 0-based round index                          */
+  int32_t mode;           /* 0 push sparse, 1 push dense, 2 pull          */
+  uint64_t frontier_in;   /* |frontier| entering the round                */
+  uint64_t actives;       /* actives unpacked by the forward sync         */
+  uint64_t edges;         /* edges the edge-map read this round           */
+  uint64_t frontier_out;  /* |frontier| after the update                  */
+  double ms[5];           /* fwd, edge-map, bwd+aggregate, update, round  */
+} grd_round_rec;
+/* Copies up to cap records; *n = number recorded. */
+int grd_get_round_log(const grd_ctx* ctx, grd_round_rec* out, size_t cap,
+                      size_t* n);
 
 /* Results (blocking device->host copies) -----------------------------------*/
 /* Compute-side vertex_properties, gid order (uint32 for CC/SSSP, float for PR
