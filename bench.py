@@ -48,7 +48,95 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pagerank", action="store_true")
     ap.add_argument("--pr-scale", type=int, default=24)
+    ap.add_argument("--batch", action="store_true", help="run the batched workload (default at N=1)")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-graphs", type=int, default=512)
+    ap.add_argument("--batch-sources", type=int, default=64)
     return ap.parse_args()
+
+
+def bench_batch(g, args, local) -> dict:
+    """Batched workload: (1) 512 graphs (log-uniform scale 10..18, ef in
+    {4,8,16,32}, half RMAT / half ER) each running CC and 20-iteration
+    PageRank; (2) 64 SSSP sources on one RMAT-20 graph (w in [1,255]).
+    Plain = one ctx per graph (per source), run one after another with the
+    fixed schedule; batched = one disjoint union per algorithm, schedule
+    picked by the autotuner, one device-driven launch per algorithm."""
+    import numpy as np
+    from grudon_gb300 import autotune
+    from grudon_gb300 import batch as B
+    t_gen = time.perf_counter()
+    spec = B.batch_spec(args.batch_graphs)
+    sym = [B.make_graph(s, symmetrize=True) for s in spec]
+    dirg = [B.make_graph(s) for s in spec]
+    t_gen = time.perf_counter() - t_gen
+    E1 = sum(x.num_edges for x in sym) + 20 * sum(x.num_edges for x in dirg)
+    _, _, plain_s = B.run_plain_graphs(sym, dirg, 20, local)
+    Uc, Up = B.Union(sym), B.Union(dirg)
+    tune_cc = autotune.tune(Uc.graph, g.GRD_CC, lambda c: c.init(), device=local, reps=2)
+    best = tune_cc.best
+    part = Uc.graph.partition_edge_balanced(best.num_memory) if best.num_memory > 1 else None
+    ctx_c = g.Context(Uc.graph, part, best.num_memory, local)
+    ctx_c.set_algo(g.GRD_CC, **best.params())
+    part = Up.graph.partition_edge_balanced(best.num_memory) if best.num_memory > 1 else None
+    ctx_p = g.Context(Up.graph, part, best.num_memory, local)
+    ctx_p.set_algo(g.GRD_PR_PULL, max_rounds=20, tolerance=0.0)
+    for c in (ctx_c, ctx_p):  # warm-up
+        c.init()
+        c.run()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for c in (ctx_c, ctx_p):
+            c.init()
+            c.run()
+    ctx_c.synchronize()
+    batched_s = (time.perf_counter() - t0) / reps
+    ctx_c.close()
+    ctx_p.close()
+    part1 = {"graphs": len(spec), "vertices": int(Uc.sizes.sum()), "edges_cc": Uc.graph.num_edges,
+             "edges_pr": Up.graph.num_edges, "generate_s": t_gen,
+             "plain_s": plain_s, "batched_s": batched_s, "speedup": plain_s / batched_s,
+             "batched_gteps": E1 / batched_s / 1e9, "plain_gteps": E1 / plain_s / 1e9,
+             "autotuned": best.__dict__, "tune_table_ms": [round(r["ms"], 3) for r in tune_cc.table]}
+
+    # (2) multi-source SSSP
+    G = g.Graph.rmat(20, 16, weighted=True)
+    rng = np.random.default_rng(0x53535350)
+    sources = rng.integers(0, G.num_vertices, args.batch_sources)
+    c1 = g.Context(G, None, 1, local)
+    c1.set_algo(g.GRD_SSSP_W)
+    c1.init()
+    c1.run()
+    t0 = time.perf_counter()
+    for s in sources:
+        c1.set_algo(g.GRD_SSSP_W, source=int(s))
+        c1.init()
+        c1.run()
+    c1.synchronize()
+    plain2 = time.perf_counter() - t0
+    c1.close()
+    U = B.Union([G] * len(sources))
+    c2 = g.Context(U.graph, None, 1, local)
+    c2.set_algo(g.GRD_SSSP_W)
+    srcs = U.bases + sources
+    c2.init_sources(srcs)
+    c2.run()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        c2.init_sources(srcs)
+        st = c2.run()
+    c2.synchronize()
+    batched2 = (time.perf_counter() - t0) / reps
+    c2.close()
+    E2 = len(sources) * G.num_edges
+    part2 = {"sources": len(sources), "graph": "RMAT-20 ef16 w in [1,255]", "plain_s": plain2,
+             "batched_s": batched2, "speedup": plain2 / batched2, "rounds": st["rounds"],
+             "batched_gteps": E2 / batched2 / 1e9, "plain_gteps": E2 / plain2 / 1e9}
+    total_plain, total_batched = plain_s + plain2, batched_s + batched2
+    return {"part1_graphs": part1, "part2_sssp_sources": part2,
+            "end_to_end_speedup": total_plain / total_batched,
+            "note": "batched and plain both use the fixed per-round heuristic; timings exclude layout build"}
 
 
 def bench_pagerank(g, args, local, hbm_peak, barrier, ws) -> dict:
@@ -369,6 +457,7 @@ def main():
     pr = None
     if not args.no_pagerank:
         pr = bench_pagerank(g, args, local, hbm_peak, barrier, ws)
+    batch = bench_batch(g, args, local) if (args.batch or (ws == 1 and not args.no_batch)) else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
@@ -387,6 +476,8 @@ def main():
             pr.pop("_graph", None)
             pr.pop("_ranks", None)
             line["pagerank_rmat24"] = pr
+        if batch is not None:
+            line["batch"] = batch
         print(json.dumps(line), flush=True)
     ctx_cc.close()
     ctx_ss.close()

@@ -232,17 +232,24 @@ class Context:
 
     def set_algo(self, algo, source: int = 0, max_rounds: int = 1000, damping: float = 0.85,
                  tolerance: Optional[float] = None, direction: int = GRD_DIR_AUTO,
-                 frontier_format: int = GRD_FMT_AUTO) -> None:
+                 frontier_format: int = GRD_FMT_AUTO, dense_div: int = 0, pull_div: int = 0,
+                 push_blocks_per_sm: int = 0) -> None:
         if isinstance(algo, str):
             algo = ALGO_NAMES[algo]
         if tolerance is None:
             tolerance = 1e-7 if algo == GRD_PR_PULL else 1e-6
-        p = _ffi.grd_params(source, max_rounds, damping, tolerance, direction, frontier_format)
+        p = _ffi.grd_params(source, max_rounds, damping, tolerance, direction, frontier_format, dense_div, pull_div,
+                            push_blocks_per_sm)
         self._check(self._lib.grd_set_algo(self._ctx, algo, C.byref(p)))
         self.algo = algo
 
     def init(self) -> None:
         self._check(self._lib.grd_init(self._ctx))
+
+    def init_sources(self, sources) -> None:
+        """SSSP init with several sources at distance 0."""
+        s = _u32(sources)
+        self._check(self._lib.grd_init_sources(self._ctx, s.ctypes.data_as(_ffi.u32p), len(s)))
 
     def sync_fwd(self) -> None:
         self._check(self._lib.grd_sync_fwd(self._ctx))

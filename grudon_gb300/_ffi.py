@@ -44,7 +44,8 @@ class grd_csr(C.Structure):
 
 class grd_params(C.Structure):
     _fields_ = [("source", C.c_uint32), ("max_rounds", C.c_uint32), ("damping", C.c_double),
-                ("tolerance", C.c_double), ("direction", C.c_int), ("frontier_format", C.c_int)]
+                ("tolerance", C.c_double), ("direction", C.c_int), ("frontier_format", C.c_int),
+                ("dense_div", C.c_uint32), ("pull_div", C.c_uint32), ("push_blocks_per_sm", C.c_uint32)]
 
 
 class grd_stats(C.Structure):
@@ -76,6 +77,7 @@ SIGNATURES = {
     "grd_upload": (C.c_int, [C.c_void_p, u64p]),
     "grd_set_algo": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(grd_params)]),
     "grd_init": (C.c_int, [C.c_void_p]),
+    "grd_init_sources": (C.c_int, [C.c_void_p, u32p, C.c_size_t]),
     "grd_sync_fwd": (C.c_int, [C.c_void_p]),
     "grd_edge_map": (C.c_int, [C.c_void_p]),
     "grd_sync_bwd": (C.c_int, [C.c_void_p]),

@@ -186,6 +186,7 @@ uint32_t grid_for(grd_ctx* ctx, uint32_t blocks_per_sm) { return (uint32_t)ctx->
 template <class Kernel>
 uint32_t resident_grid(grd_ctx* ctx, Kernel k) {
   int per_sm = 0;
+  if (ctx->params.push_blocks_per_sm) return (uint32_t)ctx->num_sms * ctx->params.push_blocks_per_sm;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, 0) != cudaSuccess || per_sm <= 0) {
     (void)cudaGetLastError();
     per_sm = 4;
@@ -200,7 +201,7 @@ uint32_t resident_grid(grd_ctx* ctx, Kernel k) {
 bool use_dense(const grd_ctx* ctx) {
   if (ctx->params.frontier_format == GRD_FMT_BITVEC) return true;
   if (ctx->params.frontier_format == GRD_FMT_LIST) return false;
-  return ctx->last_frontier * 32 >= ctx->g.S;
+  return ctx->last_frontier * ctx->params.dense_div >= ctx->g.S;
 }
 
 // Direction: the pull map reads every in-edge once; the push map reads only
@@ -212,7 +213,7 @@ bool use_pull(const grd_ctx* ctx) {
   if (!ctx->in_edges_alloc) return false;
   if (ctx->params.direction == GRD_DIR_PULL) return true;
   if (ctx->params.direction == GRD_DIR_PUSH) return false;
-  return ctx->last_frontier * 2 >= ctx->g.V;
+  return ctx->last_frontier * ctx->params.pull_div >= ctx->g.V;
 }
 
 }  // namespace
@@ -475,6 +476,12 @@ int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
   p.direction = GRD_DIR_AUTO;
   p.frontier_format = GRD_FMT_AUTO;
   if (params) p = *params;
+  if (p.dense_div == 0) p.dense_div = 32;
+  if (p.pull_div == 0) p.pull_div = 2;
+  if (p.push_blocks_per_sm > 32) {
+    ctx->err = "push_blocks_per_sm must be <= 32";
+    return GRD_E_INVALID;
+  }
   if ((algo == GRD_SSSP_HOP || algo == GRD_SSSP_W) && p.source >= ctx->L.V) {
     ctx->err = "SSSP source out of range";
     return GRD_E_INVALID;
@@ -519,6 +526,54 @@ int grd_init(grd_ctx* ctx) {
   ctx->pull.edges = 0;
   ctx->round_log.clear();
   ctx->inited = true;
+  return GRD_OK;
+}
+
+static __global__ void k_seed_sources(DevState st, const uint32_t* src, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t s = src[i];
+    st.prop[s] = 0;
+    st.upd[s] = 0;
+    atomicOr(&st.F[s >> 5], 1u << (s & 31));
+  }
+}
+
+int grd_init_sources(grd_ctx* ctx, const uint32_t* sources, size_t n) {
+  if (!ctx) return GRD_E_INVALID;
+  if (ctx->algo != GRD_SSSP_HOP && ctx->algo != GRD_SSSP_W) {
+    ctx->err = "grd_init_sources applies to SSSP only";
+    return GRD_E_INVALID;
+  }
+  if (!sources || n == 0 || n > 0xFFFFFFFFull) return GRD_E_INVALID;
+  std::vector<uint32_t> src(sources, sources + n);
+  std::sort(src.begin(), src.end());
+  src.erase(std::unique(src.begin(), src.end()), src.end());
+  if (src.back() >= ctx->L.V) {
+    ctx->err = "source out of range";
+    return GRD_E_INVALID;
+  }
+  const uint32_t saved = ctx->params.source;
+  ctx->params.source = 0xFFFFFFFFu;  // init with no source, then seed them all
+  const int rc = grd_init(ctx);
+  ctx->params.source = saved;
+  TRY(rc);
+  const size_t m = src.size();
+  if (ctx->agg_cap < m) {
+    void* p = nullptr;
+    TRY(grd_dev_alloc_bytes(ctx, &p, sizeof(uint32_t) * 2 * m));
+    ctx->agg_buf = static_cast<uint32_t*>(p);
+    ctx->agg_cap = m;
+  }
+  CK(cudaMemcpyAsync(ctx->agg_buf, src.data(), sizeof(uint32_t) * m, cudaMemcpyHostToDevice, ctx->stream));
+  k_seed_sources<<<(uint32_t)std::min<size_t>((m + 255) / 256, grid_for(ctx, 4)), 256, 0, ctx->stream>>>(
+      ctx->st, ctx->agg_buf, (uint32_t)m);
+  CK_LAUNCH();
+  ctx->h_seed[0] = m;
+  CK(cudaMemcpyAsync(ctx->st.counters + C_FRONTIER, ctx->h_seed, sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->last_frontier = m;
+  ctx->stats.kernel_launches += 1;
   return GRD_OK;
 }
 

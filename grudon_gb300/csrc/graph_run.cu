@@ -24,6 +24,7 @@ namespace {
 
 struct PolicyArgs {
   int direction, format, has_in;
+  uint32_t dense_div, pull_div;
   uint32_t launches[3];  // kernels of one round per edge-map mode
   unsigned long long edges;
 };
@@ -31,8 +32,9 @@ struct PolicyArgs {
 __global__ void k_policy(DevGraph g, DevState st, cudaGraphConditionalHandle sw, PolicyArgs a) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   const unsigned long long f = st.counters[C_FRONTIER];
-  const bool pull = a.has_in && (a.direction == GRD_DIR_PULL || (a.direction == GRD_DIR_AUTO && f * 2 >= g.V));
-  const bool dense = a.format == GRD_FMT_BITVEC || (a.format == GRD_FMT_AUTO && f * 32 >= g.S);
+  const bool pull =
+      a.has_in && (a.direction == GRD_DIR_PULL || (a.direction == GRD_DIR_AUTO && f * a.pull_div >= g.V));
+  const bool dense = a.format == GRD_FMT_BITVEC || (a.format == GRD_FMT_AUTO && f * a.dense_div >= g.S);
   const int mode = pull ? MODE_PULL : (dense ? MODE_PUSH_DENSE : MODE_PUSH_SPARSE);
   st.counters[C_MODE] = mode;
   if (pull) {
@@ -115,6 +117,8 @@ int build(grd_ctx* ctx) {
   pa.direction = ctx->params.direction;
   pa.format = ctx->params.frontier_format;
   pa.has_in = ctx->in_edges_alloc ? 1 : 0;
+  pa.dense_div = ctx->params.dense_div;
+  pa.pull_div = ctx->params.pull_div;
   pa.edges = ctx->L.E;
   const uint32_t base = 3 /*fwd*/ + 1 /*policy*/ + 2 /*bwd pack*/ + (ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1) +
                         1 /*update*/ + 1 /*round end*/;

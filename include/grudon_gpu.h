@@ -88,6 +88,11 @@ typedef struct grd_params {
                            PR_PULL: stop when L1 residual / V < tolerance    */
   int direction;        /* GRD_DIR_*                                          */
   int frontier_format;  /* GRD_FMT_*                                          */
+  /* Schedule knobs (0 = built-in default); results never depend on them.   */
+  uint32_t dense_div;   /* dense dirty tracking when |F| >= S / dense_div (32)*/
+  uint32_t pull_div;    /* AUTO pulls when |F| >= V / pull_div (2); needs the
+                           in-edge view                                       */
+  uint32_t push_blocks_per_sm; /* push grid; 0 = occupancy limit            */
 } grd_params;
 
 typedef struct grd_stats {
@@ -141,6 +146,9 @@ int grd_upload(grd_ctx* ctx, uint64_t* bytes_copied);
 /* Algorithm selection and per-stage round API -----------------------------*/
 int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params);
 int grd_init(grd_ctx* ctx);
+/* SSSP init with several sources at distance 0 (e.g. one per copy of a
+ * disjoint-union batch); other algorithms: GRD_E_INVALID. */
+int grd_init_sources(grd_ctx* ctx, const uint32_t* sources, size_t n);
 int grd_sync_fwd(grd_ctx* ctx);
 int grd_edge_map(grd_ctx* ctx);
 int grd_sync_bwd(grd_ctx* ctx);
