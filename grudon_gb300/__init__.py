@@ -14,12 +14,14 @@ import numpy as np
 
 from . import _ffi
 from ._ffi import (GRD_CC, GRD_DIR_AUTO, GRD_DIR_PULL, GRD_DIR_PUSH, GRD_FMT_AUTO, GRD_FMT_BITVEC,
-                   GRD_FMT_LIST, GRD_PR_DELTA, GRD_PR_PULL, GRD_RUN_STRICT, GRD_SSSP_HOP, GRD_SSSP_W)
+                   GRD_FMT_LIST, GRD_PR_DELTA, GRD_PR_PULL, GRD_ROUND_PULL_BITVEC, GRD_ROUND_PULL_LIST,
+                   GRD_ROUND_PUSH_BITVEC, GRD_ROUND_PUSH_LIST, GRD_RUN_STRICT, GRD_SSSP_HOP, GRD_SSSP_W)
 
 __all__ = [
     "GrdError", "Graph", "Context", "lib", "device_count", "rmat_seed",
     "GRD_PR_DELTA", "GRD_PR_PULL", "GRD_CC", "GRD_SSSP_HOP", "GRD_SSSP_W",
     "GRD_DIR_AUTO", "GRD_DIR_PUSH", "GRD_DIR_PULL", "GRD_FMT_AUTO", "GRD_FMT_BITVEC", "GRD_FMT_LIST",
+    "GRD_ROUND_PUSH_BITVEC", "GRD_ROUND_PUSH_LIST", "GRD_ROUND_PULL_BITVEC", "GRD_ROUND_PULL_LIST",
     "GRD_RUN_STRICT", "ALGO_NAMES",
 ]
 

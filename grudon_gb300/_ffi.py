@@ -24,6 +24,7 @@ GRD_SSSP_W = 4
 
 GRD_DIR_AUTO, GRD_DIR_PUSH, GRD_DIR_PULL = 0, 1, 2
 GRD_FMT_AUTO, GRD_FMT_BITVEC, GRD_FMT_LIST = 0, 1, 2
+GRD_ROUND_PUSH_BITVEC, GRD_ROUND_PUSH_LIST, GRD_ROUND_PULL_BITVEC, GRD_ROUND_PULL_LIST = 0, 1, 2, 3
 GRD_RUN_STRICT = 1
 GRD_RUN_HOST_LOOP = 2
 
@@ -58,7 +59,8 @@ class grd_stats(C.Structure):
 
 class grd_round_rec(C.Structure):
     _fields_ = [("round", C.c_uint32), ("mode", C.c_int32), ("frontier_in", C.c_uint64), ("actives", C.c_uint64),
-                ("edges", C.c_uint64), ("frontier_out", C.c_uint64), ("ms", C.c_double * 5)]
+                ("edges", C.c_uint64), ("frontier_out", C.c_uint64), ("ms", C.c_double * 5),
+                ("frontier_edges_in", C.c_uint64), ("max_degree_in", C.c_uint64), ("unvisited_in", C.c_uint64)]
 
 
 class grd_host_graph(C.Structure):

@@ -61,6 +61,13 @@ int alloc_and_upload(grd_ctx* ctx) {
   g.S = L.S;
   g.num_tiles = (uint32_t)L.num_tiles();
   g.num_hubs = (uint32_t)L.hubs.size();
+  g.E = L.E;
+  g.bv_bytes = g.bv_refbytes = 0;
+  for (uint32_t p = 0; p < L.M; ++p) {
+    const unsigned long long words64 = ((unsigned long long)L.T(p) + 63ull) / 64ull;
+    g.bv_bytes += words64 * 8ull;
+    g.bv_refbytes += words64 * 64ull;
+  }
   const size_t V = L.V, S = L.S, E = L.E, M = L.M, T = L.num_tiles();
   const size_t VW = (V + 31) / 32, SW = S / 32;
   TRY(dev_alloc(ctx, (uint32_t**)&g.slot_gid, S));
@@ -97,7 +104,13 @@ int alloc_and_upload(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, &st.blk_sum, lbs_blocks(ctx)));
   TRY(dev_alloc(ctx, &st.blk_off, lbs_blocks(ctx)));
   TRY(dev_alloc(ctx, &st.counters, NUM_COUNTERS));
+  TRY(dev_alloc(ctx, &st.FL, V));
+  TRY(dev_alloc(ctx, &st.DL, S));
+  TRY(dev_alloc(ctx, &st.UL, V));
+  TRY(dev_alloc(ctx, &st.own_slot, V));
+  TRY(dev_alloc(ctx, &st.lc, NUM_LIST_COUNTERS));
   CK(cudaMemsetAsync(st.counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, ctx->stream));
+  CK(cudaMemsetAsync(st.lc, 0, sizeof(uint32_t) * NUM_LIST_COUNTERS, ctx->stream));
   return GRD_OK;
 }
 
@@ -124,6 +137,16 @@ int grd_upload_layout(grd_ctx* ctx) {
   for (uint32_t p = 0; p < L.M; ++p) T[p] = L.T(p);
   TRY(upload(ctx, (uint32_t*)g.part_T, T));
   TRY(upload(ctx, (uint32_t*)g.part_owned, L.n_owned));
+  {
+    // gid -> owned global slot (the first n_owned slots of each partition).
+    std::vector<uint32_t> own(L.V);
+    for (uint32_t p = 0; p < L.M; ++p)
+      for (uint32_t k = 0; k < L.n_owned[p]; ++k) own[L.slot_gid[L.slot_base[p] + k]] = L.slot_base[p] + k;
+    CK(cudaMemcpyAsync(ctx->st.own_slot, own.data(), sizeof(uint32_t) * own.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // `own` is a temporary
+    ctx->upload_bytes += sizeof(uint32_t) * own.size();
+  }
   if (ctx->in_edges_alloc) {
     TRY(upload(ctx, (uint32_t*)g.in_off, L.in_off));
     TRY(upload(ctx, (uint32_t*)g.in_src, L.in_src));
@@ -194,21 +217,25 @@ uint32_t resident_grid(grd_ctx* ctx, Kernel k) {
   return (uint32_t)ctx->num_sms * (uint32_t)per_sm;
 }
 
-// Dense rounds (reductions only, dirty set rebuilt by one linear pass) pay an
-// O(S) pass; sparse rounds pay a returned atomic per improving edge.  The
-// fixed rule takes the dense form when the frontier entering the round is at
-// least 1/32 of the slot space.  GRD_FMT_BITVEC / GRD_FMT_LIST force it.
+// Round format.  Bitvector rounds sync through per-partition bitvectors
+// (O(slots) scans) and track dirty slots densely (reductions, then one linear
+// diff pass); list rounds sync through (slot, value) lists and track dirty
+// slots with returned atomics (O(frontier + its edges)).  The fixed rule
+// takes the bitvector form when the frontier entering the round holds at
+// least 1/dense_div of the slots or of the edges.  GRD_FMT_BITVEC /
+// GRD_FMT_LIST force it.  k_policy applies the same rule on the device.
 bool use_dense(const grd_ctx* ctx) {
   if (ctx->params.frontier_format == GRD_FMT_BITVEC) return true;
   if (ctx->params.frontier_format == GRD_FMT_LIST) return false;
-  return ctx->last_frontier * ctx->params.dense_div >= ctx->g.S;
+  const uint64_t d = ctx->params.dense_div;
+  return ctx->last_frontier * d >= ctx->g.S || ctx->last_fedges * d >= ctx->L.E;
 }
 
 // Direction: the pull map reads every in-edge once; the push map reads only
-// the frontier's out-edges (load-balanced, fire-and-forget reductions in
-// dense rounds).  Measured on RMAT, push wins even for full frontiers, so the
-// fixed rule pulls only when at least half the vertices are active and the
-// in-edge view already exists (it is built when pull is requested).
+// the frontier's out-edges (load-balanced).  Measured on RMAT, push wins even
+// for full frontiers, so the fixed rule pulls only when at least 1/pull_div of
+// the vertices are active and the in-edge view exists (it is built when pull
+// is requested).
 bool use_pull(const grd_ctx* ctx) {
   if (!ctx->in_edges_alloc) return false;
   if (ctx->params.direction == GRD_DIR_PULL) return true;
@@ -217,6 +244,11 @@ bool use_pull(const grd_ctx* ctx) {
 }
 
 }  // namespace
+
+int grd_choose_round_mode(const grd_ctx* ctx) {
+  const bool pull = use_pull(ctx), list = !use_dense(ctx);
+  return pull ? (list ? RM_PULL_LIST : RM_PULL_BITVEC) : (list ? RM_PUSH_LIST : RM_PUSH_BITVEC);
+}
 
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
   const uint32_t T = ctx->g.num_tiles;
@@ -233,18 +265,27 @@ int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
   return GRD_OK;
 }
 
-// Kernels one edge-map round launches in each mode (push sparse / push
-// dense / pull).
+// Kernels of the edge-map of one round in each mode.
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
-  if (mode == MODE_PULL) return ctx->pull.num_in_hubs ? 2 : 1;
-  return 4 + (ctx->g.num_hubs ? 1 : 0) + (mode == MODE_PUSH_DENSE ? 1 : 0);
+  if (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST) return ctx->pull.num_in_hubs ? 2 : 1;
+  return 4 + (ctx->g.num_hubs ? 1 : 0) + (mode == RM_PUSH_BITVEC ? 1 : 0);
 }
 
+// Kernels of a whole round in each mode (edge-map + syncs + update).
+uint32_t grd_round_launches(const grd_ctx* ctx, int mode) {
+  const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
+  const uint32_t groups = ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1;
+  const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (3 /*fwd*/ + 2 + groups /*bwd*/ + 1 /*update*/);
+  return sync + grd_edge_map_launches(ctx, mode);
+}
+
+// Stage API edge-map (bitvector sync around it): push with dense dirty
+// tracking, or pull.
 int grd_enqueue_edge_map(grd_ctx* ctx) {
-  const int mode = use_pull(ctx) ? MODE_PULL : (use_dense(ctx) ? MODE_PUSH_DENSE : MODE_PUSH_SPARSE);
+  const int mode = use_pull(ctx) ? RM_PULL_BITVEC : RM_PUSH_BITVEC;
   TRY(grd_enqueue_edge_map_mode(ctx, mode));
   ctx->last_mode = mode;
-  if (mode == MODE_PULL) {
+  if (mode == RM_PULL_BITVEC) {
     ctx->stats.pull_rounds++;
     ctx->pull.edges += ctx->L.E;
   } else {
@@ -257,11 +298,20 @@ int grd_enqueue_edge_map(grd_ctx* ctx) {
 int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
-    if (mode == MODE_PULL) {
-      k_pull<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    const uint32_t pull_hub_grid = std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8));
+    if (mode == RM_PULL_BITVEC) {
+      k_pull<A, false><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       if (ctx->pull.num_in_hubs)
-        k_pull_hub<A><<<std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8)), 256, 0, ctx->stream>>>(
-            ctx->g, ctx->st, ctx->pull.in_hubs, ctx->pull.num_in_hubs);
+        k_pull_hub<A, false><<<pull_hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_hubs,
+                                                                     ctx->pull.num_in_hubs);
+      CK_LAUNCH();
+      return GRD_OK;
+    }
+    if (mode == RM_PULL_LIST) {
+      k_pull<A, true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ctx->pull.num_in_hubs)
+        k_pull_hub<A, true><<<pull_hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_hubs,
+                                                                    ctx->pull.num_in_hubs);
       CK_LAUNCH();
       return GRD_OK;
     }
@@ -270,8 +320,7 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
     k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(ctx->st, B);
     k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
-    const bool dense = mode == MODE_PUSH_DENSE;
-    if (dense) {
+    if (mode == RM_PUSH_BITVEC) {
       k_push_lbs<A, true><<<resident_grid(ctx, k_push_lbs<A, true>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       k_diff_dirty<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
@@ -292,7 +341,7 @@ int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate) {
     constexpr int A = decltype(a)::value;
     constexpr bool kPR = (A == A_PR_DELTA);
     if (do_pack) {
-      k_tile_count<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.tile_cnt);
+      k_tile_count<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.tile_cnt, ctx->st.FB);
       k_scan_tiles<<<1, 1024, 0, ctx->stream>>>(ctx->g, ctx->st, 0);
       if (!fused) k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, nullptr, 0u, ctx->g, ctx->st, OpBwdPack<A>{});
       ctx->stats.kernel_launches += fused ? 2 : 3;
@@ -317,8 +366,9 @@ int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate) {
   });
 }
 
+// The per-round counters and list lengths it rebuilds are cleared by the
+// forward sync that starts the round.
 int grd_enqueue_update(grd_ctx* ctx) {
-  CK(cudaMemsetAsync(ctx->st.counters + C_FRONTIER, 0, sizeof(unsigned long long), ctx->stream));
   const uint32_t blocks = std::max<uint32_t>(1, std::min<uint32_t>((ctx->g.V + 255) / 256, grid_for(ctx, 8)));
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
@@ -327,6 +377,48 @@ int grd_enqueue_update(grd_ctx* ctx) {
     ctx->stats.kernel_launches += 1;
     return GRD_OK;
   });
+}
+
+// List-round stages (three kernels per round besides the edge-map).
+int grd_enqueue_fwd_list(grd_ctx* ctx) {
+  k_fwd_list<<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+  CK_LAUNCH();
+  return GRD_OK;
+}
+
+int grd_enqueue_bwd_update_list(grd_ctx* ctx) {
+  return dispatch(ctx->algo, [&](auto a) -> int {
+    constexpr int A = decltype(a)::value;
+    k_bwd_list<A><<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    k_update_list<A><<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
+                                                                ctx->params.damping);
+    CK_LAUNCH();
+    return GRD_OK;
+  });
+}
+
+// One whole round in a given mode (host loop and loop-graph branches).
+int grd_enqueue_round(grd_ctx* ctx, int mode) {
+  const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
+  const uint64_t launches = ctx->stats.kernel_launches;
+  if (list) {
+    TRY(grd_enqueue_fwd_list(ctx));
+  } else {
+    TRY(grd_enqueue_fwd(ctx, true));
+  }
+  grd_prof_mark(ctx, 1);
+  TRY(grd_enqueue_edge_map_mode(ctx, mode));
+  grd_prof_mark(ctx, 2);
+  if (list) {
+    TRY(grd_enqueue_bwd_update_list(ctx));
+    grd_prof_mark(ctx, 3);
+  } else {
+    TRY(grd_enqueue_bwd(ctx, true, true, true));
+    grd_prof_mark(ctx, 3);
+    TRY(grd_enqueue_update(ctx));
+  }
+  ctx->stats.kernel_launches = launches + grd_round_launches(ctx, mode);
+  return GRD_OK;
 }
 
 // Once per round, after the update: copies the device counters to the host
@@ -339,9 +431,10 @@ int grd_read_counters(grd_ctx* ctx) {
   ctx->stats.bytes_synced = ctx->h_counters[C_BYTES];
   ctx->stats.reference_bytes_moved = ctx->h_counters[C_REFBYTES];
   ctx->stats.actives_total += ctx->h_counters[C_ACTIVE];
-  if (ctx->last_mode >= 0 && ctx->last_mode != MODE_PULL) ctx->stats.push_actives += ctx->h_counters[C_ACTIVE];
+  if (ctx->last_mode >= 0 && !rm_is_pull(ctx->last_mode)) ctx->stats.push_actives += ctx->h_counters[C_ACTIVE];
   ctx->last_mode = -1;
   ctx->last_frontier = ctx->h_counters[C_FRONTIER];
+  ctx->last_fedges = ctx->h_counters[C_FEDGES];
   if (ctx->h_counters[C_ERR]) {
     ctx->err = "device-side error code " + std::to_string(ctx->h_counters[C_ERR]);
     return ctx->h_counters[C_ERR] == 1 ? GRD_E_TIMEOUT : GRD_E_CUDA;
@@ -515,6 +608,7 @@ int grd_init(grd_ctx* ctx) {
   }
   CK(cudaSetDevice(ctx->device));
   CK(cudaMemsetAsync(ctx->st.counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, ctx->stream));
+  CK(cudaMemsetAsync(ctx->st.lc, 0, sizeof(uint32_t) * NUM_LIST_COUNTERS, ctx->stream));
   const uint64_t n = std::max<uint64_t>(ctx->g.S, ctx->g.V);
   const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)grid_for(ctx, 16));
   int rc = grd_enqueue_init(ctx, blocks);
@@ -529,12 +623,17 @@ int grd_init(grd_ctx* ctx) {
   return GRD_OK;
 }
 
-static __global__ void k_seed_sources(DevState st, const uint32_t* src, uint32_t n) {
+static __global__ void k_seed_sources(DevGraph g, DevState st, const uint32_t* src, uint32_t n) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t s = src[i];
     st.prop[s] = 0;
     st.upd[s] = 0;
     atomicOr(&st.F[s >> 5], 1u << (s & 31));
+    list_append(st.FL, st.lc + L_FL, s);  // sources are distinct
+    const unsigned long long d = g.outdeg[s];
+    atomicAdd(&st.counters[C_FEDGES], d);
+    atomicAdd(&st.counters[C_UNVISITED], 0ull - d);
+    atomicMax(&st.counters[C_FMAXDEG], d);
   }
 }
 
@@ -566,13 +665,17 @@ int grd_init_sources(grd_ctx* ctx, const uint32_t* sources, size_t n) {
   }
   CK(cudaMemcpyAsync(ctx->agg_buf, src.data(), sizeof(uint32_t) * m, cudaMemcpyHostToDevice, ctx->stream));
   k_seed_sources<<<(uint32_t)std::min<size_t>((m + 255) / 256, grid_for(ctx, 4)), 256, 0, ctx->stream>>>(
-      ctx->st, ctx->agg_buf, (uint32_t)m);
+      ctx->g, ctx->st, ctx->agg_buf, (uint32_t)m);
   CK_LAUNCH();
   ctx->h_seed[0] = m;
   CK(cudaMemcpyAsync(ctx->st.counters + C_FRONTIER, ctx->h_seed, sizeof(unsigned long long), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->last_frontier = m;
+  CK(cudaMemcpyAsync(ctx->h_counters, ctx->st.counters, sizeof(unsigned long long) * NUM_COUNTERS,
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->last_fedges = ctx->h_counters[C_FEDGES];
   ctx->stats.kernel_launches += 1;
   return GRD_OK;
 }
@@ -637,16 +740,19 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
     uint64_t f = 1;
     while (ctx->stats.rounds < ctx->params.max_rounds) {
       const uint64_t f_in = ctx->last_frontier, e_in = ctx->stats.edges_scanned;
+      const uint64_t fe_in = ctx->h_counters[C_FEDGES], fm_in = ctx->h_counters[C_FMAXDEG],
+                     un_in = ctx->h_counters[C_UNVISITED];
+      const int mode = grd_choose_round_mode(ctx);
       grd_prof_mark(ctx, 0);
-      TRY(grd_enqueue_fwd(ctx, true));
-      grd_prof_mark(ctx, 1);
-      TRY(grd_enqueue_edge_map(ctx));
-      const int mode = ctx->last_mode;
-      grd_prof_mark(ctx, 2);
-      TRY(grd_enqueue_bwd(ctx, true, true, true));
-      grd_prof_mark(ctx, 3);
-      TRY(grd_enqueue_update(ctx));
+      TRY(grd_enqueue_round(ctx, mode));
       grd_prof_mark(ctx, 4);
+      ctx->last_mode = mode;
+      if (rm_is_pull(mode)) {
+        ctx->stats.pull_rounds++;
+        ctx->pull.edges += ctx->L.E;
+      } else {
+        ctx->stats.push_rounds++;
+      }
       TRY(grd_read_counters(ctx));
       f = ctx->h_counters[C_FRONTIER];
       if (ctx->profiling) {
@@ -657,6 +763,9 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
         rec.actives = ctx->h_counters[C_ACTIVE];
         rec.edges = ctx->stats.edges_scanned - e_in;
         rec.frontier_out = f;
+        rec.frontier_edges_in = fe_in;
+        rec.max_degree_in = fm_in;
+        rec.unvisited_in = un_in;
         grd_prof_collect(ctx, rec.ms);
         ctx->round_log.push_back(rec);
       }

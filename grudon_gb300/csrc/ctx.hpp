@@ -37,6 +37,7 @@ struct grd_ctx {
   bool in_edges_alloc = false;
   PullState pull;
   uint64_t last_frontier = 0;  // |frontier| entering the next round
+  uint64_t last_fedges = 0;    // its out-edges
   std::vector<grd_round_rec> round_log;  // profiled host-loop rounds
   int last_mode = -1;          // edge-map mode of the round in flight (host loop)
   cudaGraph_t run_graph = nullptr;     // device-driven round loop (graph_run.cu)
@@ -86,9 +87,23 @@ int grd_ensure_in_edges(grd_ctx* ctx);
 int grd_read_counters(grd_ctx* ctx);
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused);
 int grd_enqueue_edge_map(grd_ctx* ctx);
-enum EdgeMapMode { MODE_PUSH_SPARSE = 0, MODE_PUSH_DENSE = 1, MODE_PULL = 2 };
+// Round modes: direction x sync format.  Values are the SWITCH branch indices
+// of the loop graph and the `mode` field of grd_round_rec.
+enum RoundMode {
+  RM_PUSH_BITVEC = GRD_ROUND_PUSH_BITVEC,
+  RM_PUSH_LIST = GRD_ROUND_PUSH_LIST,
+  RM_PULL_BITVEC = GRD_ROUND_PULL_BITVEC,
+  RM_PULL_LIST = GRD_ROUND_PULL_LIST,
+  NUM_ROUND_MODES = 4
+};
+__host__ __device__ inline bool rm_is_pull(int m) { return m == RM_PULL_BITVEC || m == RM_PULL_LIST; }
+int grd_choose_round_mode(const grd_ctx* ctx);
 int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode);
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode);
+uint32_t grd_round_launches(const grd_ctx* ctx, int mode);
+int grd_enqueue_fwd_list(grd_ctx* ctx);
+int grd_enqueue_bwd_update_list(grd_ctx* ctx);
+int grd_enqueue_round(grd_ctx* ctx, int mode);
 // Device-driven loop (graph_run.cu).
 int grd_graph_run(grd_ctx* ctx, bool* used);
 void grd_graph_release(grd_ctx* ctx);

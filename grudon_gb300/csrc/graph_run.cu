@@ -2,14 +2,16 @@
 //
 // Top level: a conditional WHILE node whose body is one round of
 // GraphAlgorithm::run (src/GraphAlgorithm.cpp:177-690):
-//   forward sync -> k_policy -> SWITCH {push sparse, push dense, pull}
-//   -> backward sync + aggregate -> update -> k_round_end
-// k_policy applies the direction / frontier-format rule on the device (the
-// frontier size of the previous update is already there) and selects the
-// switch branch; k_round_end counts the round and keeps the loop going while
-// the frontier is non-empty and the round cap is not reached, so the loop is
-// always bounded.  One graph launch runs the whole algorithm with no host
-// round trip; the host reads the counters once at the end.
+//   k_policy -> SWITCH {push+bitvector, push+list, pull+bitvector, pull+list}
+//   -> k_round_end
+// where every branch is a whole round (forward sync, edge-map, backward sync
+// + aggregate, update) in that mode.  k_policy applies the direction /
+// frontier-format rule on the device (the frontier size of the previous
+// update is already there) and selects the branch; k_round_end counts the
+// round and keeps the loop going while the frontier is non-empty and the
+// round cap is not reached, so the loop is always bounded.  One graph launch
+// runs the whole algorithm with no host round trip; the host reads the
+// counters once at the end.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,7 +27,7 @@ namespace {
 struct PolicyArgs {
   int direction, format, has_in;
   uint32_t dense_div, pull_div;
-  uint32_t launches[3];  // kernels of one round per edge-map mode
+  uint32_t launches[NUM_ROUND_MODES];  // kernels of one round per mode
   unsigned long long edges;
 };
 
@@ -34,8 +36,10 @@ __global__ void k_policy(DevGraph g, DevState st, cudaGraphConditionalHandle sw,
   const unsigned long long f = st.counters[C_FRONTIER];
   const bool pull =
       a.has_in && (a.direction == GRD_DIR_PULL || (a.direction == GRD_DIR_AUTO && f * a.pull_div >= g.V));
-  const bool dense = a.format == GRD_FMT_BITVEC || (a.format == GRD_FMT_AUTO && f * a.dense_div >= g.S);
-  const int mode = pull ? MODE_PULL : (dense ? MODE_PUSH_DENSE : MODE_PUSH_SPARSE);
+  const unsigned long long fe = st.counters[C_FEDGES];
+  const bool list = a.format == GRD_FMT_LIST ||
+                    (a.format == GRD_FMT_AUTO && f * a.dense_div < g.S && fe * a.dense_div < a.edges);
+  const int mode = pull ? (list ? RM_PULL_LIST : RM_PULL_BITVEC) : (list ? RM_PUSH_LIST : RM_PUSH_BITVEC);
   st.counters[C_MODE] = mode;
   if (pull) {
     st.counters[C_PULL_ROUNDS] += 1;
@@ -52,7 +56,7 @@ __global__ void k_round_end(DevState st, cudaGraphConditionalHandle wh, uint32_t
   const unsigned long long r = st.counters[C_ROUNDS] + 1;
   st.counters[C_ROUNDS] = r;
   st.counters[C_ACTIVE_TOTAL] += st.counters[C_ACTIVE];
-  if (st.counters[C_MODE] != MODE_PULL) st.counters[C_PUSH_ACTIVES] += st.counters[C_ACTIVE];
+  if (!rm_is_pull((int)st.counters[C_MODE])) st.counters[C_PUSH_ACTIVES] += st.counters[C_ACTIVE];
   cudaGraphSetConditional(wh, (st.counters[C_FRONTIER] > 0 && r < max_rounds) ? 1u : 0u);
 }
 
@@ -120,28 +124,21 @@ int build(grd_ctx* ctx) {
   pa.dense_div = ctx->params.dense_div;
   pa.pull_div = ctx->params.pull_div;
   pa.edges = ctx->L.E;
-  const uint32_t base = 3 /*fwd*/ + 1 /*policy*/ + 2 /*bwd pack*/ + (ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1) +
-                        1 /*update*/ + 1 /*round end*/;
-  for (int m = 0; m < 3; ++m) pa.launches[m] = base + grd_edge_map_launches(ctx, m);
+  for (int m = 0; m < NUM_ROUND_MODES; ++m) pa.launches[m] = 2 /*policy, round end*/ + grd_round_launches(ctx, m);
 
   int rc = capture_into(ctx, loop_body);
   if (rc != GRD_OK) return rc;
-  cudaGraph_t branches[3] = {};
-  rc = grd_enqueue_fwd(ctx, true);
-  if (rc == GRD_OK) {
-    k_policy<<<1, 32, 0, ctx->stream>>>(ctx->g, ctx->st, sw, pa);
-    rc = add_conditional(ctx, ctx->stream, sw, cudaGraphCondTypeSwitch, 3, branches);
-  }
-  if (rc == GRD_OK) rc = grd_enqueue_bwd(ctx, true, true, true);
-  if (rc == GRD_OK) rc = grd_enqueue_update(ctx);
+  cudaGraph_t branches[NUM_ROUND_MODES] = {};
+  k_policy<<<1, 32, 0, ctx->stream>>>(ctx->g, ctx->st, sw, pa);
+  rc = add_conditional(ctx, ctx->stream, sw, cudaGraphCondTypeSwitch, NUM_ROUND_MODES, branches);
   if (rc == GRD_OK) k_round_end<<<1, 32, 0, ctx->stream>>>(ctx->st, wh, ctx->params.max_rounds);
   const int rc_end = end_capture(ctx, loop_body);
   if (rc != GRD_OK) return rc;
   if (rc_end != GRD_OK) return rc_end;
-  for (int m = 0; m < 3; ++m) {
-    if (m == MODE_PULL && !ctx->in_edges_alloc) continue;  // never selected
+  for (int m = 0; m < NUM_ROUND_MODES; ++m) {
+    if (rm_is_pull(m) && !ctx->in_edges_alloc) continue;  // never selected: empty branch
     TRY(capture_into(ctx, branches[m]));
-    rc = grd_enqueue_edge_map_mode(ctx, m);
+    rc = grd_enqueue_round(ctx, m);
     const int e = end_capture(ctx, branches[m]);
     if (rc != GRD_OK) return rc;
     if (e != GRD_OK) return e;

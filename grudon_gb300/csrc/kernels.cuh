@@ -13,10 +13,13 @@
 // partition's wire bitvector is u32 words 2w,2w+1, so the layout is the
 // reference's DynamicBitSet word layout.
 #pragma once
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace grd {
+
+enum ListCounter : int { L_DL = 0, L_UL = 1, L_FL = 2, NUM_LIST_COUNTERS = 4 };
 
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 constexpr uint32_t K_TILE_SLOTS = 8192;
@@ -42,7 +45,12 @@ enum Counter : int {
   C_MODE = 13,          // edge-map mode chosen for the current round
   C_LAUNCHES = 14,      // device-driven loop: kernels launched
   C_PUSH_ACTIVES = 15,  // device-driven loop: C_ACTIVE summed over push rounds
-  NUM_COUNTERS = 16
+  // Shape of the frontier left by the last update (round-policy inputs).
+  C_FEDGES = 16,     // out-edges of the frontier (sum of global out-degrees)
+  C_FMAXDEG = 17,    // largest out-degree in the frontier
+  C_UNVISITED = 18,  // SSSP: out-edges of vertices not reached yet
+  C_DONE = 19,       // finished-block count of k_update_list (last-block reset)
+  NUM_COUNTERS = 20
 };
 
 struct HubChunkD {
@@ -52,6 +60,10 @@ struct HubChunkD {
 struct DevGraph {
   uint32_t V, M;
   uint64_t S;
+  uint64_t E;
+  // Wire size of the bitvectors of one sync pass (one per memory partition):
+  // true bytes, and the reference's count (MPI_UINT64_T elements x 8).
+  unsigned long long bv_bytes, bv_refbytes;
   uint32_t num_tiles, num_hubs;
   const uint32_t* slot_gid;
   const uint32_t* row_off;
@@ -92,6 +104,13 @@ struct DevState {
   uint32_t* chunk_start;  // [E/256+2] first active of each 256-edge chunk
   uint32_t* blk_sum;      // [LBS blocks]
   uint32_t* blk_off;      // [LBS blocks]
+  // Sparse-list sync (list-format rounds): the frontier as a gid list, the
+  // memory-side dirty slots and the compute-side updated gids as lists.
+  uint32_t* FL;           // [V] frontier gids (valid after every update)
+  uint32_t* DL;           // [S] dirty slots of the current round
+  uint32_t* UL;           // [V] gids whose vertex_updates changed this round
+  uint32_t* own_slot;     // [V] gid -> its owned global slot
+  uint32_t* lc;           // [4] list lengths: L_DL, L_UL, L_FL
   unsigned long long* counters;
 };
 
@@ -143,17 +162,108 @@ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
   return s < a ? 0xFFFFFFFFu : s;
 }
 
+// Appends value to list with one counter update per group of converged
+// lanes (warp-aggregated atomic).
+__device__ __forceinline__ void list_append(uint32_t* list, uint32_t* counter, uint32_t value) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group grp = cg::coalesced_threads();
+  uint32_t base = 0;
+  if (grp.thread_rank() == 0) base = atomicAdd(counter, grp.size());
+  base = grp.shfl(base, 0);
+  list[base + grp.thread_rank()] = value;
+}
+
+// Sets bit i of bm; the lane that sets it first appends i to list.
+__device__ __forceinline__ void mark_listed(uint32_t* bm, uint32_t i, uint32_t* list, uint32_t* counter) {
+  const uint32_t bit = 1u << (i & 31);
+  uint32_t* w = bm + (i >> 5);
+  if (__ldcg(w) & bit) return;
+  if (atomicOr(w, bit) & bit) return;
+  list_append(list, counter, i);
+}
+
+// Sets bit i of bm; true for the thread that set it.
+__device__ __forceinline__ bool claim_bit(uint32_t* bm, uint32_t i) {
+  const uint32_t bit = 1u << (i & 31);
+  uint32_t* w = bm + (i >> 5);
+  if (__ldcg(w) & bit) return false;
+  return !(atomicOr(w, bit) & bit);
+}
+
+__device__ __forceinline__ uint32_t block_max(uint32_t v) {
+  __shared__ uint32_t s_mx[32];
+  const uint32_t w = threadIdx.x >> 5, lane = lane_id();
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(FULL, v, o));
+  __syncthreads();
+  if (lane == 0) s_mx[w] = v;
+  __syncthreads();
+  const uint32_t nw = (blockDim.x + 31) >> 5;
+  uint32_t r = lane < nw ? s_mx[lane] : 0;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) r = max(r, __shfl_xor_sync(FULL, r, o));
+  return r;
+}
+
+// Block-aggregated append: every thread of the block calls it (block-uniform
+// control flow); the threads whose flag is set append their value.  One
+// counter update per block and call.
+__device__ __forceinline__ void block_append(uint32_t* list, uint32_t* counter, bool flag, uint32_t value) {
+  __shared__ uint32_t s_wc[32];
+  __shared__ uint32_t s_base;
+  const uint32_t w = threadIdx.x >> 5, lane = lane_id();
+  const uint32_t m = __ballot_sync(FULL, flag);
+  if (lane == 0) s_wc[w] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t nw = (blockDim.x + 31) >> 5;
+    uint32_t t = 0;
+    for (uint32_t k = 0; k < nw; ++k) {
+      const uint32_t c = s_wc[k];
+      s_wc[k] = t;
+      t += c;
+    }
+    s_base = t ? atomicAdd(counter, t) : 0u;
+  }
+  __syncthreads();
+  if (flag) list[s_base + s_wc[w] + __popc(m & ((1u << lane) - 1u))] = value;
+  __syncthreads();  // s_wc / s_base are reused by the next call
+}
+
+// Warp-aggregated append of up to N flagged values per lane; every lane of
+// the warp calls it.  One counter update per warp and call.
+template <int N>
+__device__ __forceinline__ void warp_append_n(uint32_t* list, uint32_t* counter, const bool (&flag)[N],
+                                              const uint32_t (&value)[N]) {
+  uint32_t cnt = 0;
+#pragma unroll
+  for (int k = 0; k < N; ++k) cnt += flag[k] ? 1u : 0u;
+  const uint32_t incl = warp_incl_scan(cnt);
+  const uint32_t tot = __shfl_sync(FULL, incl, 31);
+  if (tot == 0) return;
+  uint32_t base = 0;
+  if (lane_id() == 31) base = atomicAdd(counter, tot);
+  uint32_t pos = __shfl_sync(FULL, base, 31) + incl - cnt;
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+    if (flag[k]) list[pos++] = value[k];
+}
+
 // ------------------------------------------------------------------- init --
-// Reference init(): pr.cpp:20-61, cc.cpp:18-40, sssp.cpp:18-47.
+// Reference init(): pr.cpp:20-61, cc.cpp:18-40, sssp.cpp:18-47.  Also lists
+// the frontier and records its shape (count, out-edges, largest degree, and
+// for SSSP the out-edges not reached yet).  Block-uniform loop: every thread
+// of a block runs the same iterations (block-aggregated list appends).
 template <int A>
 __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t source, double damping) {
   const uint64_t n = g.S > g.V ? g.S : g.V;
-  uint32_t fcount = 0;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ((n + 31) & ~31ull);
-       i += (uint64_t)gridDim.x * blockDim.x) {
+  uint32_t fcount = 0, fedges = 0, fmax = 0, unvis = 0;
+  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x; b < n; b += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = b + threadIdx.x;
     uint32_t fbit = 0;
     if (i < g.V) {
       const uint32_t v = (uint32_t)i;
+      const uint32_t deg = g.outdeg[v];
       if (A == A_CC) {
         st.prop[v] = v;
         st.upd[v] = 0xFFFFFFFFu;
@@ -163,8 +273,8 @@ __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t 
         st.prop[v] = x;
         st.upd[v] = x;
         fbit = (v == source);
+        if (!fbit) unvis += deg;
       } else {  // PageRank (delta and pull share the initial state)
-        const uint32_t deg = g.outdeg[v];
         if (deg != 0) {
           st.prop[v] = __float_as_uint((float)(damping * (1.0 - damping) / (double)deg));
           st.ranks[v] = (float)(1.0 - damping);
@@ -175,9 +285,14 @@ __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t 
         }
         st.upd[v] = 0;
       }
+      if (fbit) {
+        fedges += deg;
+        fmax = max(fmax, deg);
+      }
     }
     const uint32_t m = __ballot_sync(FULL, fbit);
-    if (lane_id() == 0 && i < g.V) {
+    block_append(st.FL, st.lc + L_FL, fbit != 0, (uint32_t)i);
+    if (lane_id() == 0 && i < g.V) {  // i is the first gid of its word
       st.F[i >> 5] = m;
       st.UD[i >> 5] = 0;
       fcount += __popc(m);
@@ -193,17 +308,39 @@ __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t 
       }
     }
   }
-  fcount = block_sum(fcount);  // one counter update per block
-  if (threadIdx.x == 0 && fcount) atomicAdd(&st.counters[C_FRONTIER], (unsigned long long)fcount);
+  // one counter update per block
+  fcount = block_sum(fcount);
+  fedges = block_sum(fedges);
+  unvis = block_sum(unvis);
+  fmax = block_max(fmax);
+  if (threadIdx.x == 0) {
+    if (fcount) atomicAdd(&st.counters[C_FRONTIER], (unsigned long long)fcount);
+    if (fedges) atomicAdd(&st.counters[C_FEDGES], (unsigned long long)fedges);
+    if (unvis) atomicAdd(&st.counters[C_UNVISITED], (unsigned long long)unvis);
+    if (fmax) atomicMax(&st.counters[C_FMAXDEG], (unsigned long long)fmax);
+  }
 }
 
 // ---------------------------------------------------- forward sync: bits --
 // Compute side of src/GraphAlgorithm.cpp:199-246: every frontier vertex sets
 // the bit of its owned slot in its mirror partition's bitvector.  One warp
 // builds one 32-bit word by ballot over 32 consecutive slots; the per-tile
-// popcount feeds the compaction scan.
+// popcount feeds the compaction scan.  A round starts here (bitvector
+// rounds), so block 0 also clears the per-round counters and the lists the
+// update of this round rebuilds (nothing reads them before the update).
+__device__ __forceinline__ void reset_round_counters(const DevState& st) {
+  st.counters[C_FRONTIER] = 0;
+  st.counters[C_FEDGES] = 0;
+  st.counters[C_FMAXDEG] = 0;
+}
+
 static __global__ void __launch_bounds__(256) k_fwd_bits(DevGraph g, DevState st) {
   const uint32_t t = blockIdx.x;
+  if (t == 0 && threadIdx.x == 0) {
+    reset_round_counters(st);
+    st.lc[L_FL] = 0;
+    st.lc[L_UL] = 0;  // the bitvector update consumes every dirty bit
+  }
   const uint32_t p = g.tile_part[t];
   const uint32_t base = g.part_base[p], nown = g.part_owned[p];
   const uint32_t t0 = t * K_TILE_SLOTS;
@@ -233,12 +370,18 @@ static __global__ void __launch_bounds__(256) k_fwd_bits(DevGraph g, DevState st
   if (threadIdx.x == 0) st.tile_cnt[t] = cnt;
 }
 
-// Per-tile set-bit count of a bitvector (backward sync).
-static __global__ void __launch_bounds__(256) k_tile_count(const uint32_t* __restrict__ bits, uint32_t* tile_cnt) {
+// Per-tile set-bit count of a bitvector (backward sync).  `zero`, when
+// given, is another bitvector whose words of this tile are cleared (the
+// forward bitvector, no longer read once the edge-map has run).
+static __global__ void __launch_bounds__(256) k_tile_count(const uint32_t* __restrict__ bits, uint32_t* tile_cnt,
+                                                           uint32_t* zero = nullptr) {
   const uint32_t t = blockIdx.x;
   const uint32_t* w = bits + (size_t)t * K_TILE_WORDS;
   uint32_t c = 0;
-  for (uint32_t i = threadIdx.x; i < K_TILE_WORDS; i += blockDim.x) c += __popc(w[i]);
+  for (uint32_t i = threadIdx.x; i < K_TILE_WORDS; i += blockDim.x) {
+    c += __popc(w[i]);
+    if (zero) zero[(size_t)t * K_TILE_WORDS + i] = 0;
+  }
   c = block_sum(c);
   if (threadIdx.x == 0) tile_cnt[t] = c;
 }
@@ -514,34 +657,51 @@ __global__ void __launch_bounds__(256) k_aggregate_values(DevState st, const uin
     const uint32_t gid = gids[i], v = vals[i];
     if (A == A_PR_DELTA || A == A_PR_PULL) {
       atomicAdd(reinterpret_cast<float*>(st.upd) + gid, __uint_as_float(v));
-      red_or(st.UD + (gid >> 5), 1u << (gid & 31));
+      mark_listed(st.UD, gid, st.UL, st.lc + L_UL);
     } else {
       const uint32_t old = atomicMin(&st.upd[gid], v);
-      if (v < old) red_or(st.UD + (gid >> 5), 1u << (gid & 31));
+      if (v < old) mark_listed(st.UD, gid, st.UL, st.lc + L_UL);
     }
   }
 }
 
 // -------------------------------------------------------------- edge map --
-// One relaxation (PropertyList::minUpdate / addUpdate,
+// Relaxation (PropertyList::minUpdate / addUpdate,
 // include/DistributedGraph.hpp:103-130): the dirty bit is set when a min
 // lowers the value, and always for an add.  `cur` is a prior read of
 // mupd[d] (a stale read is only ever larger, values never grow in a round).
-// Dense mode (kDense) issues reductions only and leaves the dirty set to
-// k_diff_dirty; sparse mode marks dirty bits as it goes.
-template <int A, bool kDense>
-__device__ __forceinline__ void relax_apply(const DevState& st, uint32_t d, uint32_t cand, uint32_t cur) {
-  if (A == A_PR_DELTA) {
+//
+// Dense form (bitvector rounds): reductions only; the dirty set is rebuilt
+// afterwards by k_diff_dirty.
+template <int A>
+__device__ __forceinline__ void relax_dense(const DevState& st, uint32_t d, uint32_t cand, uint32_t cur) {
+  if (A == A_PR_DELTA)
     red_add_f32(reinterpret_cast<float*>(st.mupd) + d, __uint_as_float(cand));
-    if (!kDense) red_or(st.MD + (d >> 5), 1u << (d & 31));
-  } else if (cand < cur) {
-    if (kDense) {
-      red_min(st.mupd + d, cand);
-    } else {
-      const uint32_t old = atomicMin(&st.mupd[d], cand);
-      if (cand < old) red_or(st.MD + (d >> 5), 1u << (d & 31));
+  else if (cand < cur)
+    red_min(st.mupd + d, cand);
+}
+
+// Sparse form (list rounds), N edges per lane (d = 0xFFFFFFFF: none): all N
+// returning atomics are issued before any result is used, then every lowered
+// slot (PageRank: every touched slot) claims its dirty bit; nd[k] is set for
+// the one thread that claimed it, so each dirty slot is listed once.
+template <int A, int N>
+__device__ __forceinline__ void relax_sparse(const DevState& st, const uint32_t (&d)[N], const uint32_t (&cand)[N],
+                                             const uint32_t (&cur)[N], bool (&nd)[N]) {
+  bool low[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    low[k] = false;
+    if (d[k] == 0xFFFFFFFFu) continue;
+    if (A == A_PR_DELTA) {
+      red_add_f32(reinterpret_cast<float*>(st.mupd) + d[k], __uint_as_float(cand[k]));
+      low[k] = true;
+    } else if (cand[k] < cur[k]) {
+      low[k] = cand[k] < atomicMin(&st.mupd[d[k]], cand[k]);
     }
   }
+#pragma unroll
+  for (int k = 0; k < N; ++k) nd[k] = low[k] && claim_bit(st.MD, d[k]);
 }
 
 template <int A>
@@ -733,9 +893,15 @@ __global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
       }
 #pragma unroll
       for (int k = 0; k < B; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek<A>(st, dst[k]) : 0u;
+      if (kDense) {
 #pragma unroll
-      for (int k = 0; k < B; ++k)
-        if (dst[k] != 0xFFFFFFFFu) relax_apply<A, kDense>(st, dst[k], cand[k], cur[k]);
+        for (int k = 0; k < B; ++k)
+          if (dst[k] != 0xFFFFFFFFu) relax_dense<A>(st, dst[k], cand[k], cur[k]);
+      } else {
+        bool nd[B];
+        relax_sparse<A, B>(st, dst, cand, cur, nd);
+        warp_append_n<B>(st.DL, st.lc + L_DL, nd, dst);
+      }
       __syncwarp();
       e = wend;
       i0 += LBS_WIN;
@@ -745,12 +911,22 @@ __global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
 
 // Hub rows: static work items of at most 4096 edges; a block runs an item
 // when its row is active this round (bit set in the forward bitvector) and
-// reads the aligned interior of the row with 128-bit loads.
-template <int A, bool kDense>
-__device__ __forceinline__ void hub_edge(const DevGraph& g, const DevState& st, uint32_t e, uint32_t sv) {
-  const uint32_t d = __ldg(&g.col[e]);
-  const uint32_t c = relax_cand<A>(sv, A == A_SSSP_W ? __ldg(&g.wgt[e]) : 0u);
-  relax_apply<A, kDense>(st, d, c, relax_peek<A>(st, d));
+// reads the aligned interior of the row with 128-bit loads.  All loops are
+// block-uniform (the sparse form appends warp-aggregated).
+template <int A, bool kDense, int N>
+__device__ __forceinline__ void hub_relax(const DevState& st, const uint32_t (&d)[N], const uint32_t (&c)[N]) {
+  uint32_t cur[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) cur[k] = d[k] != 0xFFFFFFFFu ? relax_peek<A>(st, d[k]) : 0u;
+  if (kDense) {
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      if (d[k] != 0xFFFFFFFFu) relax_dense<A>(st, d[k], c[k], cur[k]);
+  } else {
+    bool nd[N];
+    relax_sparse<A, N>(st, d, c, cur, nd);
+    warp_append_n<N>(st.DL, st.lc + L_DL, nd, d);
+  }
 }
 
 template <int A, bool kDense>
@@ -762,23 +938,34 @@ __global__ void __launch_bounds__(256) k_hub_push(DevGraph g, DevState st) {
     const uint32_t sv = source_value<A>(st.mprop[h.slot]);
     const uint32_t a0 = min(h.e1, (h.e0 + 3u) & ~3u);
     const uint32_t a1 = max(a0, h.e1 & ~3u);
-    for (uint32_t e = h.e0 + threadIdx.x; e < a0; e += blockDim.x) hub_edge<A, kDense>(g, st, e, sv);
+    {
+      // unaligned head [e0, a0) and tail [a1, e1): at most 3 edges each
+      const uint32_t t = threadIdx.x;
+      uint32_t e = 0xFFFFFFFFu;
+      if (t < a0 - h.e0) e = h.e0 + t;
+      else if (t >= 4 && t - 4 < h.e1 - a1) e = a1 + (t - 4);
+      uint32_t d[1] = {0xFFFFFFFFu}, cv[1] = {0u};
+      if (e != 0xFFFFFFFFu) {
+        d[0] = __ldg(&g.col[e]);
+        cv[0] = relax_cand<A>(sv, A == A_SSSP_W ? __ldg(&g.wgt[e]) : 0u);
+      }
+      hub_relax<A, kDense, 1>(st, d, cv);
+    }
     const uint4* c4 = reinterpret_cast<const uint4*>(g.col);
     const uint4* w4 = reinterpret_cast<const uint4*>(g.wgt);
-    for (uint32_t q = (a0 >> 2) + threadIdx.x; q < (a1 >> 2); q += blockDim.x) {
-      const uint4 d = __ldg(&c4[q]);
-      uint4 w = make_uint4(0, 0, 0, 0);
-      if (A == A_SSSP_W) w = __ldg(&w4[q]);
-      const uint32_t c0 = relax_cand<A>(sv, w.x), c1 = relax_cand<A>(sv, w.y);
-      const uint32_t c2 = relax_cand<A>(sv, w.z), c3 = relax_cand<A>(sv, w.w);
-      const uint32_t p0 = relax_peek<A>(st, d.x), p1 = relax_peek<A>(st, d.y);
-      const uint32_t p2 = relax_peek<A>(st, d.z), p3 = relax_peek<A>(st, d.w);
-      relax_apply<A, kDense>(st, d.x, c0, p0);
-      relax_apply<A, kDense>(st, d.y, c1, p1);
-      relax_apply<A, kDense>(st, d.z, c2, p2);
-      relax_apply<A, kDense>(st, d.w, c3, p3);
+    for (uint32_t q0 = a0 >> 2; q0 < (a1 >> 2); q0 += blockDim.x) {
+      const uint32_t q = q0 + threadIdx.x;
+      uint32_t d[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, cv[4] = {0u, 0u, 0u, 0u};
+      if (q < (a1 >> 2)) {
+        const uint4 dv = __ldg(&c4[q]);
+        uint4 w = make_uint4(0, 0, 0, 0);
+        if (A == A_SSSP_W) w = __ldg(&w4[q]);
+        d[0] = dv.x, d[1] = dv.y, d[2] = dv.z, d[3] = dv.w;
+        cv[0] = relax_cand<A>(sv, w.x), cv[1] = relax_cand<A>(sv, w.y);
+        cv[2] = relax_cand<A>(sv, w.z), cv[3] = relax_cand<A>(sv, w.w);
+      }
+      hub_relax<A, kDense, 4>(st, d, cv);
     }
-    for (uint32_t e = a1 + threadIdx.x; e < h.e1; e += blockDim.x) hub_edge<A, kDense>(g, st, e, sv);
     if (threadIdx.x == 0) scanned += h.e1 - h.e0;
   }
   if (threadIdx.x == 0 && scanned) atomicAdd(&st.counters[C_EDGES], scanned);
@@ -874,7 +1061,7 @@ __device__ __forceinline__ bool pull_commit(const DevState& st, uint32_t d, cons
 // shared memory, then every lane folds its own slot's part of the stage in
 // ascending source order.  In-lists longer than K_PULL_HUB go to k_pull_hub.
 // The warp writes its 32 dirty bits as one word.
-template <int A>
+template <int A, bool kList = false>
 __global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
   __shared__ uint32_t s_val[8][PULL_CH];
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
@@ -920,6 +1107,9 @@ __global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
     else if (A == A_PR_PULL) dirty = true;  // the hub kernel writes the value
     const uint32_t m = __ballot_sync(FULL, dirty);
     if (lane == 0) st.MD[d >> 5] = m;
+    // S is a multiple of 256, so every warp of a block runs the same
+    // iterations and the block-wide append is safe.
+    if (kList) block_append(st.DL, st.lc + L_DL, dirty, d);
   }
 }
 
@@ -927,7 +1117,7 @@ __global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
 // t+256, ... (coalesced), then thread 0 folds the 256 partials in thread
 // order (a fixed order, so sums are reproducible).  Runs after k_pull, whose
 // dirty word for the slot is already written: a dirty hub ORs its bit in.
-template <int A>
+template <int A, bool kList = false>
 __global__ void __launch_bounds__(256) k_pull_hub(DevGraph g, DevState st, const HubChunkD* hubs, uint32_t n) {
   __shared__ uint32_t s_part[256];
   for (uint32_t h = blockIdx.x; h < n; h += gridDim.x) {
@@ -958,53 +1148,198 @@ __global__ void __launch_bounds__(256) k_pull_hub(DevGraph g, DevState st, const
     if (threadIdx.x == 0) {
       PullAcc<A> tot;
       for (int i = 0; i < 256; ++i) tot.fold(s_part[i]);
-      if (pull_commit<A>(st, hc.slot, tot, true) && A != A_PR_PULL)
-        red_or(st.MD + (hc.slot >> 5), 1u << (hc.slot & 31));
+      if (pull_commit<A>(st, hc.slot, tot, true) && A != A_PR_PULL) {
+        if (kList)
+          mark_listed(st.MD, hc.slot, st.DL, st.lc + L_DL);
+        else
+          red_or(st.MD + (hc.slot >> 5), 1u << (hc.slot & 31));
+      }
     }
     __syncthreads();
   }
 }
 
+// -------------------------------------------------------- list-format sync --
+// List rounds carry the same data as bitvector rounds — the frontier's values
+// to their owning memory partitions, the dirty memory-side updates back — as
+// (slot, value) lists, so a round costs O(frontier + dirty) instead of
+// O(slots).  Values, dirty sets and round counts are identical to bitvector
+// rounds.  The byte statistics keep the bitvector formula: every sync pass
+// sends each partition's bitvector (a constant) plus 4 bytes per value.
+//
+// Between rounds: FB and MD are all-zero, F and FL hold the frontier, and UL
+// lists exactly the gids whose vertex_updates dirty bit is set.
+
+// Forward sync from the frontier list: the j-th entry's value goes to the
+// owned slot of its gid, which joins the active list (j-th entry) and the
+// forward bitvector (hub rows, PageRank pull).  A round starts here, so block
+// 0 also clears the per-round counters and the dirty-slot list.
+static __global__ void __launch_bounds__(256) k_fwd_list(DevGraph g, DevState st) {
+  const uint32_t K = __ldcg(&st.lc[L_FL]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st.counters[C_ACTIVE] = K;
+    st.counters[C_BYTES] += g.bv_bytes + 4ull * K;
+    st.counters[C_REFBYTES] += g.bv_refbytes + 4ull * K;
+    reset_round_counters(st);
+    st.lc[L_DL] = 0;
+  }
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < K; j += gridDim.x * blockDim.x) {
+    const uint32_t gid = st.FL[j];
+    const uint32_t s = st.own_slot[gid];
+    st.AL[j] = s;
+    st.mprop[s] = st.prop[gid];
+    atomicOr(&st.FB[s >> 5], 1u << (s & 31));
+  }
+}
+
+// Backward sync from the dirty list: send (retire) each dirty slot's value,
+// clear its dirty bit, and aggregate it into the compute-side
+// vertex_updates, listing every gid whose entry became dirty.  Also retires
+// the old frontier (its FB and F bits), which nothing reads after the
+// edge-map.
+template <int A>
+__global__ void __launch_bounds__(256) k_bwd_list(DevGraph g, DevState st) {
+  const uint32_t n = __ldcg(&st.lc[L_DL]);
+  const uint32_t K = (uint32_t)__ldcg(&st.counters[C_ACTIVE]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st.counters[C_BYTES] += g.bv_bytes + 4ull * n;
+    st.counters[C_REFBYTES] += g.bv_refbytes + 4ull * n;
+    st.lc[L_FL] = 0;  // the update rebuilds it; entries below are read by index
+  }
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < K; j += gridDim.x * blockDim.x) {
+    const uint32_t s = st.AL[j], gid = st.FL[j];
+    atomicAnd(&st.FB[s >> 5], ~(1u << (s & 31)));
+    atomicAnd(&st.F[gid >> 5], ~(1u << (gid & 31)));
+  }
+  for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+    const uint32_t j = b + threadIdx.x;
+    bool listed = false;
+    uint32_t gid = 0;
+    if (j < n) {
+      const uint32_t s = st.DL[j];
+      const uint32_t v = st.mupd[s];
+      gid = __ldg(&g.slot_gid[s]);
+      retire_update<A>(st, s, v);
+      st.BV[j] = v;
+      atomicAnd(&st.MD[s >> 5], ~(1u << (s & 31)));
+      if (A == A_PR_DELTA) {
+        atomicAdd(reinterpret_cast<float*>(st.upd) + gid, __uint_as_float(v));
+        listed = claim_bit(st.UD, gid);
+      } else if (v < __ldcg(&st.upd[gid])) {
+        if (v < atomicMin(&st.upd[gid], v)) listed = claim_bit(st.UD, gid);
+      }
+    }
+    block_append(st.UL, st.lc + L_UL, listed, gid);
+  }
+}
+
 // ------------------------------------------------------------------ update --
 // UpdateWorker::update = update_frontier() then apply_updates()
-// (src/Workers.cpp:77-82), over the vertex_updates dirty set; rebuilds the
-// frontier bitmap (frontier.reset() first, src/GraphAlgorithm.cpp:646),
-// clears the dirty bits (clear_uv, :661) and counts |frontier|.
-// PageRank: pr.cpp:123-147 then :63-88.  prev_updates is set and reset within
-// the same round for every frontier vertex, so its test is always true and
-// the array is not kept.  CC/SSSP: cc.cpp:86-107, sssp.cpp:92-113.
+// (src/Workers.cpp:77-82) for one vertex whose vertex_updates entry is dirty.
+// PageRank: pr.cpp:123-147 then :63-88.  prev_updates is set and reset
+// within the same round for every frontier vertex, so its test is always
+// true and the array is not kept.  CC/SSSP: cc.cpp:86-107, sssp.cpp:92-113.
+// Returns true when v joins the frontier; `visited` collects the out-degree
+// of SSSP vertices reached for the first time.
+template <int A>
+__device__ __forceinline__ bool update_one(const DevGraph& g, const DevState& st, uint32_t v, double tol,
+                                           double damping, uint32_t& visited) {
+  if (A == A_PR_DELTA) {
+    const float u = __uint_as_float(st.upd[v]);
+    if ((double)u > tol) {
+      st.ranks[v] = __fadd_rn(st.ranks[v], u);
+      st.prop[v] = __float_as_uint((float)(damping * (double)u / (double)g.outdeg[v]));
+      st.upd[v] = 0;
+      return true;
+    }
+    return false;
+  }
+  const uint32_t u = st.upd[v];
+  const uint32_t p = st.prop[v];
+  if (p > u) {
+    st.prop[v] = u;
+    if ((A == A_SSSP_HOP || A == A_SSSP_W) && p == 0xFFFFFFFFu) visited += g.outdeg[v];
+    return true;
+  }
+  return false;
+}
+
+// Frontier shape of one block, one counter update each.
+__device__ __forceinline__ void flush_frontier_shape(const DevState& st, uint32_t fcount, uint32_t fedges,
+                                                     uint32_t fmax, uint32_t visited) {
+  fcount = block_sum(fcount);
+  fedges = block_sum(fedges);
+  visited = block_sum(visited);
+  fmax = block_max(fmax);
+  if (threadIdx.x == 0) {
+    if (fcount) atomicAdd(&st.counters[C_FRONTIER], (unsigned long long)fcount);
+    if (fedges) atomicAdd(&st.counters[C_FEDGES], (unsigned long long)fedges);
+    if (fmax) atomicMax(&st.counters[C_FMAXDEG], (unsigned long long)fmax);
+    if (visited) atomicAdd(&st.counters[C_UNVISITED], 0ull - (unsigned long long)visited);
+  }
+}
+
+// Update over the updated-gid list (list rounds).  The last block to finish
+// empties the list.
+template <int A>
+__global__ void __launch_bounds__(256) k_update_list(DevGraph g, DevState st, double tol, double damping) {
+  const uint32_t n = __ldcg(&st.lc[L_UL]);
+  uint32_t fcount = 0, fedges = 0, fmax = 0, visited = 0;
+  for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+    const uint32_t j = b + threadIdx.x;
+    bool nf = false;
+    uint32_t v = 0;
+    if (j < n) {
+      v = st.UL[j];
+      atomicAnd(&st.UD[v >> 5], ~(1u << (v & 31)));
+      nf = update_one<A>(g, st, v, tol, damping, visited);
+      if (nf) {
+        atomicOr(&st.F[v >> 5], 1u << (v & 31));
+        const uint32_t d = g.outdeg[v];
+        ++fcount;
+        fedges += d;
+        fmax = max(fmax, d);
+      }
+    }
+    block_append(st.FL, st.lc + L_FL, nf, v);
+  }
+  flush_frontier_shape(st, fcount, fedges, fmax, visited);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&st.counters[C_DONE], 1ull) == gridDim.x - 1) {
+      st.lc[L_UL] = 0;  // every block has read n
+      st.counters[C_DONE] = 0;
+    }
+  }
+}
+
+// Update over the whole dirty bitmap (bitvector rounds): rebuilds the
+// frontier bitmap (frontier.reset() first, src/GraphAlgorithm.cpp:646) and
+// list, clears the dirty bits (clear_uv, :661) and records the frontier's
+// shape.  Block-uniform loop.
 template <int A>
 __global__ void __launch_bounds__(256) k_update(DevGraph g, DevState st, double tol, double damping) {
-  uint32_t cnt = 0;
+  uint32_t fcount = 0, fedges = 0, fmax = 0, visited = 0;
   for (uint32_t base = blockIdx.x * blockDim.x; base < g.V; base += gridDim.x * blockDim.x) {
     const uint32_t v = base + threadIdx.x;
-    uint32_t nf = 0;
+    bool nf = false;
     if (v < g.V && test_bit(st.UD, v)) {
-      if (A == A_PR_DELTA) {
-        const float u = __uint_as_float(st.upd[v]);
-        if ((double)u > tol) {
-          nf = 1;
-          st.ranks[v] = __fadd_rn(st.ranks[v], u);
-          st.prop[v] = __float_as_uint((float)(damping * (double)u / (double)g.outdeg[v]));
-          st.upd[v] = 0;
-        }
-      } else {
-        const uint32_t u = st.upd[v];
-        if (st.prop[v] > u) {
-          st.prop[v] = u;
-          nf = 1;
-        }
+      nf = update_one<A>(g, st, v, tol, damping, visited);
+      if (nf) {
+        const uint32_t d = g.outdeg[v];
+        ++fcount;
+        fedges += d;
+        fmax = max(fmax, d);
       }
     }
     const uint32_t m = __ballot_sync(FULL, nf);
     if (lane_id() == 0 && v < g.V) {  // v is the first gid of this word
       st.F[v >> 5] = m;
       st.UD[v >> 5] = 0;
-      cnt += __popc(m);
     }
+    block_append(st.FL, st.lc + L_FL, nf, v);
   }
-  cnt = block_sum(cnt);
-  if (threadIdx.x == 0 && cnt) atomicAdd(&st.counters[C_FRONTIER], (unsigned long long)cnt);
+  flush_frontier_shape(st, fcount, fedges, fmax, visited);
 }
 
 }  // namespace grd

@@ -89,7 +89,8 @@ typedef struct grd_params {
   int direction;        /* GRD_DIR_*                                          */
   int frontier_format;  /* GRD_FMT_*                                          */
   /* Schedule knobs (0 = built-in default); results never depend on them.   */
-  uint32_t dense_div;   /* dense dirty tracking when |F| >= S / dense_div (32)*/
+  uint32_t dense_div;   /* bitvector round when |F| >= S/dense_div or its
+                           out-edges >= E/dense_div (default 32)          */
   uint32_t pull_div;    /* AUTO pulls when |F| >= V / pull_div (2); needs the
                            in-edge view                                       */
   uint32_t push_blocks_per_sm; /* push grid; 0 = occupancy limit            */
@@ -189,14 +190,25 @@ int grd_get_stats(const grd_ctx* ctx, grd_stats* stats);
  * per round (cleared by grd_init). */
 int grd_set_profiling(grd_ctx* ctx, int enable);
 
+/* Round modes: direction x sync format.  Bitvector rounds sync through one
+ * bitvector per memory partition and track dirty slots densely; list rounds
+ * sync through (slot, value) lists of the frontier and of the dirty slots. */
+#define GRD_ROUND_PUSH_BITVEC 0
+#define GRD_ROUND_PUSH_LIST   1
+#define GRD_ROUND_PULL_BITVEC 2
+#define GRD_ROUND_PULL_LIST   3
+
 typedef struct grd_round_rec {
   uint32_t round;         /* 0-based round index                          */
-  int32_t mode;           /* 0 push sparse, 1 push dense, 2 pull          */
+  int32_t mode;           /* GRD_ROUND_* (direction x sync format)        */
   uint64_t frontier_in;   /* |frontier| entering the round                */
   uint64_t actives;       /* actives unpacked by the forward sync         */
   uint64_t edges;         /* edges the edge-map read this round           */
   uint64_t frontier_out;  /* |frontier| after the update                  */
   double ms[5];           /* fwd, edge-map, bwd+aggregate, update, round  */
+  uint64_t frontier_edges_in; /* out-edges of the entering frontier       */
+  uint64_t max_degree_in;     /* largest out-degree in it                 */
+  uint64_t unvisited_in;      /* SSSP: out-edges of unreached vertices    */
 } grd_round_rec;
 /* Copies up to cap records; *n = number recorded. */
 int grd_get_round_log(const grd_ctx* ctx, grd_round_rec* out, size_t cap,

@@ -25,15 +25,16 @@ GRAPHS = {
 
 
 FORMATS = [g.GRD_FMT_AUTO, g.GRD_FMT_BITVEC, g.GRD_FMT_LIST]
-# (direction, frontier format): push with sparse / dense dirty tracking, pull,
-# and the fixed heuristic choosing per round.
-MODES = [(g.GRD_DIR_PUSH, g.GRD_FMT_LIST), (g.GRD_DIR_PUSH, g.GRD_FMT_BITVEC), (g.GRD_DIR_PULL, g.GRD_FMT_AUTO),
-         (g.GRD_DIR_AUTO, g.GRD_FMT_AUTO)]
+# (direction, sync format): every round mode forced, and the fixed heuristic
+# choosing per round.
+MODES = [(g.GRD_DIR_PUSH, g.GRD_FMT_LIST), (g.GRD_DIR_PUSH, g.GRD_FMT_BITVEC), (g.GRD_DIR_PULL, g.GRD_FMT_BITVEC),
+         (g.GRD_DIR_PULL, g.GRD_FMT_LIST), (g.GRD_DIR_AUTO, g.GRD_FMT_AUTO)]
+MODE_IDS = ["push-list", "push-bitvec", "pull-bitvec", "pull-list", "auto"]
 
 
 @pytest.mark.parametrize("num_memory", [1, 3])
 @pytest.mark.parametrize("name", list(GRAPHS))
-@pytest.mark.parametrize("mode", MODES, ids=["push-list", "push-bitvec", "pull", "auto"])
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 def test_min_algorithms_bit_exact(gpu, name, num_memory, mode):
     G = GRAPHS[name]()
     ro, ci, w = G.row_offsets, G.col_indices, G.weights
@@ -58,7 +59,7 @@ def test_min_algorithms_bit_exact(gpu, name, num_memory, mode):
             assert st["reference_bytes_moved"] == ref["stats"]["reference_bytes_moved"]
 
 
-@pytest.mark.parametrize("mode", MODES, ids=["push-list", "push-bitvec", "pull", "auto"])
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 def test_device_loop_matches_host_loop(gpu, mode):
     """One CUDA-graph launch (device-side policy + switch + while) gives the
     same results and statistics as the host-driven loop."""
@@ -96,6 +97,59 @@ def test_device_loop_respects_round_cap(gpu):
         np.testing.assert_array_equal(ctx.read_props(), ref["props"])
 
 
+def test_round_log_modes_follow_policy(gpu):
+    """Forced formats run every round in that mode; the fixed rule mixes
+    bitvector rounds (large frontiers) and list rounds (small ones)."""
+    G = g.Graph.rmat(14, 8, symmetrize=True, weighted=True)
+    expect = {(g.GRD_DIR_PUSH, g.GRD_FMT_LIST): {g.GRD_ROUND_PUSH_LIST},
+              (g.GRD_DIR_PUSH, g.GRD_FMT_BITVEC): {g.GRD_ROUND_PUSH_BITVEC},
+              (g.GRD_DIR_PULL, g.GRD_FMT_LIST): {g.GRD_ROUND_PULL_LIST},
+              (g.GRD_DIR_PULL, g.GRD_FMT_BITVEC): {g.GRD_ROUND_PULL_BITVEC}}
+    with g.Context(G, G.partition_edge_balanced(2), num_memory=2) as ctx:
+        ctx.set_profiling(True)
+        for (d, f), modes in expect.items():
+            ctx.set_algo(g.GRD_CC, direction=d, frontier_format=f)
+            ctx.init()
+            ctx.run()
+            assert {r["mode"] for r in ctx.round_log()} == modes
+    # a fresh context has no in-edge view, so the fixed rule only pushes
+    with g.Context(G, G.partition_edge_balanced(2), num_memory=2) as ctx:
+        ctx.set_profiling(True)
+        ctx.set_algo(g.GRD_CC)
+        ctx.init()
+        ctx.run()
+        log = ctx.round_log()
+        tile = 8192  # slots per partition are padded to whole compaction tiles
+        S = sum(-(-(no + npx) // tile) * tile for no, npx, _ in (ctx.layout_info(p) for p in range(2)))
+        for r in log:
+            big = r["frontier_in"] * 32 >= S or r["frontier_edges_in"] * 32 >= G.num_edges
+            assert r["mode"] == (g.GRD_ROUND_PUSH_BITVEC if big else g.GRD_ROUND_PUSH_LIST)
+        assert {r["mode"] for r in log} == {g.GRD_ROUND_PUSH_BITVEC, g.GRD_ROUND_PUSH_LIST}
+
+
+@pytest.mark.parametrize("algo", [g.GRD_CC, g.GRD_SSSP_W])
+def test_values_aggregated_between_rounds_reach_list_rounds(gpu, algo):
+    """grd_aggregate_values before a run: list rounds see the same updated
+    gids as bitvector rounds."""
+    G = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
+    gids = np.array([5, 77, 5, 1000], dtype=np.uint32)
+    vals = np.array([0, 3, 2, 1], dtype=np.uint32)
+    outs = []
+    with g.Context(G, G.partition_edge_balanced(3), num_memory=3) as ctx:
+        for fmt in (g.GRD_FMT_BITVEC, g.GRD_FMT_LIST):
+            for host_loop in (True, False):
+                ctx.set_algo(algo, frontier_format=fmt)
+                ctx.init()
+                rc = ctx._lib.grd_aggregate_values(ctx._ctx, gids.ctypes.data_as(g._ffi.u32p),
+                                                   vals.ctypes.data_as(g._ffi.u32p), len(gids))
+                assert rc == 0
+                ctx.run(host_loop=host_loop)
+                outs.append((ctx.read_props(), ctx.read_updates()))
+    for p, u in outs[1:]:
+        np.testing.assert_array_equal(p, outs[0][0])
+        np.testing.assert_array_equal(u, outs[0][1])
+
+
 @pytest.mark.parametrize("num_memory", [1, 3])
 def test_stage_api_matches_oracle_round_by_round(gpu, num_memory):
     G = g.Graph.rmat(11, 8, symmetrize=True, weighted=True)
@@ -118,7 +172,7 @@ def test_stage_api_matches_oracle_round_by_round(gpu, num_memory):
 
 
 @pytest.mark.parametrize("num_memory", [1, 3])
-@pytest.mark.parametrize("mode", MODES, ids=["push-list", "push-bitvec", "pull", "auto"])
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 def test_pr_delta_close_to_oracle(gpu, num_memory, mode):
     G = g.Graph.rmat(14, 16)
     ro, ci = G.row_offsets, G.col_indices
