@@ -15,14 +15,15 @@ import numpy as np
 from . import _ffi
 from ._ffi import (GRD_CC, GRD_DIR_AUTO, GRD_DIR_PULL, GRD_DIR_PUSH, GRD_FMT_AUTO, GRD_FMT_BITVEC,
                    GRD_FMT_LIST, GRD_PR_DELTA, GRD_PR_PULL, GRD_ROUND_PULL_BITVEC, GRD_ROUND_PULL_LIST,
-                   GRD_ROUND_PUSH_BITVEC, GRD_ROUND_PUSH_LIST, GRD_RUN_STRICT, GRD_SSSP_HOP, GRD_SSSP_W)
+                   GRD_ROUND_PUSH_BITVEC, GRD_ROUND_PUSH_LIST, GRD_RUN_STRICT, GRD_SSSP_HOP, GRD_SSSP_W,
+                   GRD_POLICY_FIXED, GRD_POLICY_LEARNED)
 
 __all__ = [
     "GrdError", "Graph", "Context", "lib", "device_count", "rmat_seed",
     "GRD_PR_DELTA", "GRD_PR_PULL", "GRD_CC", "GRD_SSSP_HOP", "GRD_SSSP_W",
     "GRD_DIR_AUTO", "GRD_DIR_PUSH", "GRD_DIR_PULL", "GRD_FMT_AUTO", "GRD_FMT_BITVEC", "GRD_FMT_LIST",
     "GRD_ROUND_PUSH_BITVEC", "GRD_ROUND_PUSH_LIST", "GRD_ROUND_PULL_BITVEC", "GRD_ROUND_PULL_LIST",
-    "GRD_RUN_STRICT", "ALGO_NAMES",
+    "GRD_POLICY_FIXED", "GRD_POLICY_LEARNED", "GRD_RUN_STRICT", "ALGO_NAMES",
 ]
 
 ALGO_NAMES = {"pr": GRD_PR_DELTA, "pr_delta": GRD_PR_DELTA, "pr_pull": GRD_PR_PULL, "cc": GRD_CC,
@@ -235,15 +236,22 @@ class Context:
     def set_algo(self, algo, source: int = 0, max_rounds: int = 1000, damping: float = 0.85,
                  tolerance: Optional[float] = None, direction: int = GRD_DIR_AUTO,
                  frontier_format: int = GRD_FMT_AUTO, dense_div: int = 0, pull_div: int = 0,
-                 push_blocks_per_sm: int = 0) -> None:
+                 push_blocks_per_sm: int = 0, policy: int = _ffi.GRD_POLICY_FIXED) -> None:
+        """policy=GRD_POLICY_LEARNED picks each round's mode with the model
+        given to set_policy (the fixed rule while none is set)."""
         if isinstance(algo, str):
             algo = ALGO_NAMES[algo]
         if tolerance is None:
             tolerance = 1e-7 if algo == GRD_PR_PULL else 1e-6
         p = _ffi.grd_params(source, max_rounds, damping, tolerance, direction, frontier_format, dense_div, pull_div,
-                            push_blocks_per_sm)
+                            push_blocks_per_sm, policy)
         self._check(self._lib.grd_set_algo(self._ctx, algo, C.byref(p)))
         self.algo = algo
+
+    def set_policy(self, model) -> None:
+        """Uploads a learned round-policy model (a grd_policy_model, or None
+        to clear it)."""
+        self._check(self._lib.grd_set_policy(self._ctx, C.byref(model) if model is not None else None))
 
     def init(self) -> None:
         self._check(self._lib.grd_init(self._ctx))

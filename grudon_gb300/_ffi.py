@@ -36,6 +36,7 @@ ERROR_NAMES = {
 u8p = C.POINTER(C.c_uint8)
 u32p = C.POINTER(C.c_uint32)
 u64p = C.POINTER(C.c_uint64)
+f32p = C.POINTER(C.c_float)
 
 
 class grd_csr(C.Structure):
@@ -46,7 +47,8 @@ class grd_csr(C.Structure):
 class grd_params(C.Structure):
     _fields_ = [("source", C.c_uint32), ("max_rounds", C.c_uint32), ("damping", C.c_double),
                 ("tolerance", C.c_double), ("direction", C.c_int), ("frontier_format", C.c_int),
-                ("dense_div", C.c_uint32), ("pull_div", C.c_uint32), ("push_blocks_per_sm", C.c_uint32)]
+                ("dense_div", C.c_uint32), ("pull_div", C.c_uint32), ("push_blocks_per_sm", C.c_uint32),
+                ("policy", C.c_int)]
 
 
 class grd_stats(C.Structure):
@@ -55,6 +57,24 @@ class grd_stats(C.Structure):
                 ("last_residual", C.c_double), ("push_rounds", C.c_uint32), ("pull_rounds", C.c_uint32),
                 ("actives_total", C.c_uint64), ("kernel_launches", C.c_uint64), ("stage_ms", C.c_double * 5),
                 ("device_loop", C.c_uint32), ("push_actives", C.c_uint64)]
+
+
+GRD_POLICY_FIXED, GRD_POLICY_LEARNED = 0, 1
+GRD_POLICY_IN, GRD_POLICY_HID, GRD_POLICY_OUT = 8, 64, 4
+GRD_POLICY_NPARAM = (GRD_POLICY_HID * GRD_POLICY_IN + GRD_POLICY_HID + GRD_POLICY_HID * GRD_POLICY_HID +
+                     GRD_POLICY_HID + GRD_POLICY_OUT * GRD_POLICY_HID + GRD_POLICY_OUT)
+
+
+class grd_policy_model(C.Structure):
+    _fields_ = [("mean", C.c_float * GRD_POLICY_IN), ("scale", C.c_float * GRD_POLICY_IN),
+                ("w1", C.c_uint16 * (GRD_POLICY_HID * GRD_POLICY_IN)), ("b1", C.c_float * GRD_POLICY_HID),
+                ("w2", C.c_uint16 * (GRD_POLICY_HID * GRD_POLICY_HID)), ("b2", C.c_float * GRD_POLICY_HID),
+                ("w3", C.c_uint16 * (GRD_POLICY_OUT * GRD_POLICY_HID)), ("b3", C.c_float * GRD_POLICY_OUT)]
+
+
+class grd_policy_train_cfg(C.Structure):
+    _fields_ = [("steps", C.c_uint32), ("lr", C.c_float), ("weight_decay", C.c_float), ("seed", C.c_uint64),
+                ("device", C.c_int)]
 
 
 class grd_round_rec(C.Structure):
@@ -87,6 +107,14 @@ SIGNATURES = {
     "grd_update": (C.c_int, [C.c_void_p, u64p]),
     "grd_aggregate_values": (C.c_int, [C.c_void_p, u32p, u32p, C.c_size_t]),
     "grd_aggregate_values_noalloc": (C.c_int, [C.c_void_p, u32p, u32p, C.c_size_t]),
+    "grd_set_policy": (C.c_int, [C.c_void_p, C.POINTER(grd_policy_model)]),
+    "grd_policy_features": (C.c_int, [u64p, u64p, u64p, u64p, u32p, C.c_uint32, C.c_uint64, C.c_size_t, f32p]),
+    "grd_policy_train": (C.c_int, [f32p, f32p, u8p, C.c_size_t, C.POINTER(grd_policy_train_cfg),
+                                   C.POINTER(grd_policy_model), f32p]),
+    "grd_policy_grad": (C.c_int, [C.POINTER(grd_policy_model), f32p, f32p, u8p, C.c_size_t, C.c_int, f32p, f32p]),
+    "grd_policy_predict": (C.c_int, [C.POINTER(grd_policy_model), f32p, C.c_size_t, C.c_uint32, C.c_int, f32p,
+                                     C.POINTER(C.c_int32)]),
+    "grd_policy_error": (C.c_char_p, []),
     "grd_run": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(grd_stats)]),
     "grd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(grd_stats)]),
     "grd_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),

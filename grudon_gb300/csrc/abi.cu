@@ -250,6 +250,40 @@ int grd_choose_round_mode(const grd_ctx* ctx) {
   return pull ? (list ? RM_PULL_LIST : RM_PULL_BITVEC) : (list ? RM_PUSH_LIST : RM_PUSH_BITVEC);
 }
 
+PolicyArgs grd_policy_args(const grd_ctx* ctx) {
+  PolicyArgs a{};
+  a.direction = ctx->params.direction;
+  a.format = ctx->params.frontier_format;
+  a.has_in = ctx->in_edges_alloc ? 1 : 0;
+  a.dense_div = ctx->params.dense_div;
+  a.pull_div = ctx->params.pull_div;
+  a.edges = ctx->L.E;
+  a.round = ctx->stats.rounds;
+  return a;
+}
+
+const grd_policy_model* grd_policy_model_dev(const grd_ctx* ctx) {
+  return (ctx->params.policy == GRD_POLICY_LEARNED && ctx->has_policy) ? ctx->policy_dev : nullptr;
+}
+
+// Host loop: the next round's mode, by the same policy kernel the device
+// loop runs (so both loops choose identically), read back.
+static int host_loop_mode(grd_ctx* ctx, int* mode) {
+  const grd_policy_model* m = grd_policy_model_dev(ctx);
+  if (!m) {
+    *mode = grd_choose_round_mode(ctx);
+    return GRD_OK;
+  }
+  k_policy<false><<<1, P_HID, 0, ctx->stream>>>(ctx->g, ctx->st, 0, grd_policy_args(ctx), m);
+  CK_LAUNCH();
+  CK(cudaMemcpyAsync(ctx->h_seed + 7, ctx->st.counters + C_MODE, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *mode = (int)ctx->h_seed[7];
+  ctx->stats.kernel_launches += 1;
+  return GRD_OK;
+}
+
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
   const uint32_t T = ctx->g.num_tiles;
   k_fwd_bits<<<T, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
@@ -445,7 +479,14 @@ int grd_read_counters(grd_ctx* ctx) {
 // Stage timing: events 0..4 bracket forward sync, edge-map, backward sync and
 // update of one round; read after the round's synchronisation.
 void grd_prof_mark(grd_ctx* ctx, int i) {
-  if (ctx->profiling) cudaEventRecord(ctx->ev[i], ctx->stream);
+  if (!ctx->profiling) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(ctx->stream, &cs);
+  // inside a captured round graph the mark becomes an event-record node
+  if (cs == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(ctx->ev[i], ctx->stream, cudaEventRecordExternal);
+  else
+    cudaEventRecord(ctx->ev[i], ctx->stream);
 }
 
 void grd_prof_collect(grd_ctx* ctx, double* out) {
@@ -569,7 +610,11 @@ int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
   p.direction = GRD_DIR_AUTO;
   p.frontier_format = GRD_FMT_AUTO;
   if (params) p = *params;
-  if (p.dense_div == 0) p.dense_div = 32;
+  if (p.dense_div == 0) p.dense_div = 8;
+  if (p.policy != GRD_POLICY_FIXED && p.policy != GRD_POLICY_LEARNED) {
+    ctx->err = "unknown policy";
+    return GRD_E_INVALID;
+  }
   if (p.pull_div == 0) p.pull_div = 2;
   if (p.push_blocks_per_sm > 32) {
     ctx->err = "push_blocks_per_sm must be <= 32";
@@ -588,7 +633,8 @@ int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
     return GRD_E_INVALID;
   }
   CK(cudaSetDevice(ctx->device));
-  if (algo == GRD_PR_PULL || p.direction == GRD_DIR_PULL) {
+  if (algo == GRD_PR_PULL || p.direction == GRD_DIR_PULL ||
+      (p.policy == GRD_POLICY_LEARNED && p.direction == GRD_DIR_AUTO)) {  // the model may pull
     int rc = grd_ensure_in_edges(ctx);
     if (rc != GRD_OK) return rc;
   }
@@ -742,9 +788,13 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
       const uint64_t f_in = ctx->last_frontier, e_in = ctx->stats.edges_scanned;
       const uint64_t fe_in = ctx->h_counters[C_FEDGES], fm_in = ctx->h_counters[C_FMAXDEG],
                      un_in = ctx->h_counters[C_UNVISITED];
-      const int mode = grd_choose_round_mode(ctx);
+      int mode;
+      TRY(host_loop_mode(ctx, &mode));
       grd_prof_mark(ctx, 0);
-      TRY(grd_enqueue_round(ctx, mode));
+      if (ctx->profiling)
+        TRY(grd_round_graph_launch(ctx, mode));
+      else
+        TRY(grd_enqueue_round(ctx, mode));
       grd_prof_mark(ctx, 4);
       ctx->last_mode = mode;
       if (rm_is_pull(mode)) {
@@ -779,6 +829,25 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
     ctx->err = "round cap reached with a non-empty frontier";
     return GRD_E_ROUND_CAP;
   }
+  return GRD_OK;
+}
+
+int grd_set_policy(grd_ctx* ctx, const grd_policy_model* model) {
+  if (!ctx) return GRD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  grd_graph_release(ctx);  // the loop graph holds the model pointer (or none)
+  if (!model) {
+    ctx->has_policy = false;
+    return GRD_OK;
+  }
+  if (!ctx->policy_dev) {
+    void* p = nullptr;
+    TRY(grd_dev_alloc_bytes(ctx, &p, sizeof(grd_policy_model)));
+    ctx->policy_dev = static_cast<grd_policy_model*>(p);
+  }
+  CK(cudaMemcpyAsync(ctx->policy_dev, model, sizeof(grd_policy_model), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->has_policy = true;
   return GRD_OK;
 }
 

@@ -8,6 +8,7 @@
 #include "../../include/grudon_gpu.h"
 #include "kernels.cuh"
 #include "layout.hpp"
+#include "policy.cuh"
 
 struct PullState {
   uint32_t* comp = nullptr;       // [V] Kahan compensation of the aggregate
@@ -42,6 +43,7 @@ struct grd_ctx {
   int last_mode = -1;          // edge-map mode of the round in flight (host loop)
   cudaGraph_t run_graph = nullptr;     // device-driven round loop (graph_run.cu)
   cudaGraphExec_t run_exec = nullptr;
+  cudaGraphExec_t round_exec[4] = {};  // one round per mode (profiled host loop)
   bool graph_failed = false;           // building it failed here: host loop
   std::string graph_error;
   uint32_t* agg_buf = nullptr; // staging of grd_aggregate_values (gids, values)
@@ -49,6 +51,8 @@ struct grd_ctx {
   bool profiling = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<void*> host_registered;  // layout arrays pinned for H2D uploads
+  grd_policy_model* policy_dev = nullptr;  // learned round policy (device copy)
+  bool has_policy = false;
 };
 
 // Error plumbing shared by the host translation units (expects a `ctx`).
@@ -104,8 +108,14 @@ uint32_t grd_round_launches(const grd_ctx* ctx, int mode);
 int grd_enqueue_fwd_list(grd_ctx* ctx);
 int grd_enqueue_bwd_update_list(grd_ctx* ctx);
 int grd_enqueue_round(grd_ctx* ctx, int mode);
+// Policy inputs of this ctx, and the model the device loop uses (nullptr:
+// the fixed rule).
+grd::PolicyArgs grd_policy_args(const grd_ctx* ctx);
+const grd_policy_model* grd_policy_model_dev(const grd_ctx* ctx);
 // Device-driven loop (graph_run.cu).
 int grd_graph_run(grd_ctx* ctx, bool* used);
+// One round in `mode` as one graph launch (built on first use).
+int grd_round_graph_launch(grd_ctx* ctx, int mode);
 void grd_graph_release(grd_ctx* ctx);
 int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate);
 int grd_enqueue_update(grd_ctx* ctx);

@@ -19,37 +19,11 @@
 
 #include "ctx.hpp"
 #include "kernels.cuh"
+#include "policy.cuh"
 
 using namespace grd;
 
 namespace {
-
-struct PolicyArgs {
-  int direction, format, has_in;
-  uint32_t dense_div, pull_div;
-  uint32_t launches[NUM_ROUND_MODES];  // kernels of one round per mode
-  unsigned long long edges;
-};
-
-__global__ void k_policy(DevGraph g, DevState st, cudaGraphConditionalHandle sw, PolicyArgs a) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  const unsigned long long f = st.counters[C_FRONTIER];
-  const bool pull =
-      a.has_in && (a.direction == GRD_DIR_PULL || (a.direction == GRD_DIR_AUTO && f * a.pull_div >= g.V));
-  const unsigned long long fe = st.counters[C_FEDGES];
-  const bool list = a.format == GRD_FMT_LIST ||
-                    (a.format == GRD_FMT_AUTO && f * a.dense_div < g.S && fe * a.dense_div < a.edges);
-  const int mode = pull ? (list ? RM_PULL_LIST : RM_PULL_BITVEC) : (list ? RM_PUSH_LIST : RM_PUSH_BITVEC);
-  st.counters[C_MODE] = mode;
-  if (pull) {
-    st.counters[C_PULL_ROUNDS] += 1;
-    st.counters[C_EDGES] += a.edges;
-  } else {
-    st.counters[C_PUSH_ROUNDS] += 1;
-  }
-  st.counters[C_LAUNCHES] += a.launches[mode];
-  cudaGraphSetConditional(sw, (unsigned)mode);
-}
 
 __global__ void k_round_end(DevState st, cudaGraphConditionalHandle wh, uint32_t max_rounds) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
@@ -117,19 +91,13 @@ int build(grd_ctx* ctx) {
     loop_body = p.conditional.phGraph_out[0];
   }
   CK(cudaGraphConditionalHandleCreate(&sw, loop_body, 0, 0));
-  PolicyArgs pa{};
-  pa.direction = ctx->params.direction;
-  pa.format = ctx->params.frontier_format;
-  pa.has_in = ctx->in_edges_alloc ? 1 : 0;
-  pa.dense_div = ctx->params.dense_div;
-  pa.pull_div = ctx->params.pull_div;
-  pa.edges = ctx->L.E;
+  PolicyArgs pa = grd_policy_args(ctx);
   for (int m = 0; m < NUM_ROUND_MODES; ++m) pa.launches[m] = 2 /*policy, round end*/ + grd_round_launches(ctx, m);
 
   int rc = capture_into(ctx, loop_body);
   if (rc != GRD_OK) return rc;
   cudaGraph_t branches[NUM_ROUND_MODES] = {};
-  k_policy<<<1, 32, 0, ctx->stream>>>(ctx->g, ctx->st, sw, pa);
+  k_policy<true><<<1, P_HID, 0, ctx->stream>>>(ctx->g, ctx->st, sw, pa, grd_policy_model_dev(ctx));
   rc = add_conditional(ctx, ctx->stream, sw, cudaGraphCondTypeSwitch, NUM_ROUND_MODES, branches);
   if (rc == GRD_OK) k_round_end<<<1, 32, 0, ctx->stream>>>(ctx->st, wh, ctx->params.max_rounds);
   const int rc_end = end_capture(ctx, loop_body);
@@ -155,6 +123,35 @@ void grd_graph_release(grd_ctx* ctx) {
   if (ctx->run_graph) cudaGraphDestroy(ctx->run_graph);
   ctx->run_exec = nullptr;
   ctx->run_graph = nullptr;
+  for (auto& e : ctx->round_exec) {
+    if (e) cudaGraphExecDestroy(e);
+    e = nullptr;
+  }
+}
+
+// Profiled host-loop rounds run as one graph launch each, so their timings
+// carry the device loop's launch costs (the learned policy trains on them).
+int grd_round_graph_launch(grd_ctx* ctx, int mode) {
+  if (!ctx->round_exec[mode]) {
+    const grd_stats saved = ctx->stats;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = grd_enqueue_round(ctx, mode);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->stats = saved;
+    if (rc != GRD_OK || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      (void)cudaGetLastError();
+      if (rc != GRD_OK) return rc;
+      CK(e);
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&ctx->round_exec[mode], g, 0);
+    cudaGraphDestroy(g);
+    CK(ie);
+  }
+  CK(cudaGraphLaunch(ctx->round_exec[mode], ctx->stream));
+  ctx->stats.kernel_launches += grd_round_launches(ctx, mode);
+  return GRD_OK;
 }
 
 // Runs the rest of the algorithm as one graph launch.  Returns GRD_OK with

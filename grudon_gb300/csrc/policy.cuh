@@ -1,0 +1,133 @@
+// Per-round mode choice on the device: the fixed threshold rule and the
+// learned MLP (inference by one 64-thread block, fused into the round's
+// policy kernel).  No reference counterpart: the reference's only per-round
+// decision engine, the NDP/INC offload rule
+// (include/offload_engine/NDPEngine.hpp:17-50), is disabled in its run().
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/grudon_gpu.h"
+#include "kernels.cuh"
+
+namespace grd {
+
+constexpr int P_IN = GRD_POLICY_IN, P_HID = GRD_POLICY_HID, P_OUT = GRD_POLICY_OUT;
+static_assert(P_OUT == 4, "one output per round mode");
+
+struct PolicyArgs {
+  int direction, format, has_in;
+  uint32_t dense_div, pull_div;
+  uint32_t launches[4];     // kernels of one round per mode (device loop stats)
+  unsigned long long edges; // E
+  uint32_t round;           // round index (host loop; the device loop counts)
+};
+
+// Raw policy features (grd_policy_features computes the same on the host).
+__host__ __device__ inline void policy_features(double frontier, double fedges, double unvisited, double maxdeg,
+                                                double round, double V, double E, float* f) {
+  f[0] = log2f((float)(1.0 + frontier));
+  f[1] = log2f((float)(1.0 + fedges));
+  f[2] = log2f((float)(1.0 + unvisited));
+  f[3] = log2f((float)(1.0 + fedges / (frontier > 1.0 ? frontier : 1.0)));
+  f[4] = log2f((float)(1.0 + maxdeg));
+  f[5] = log2f((float)(1.0 + round));
+  f[6] = log2f((float)(V > 1.0 ? V : 1.0));
+  f[7] = log2f((float)(1.0 + E / (V > 1.0 ? V : 1.0)));
+}
+
+// Modes the round may use: forced direction / format, and pull only with
+// the in-edge view.  Bit m = round mode m (0 push+bitvector, 1 push+list,
+// 2 pull+bitvector, 3 pull+list).
+__host__ __device__ inline uint32_t policy_allowed(int direction, int format, bool has_in) {
+  uint32_t dir = 0x3u << 0 | 0x3u << 2;  // both directions
+  if (direction == GRD_DIR_PUSH || !has_in) dir &= 0x3u;
+  if (direction == GRD_DIR_PULL && has_in) dir &= 0xCu;
+  uint32_t fmt = 0xFu;
+  if (format == GRD_FMT_BITVEC) fmt = 0x5u;
+  if (format == GRD_FMT_LIST) fmt = 0xAu;
+  return dir & fmt;
+}
+
+__device__ __forceinline__ float h2f(uint16_t b) { return __half2float(__ushort_as_half(b)); }
+
+// MLP forward for one input by a block of exactly P_HID threads.  xs: the
+// normalised input (shared), out: P_OUT predictions (shared).  Fixed
+// summation order (fmaf chains in index order).
+__device__ __forceinline__ void policy_mlp_block(const grd_policy_model* m, const float* xs, float* h1, float* h2,
+                                                 float* out) {
+  const int j = threadIdx.x;
+  float a = m->b1[j];
+#pragma unroll
+  for (int i = 0; i < P_IN; ++i) a = fmaf(h2f(m->w1[j * P_IN + i]), xs[i], a);
+  h1[j] = fmaxf(a, 0.0f);
+  __syncthreads();
+  a = m->b2[j];
+#pragma unroll 8
+  for (int k = 0; k < P_HID; ++k) a = fmaf(h2f(m->w2[j * P_HID + k]), h1[k], a);
+  h2[j] = fmaxf(a, 0.0f);
+  __syncthreads();
+  if (j < P_OUT) {
+    float o = m->b3[j];
+#pragma unroll 8
+    for (int k = 0; k < P_HID; ++k) o = fmaf(h2f(m->w3[j * P_HID + k]), h2[k], o);
+    out[j] = o;
+  }
+  __syncthreads();
+}
+
+// Fixed rule (grd_choose_round_mode applies the same on the host).
+__device__ __forceinline__ int policy_fixed(const DevGraph& g, const PolicyArgs& a, unsigned long long f,
+                                            unsigned long long fe) {
+  const bool pull =
+      a.has_in && (a.direction == GRD_DIR_PULL || (a.direction == GRD_DIR_AUTO && f * a.pull_div >= g.V));
+  const bool list = a.format == GRD_FMT_LIST ||
+                    (a.format == GRD_FMT_AUTO && f * a.dense_div < g.S && fe * a.dense_div < a.edges);
+  return pull ? (list ? GRD_ROUND_PULL_LIST : GRD_ROUND_PULL_BITVEC)
+              : (list ? GRD_ROUND_PUSH_LIST : GRD_ROUND_PUSH_BITVEC);
+}
+
+// Mode of the next round, by a block of P_HID threads (valid in thread 0).
+__device__ __forceinline__ int policy_choose(const DevGraph& g, const DevState& st, const PolicyArgs& a,
+                                             const grd_policy_model* model, uint32_t round) {
+  __shared__ float s_x[P_IN], s_h1[P_HID], s_h2[P_HID], s_out[P_OUT];
+  const unsigned long long f = st.counters[C_FRONTIER], fe = st.counters[C_FEDGES];
+  if (model == nullptr) return policy_fixed(g, a, f, fe);
+  if (threadIdx.x == 0) {
+    float raw[P_IN];
+    policy_features((double)f, (double)fe, (double)st.counters[C_UNVISITED], (double)st.counters[C_FMAXDEG],
+                    (double)round, (double)g.V, (double)a.edges, raw);
+    for (int i = 0; i < P_IN; ++i) s_x[i] = (raw[i] - model->mean[i]) * model->scale[i];
+  }
+  __syncthreads();
+  policy_mlp_block(model, s_x, s_h1, s_h2, s_out);
+  const uint32_t allowed = policy_allowed(a.direction, a.format, a.has_in != 0);
+  int best = -1;
+  for (int m = 0; m < P_OUT; ++m)
+    if (((allowed >> m) & 1u) && (best < 0 || s_out[m] < s_out[best])) best = m;
+  return best < 0 ? policy_fixed(g, a, f, fe) : best;
+}
+
+// The round's policy kernel (one block of P_HID threads).  In the device
+// loop (kGraph) it also counts the round's statistics and selects the SWITCH
+// branch; in the host loop it only leaves the mode in C_MODE.
+template <bool kGraph>
+static __global__ void __launch_bounds__(P_HID) k_policy(DevGraph g, DevState st, cudaGraphConditionalHandle sw,
+                                                         PolicyArgs a, const grd_policy_model* model) {
+  const uint32_t round = kGraph ? (uint32_t)st.counters[C_ROUNDS] : a.round;
+  const int mode = policy_choose(g, st, a, model, round);
+  if (threadIdx.x != 0) return;
+  st.counters[C_MODE] = (unsigned long long)mode;
+  if (kGraph) {
+    if (mode >= GRD_ROUND_PULL_BITVEC) {
+      st.counters[C_PULL_ROUNDS] += 1;
+      st.counters[C_EDGES] += a.edges;
+    } else {
+      st.counters[C_PUSH_ROUNDS] += 1;
+    }
+    st.counters[C_LAUNCHES] += a.launches[mode];
+    cudaGraphSetConditional(sw, (unsigned)mode);
+  }
+}
+
+}  // namespace grd

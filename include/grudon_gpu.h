@@ -90,11 +90,17 @@ typedef struct grd_params {
   int frontier_format;  /* GRD_FMT_*                                          */
   /* Schedule knobs (0 = built-in default); results never depend on them.   */
   uint32_t dense_div;   /* bitvector round when |F| >= S/dense_div or its
-                           out-edges >= E/dense_div (default 32)          */
+                           out-edges >= E/dense_div (default 8)           */
   uint32_t pull_div;    /* AUTO pulls when |F| >= V / pull_div (2); needs the
                            in-edge view                                       */
   uint32_t push_blocks_per_sm; /* push grid; 0 = occupancy limit            */
+  int policy;           /* GRD_POLICY_FIXED (threshold rule above) or
+                           GRD_POLICY_LEARNED (model set by grd_set_policy;
+                           the fixed rule when none is set)               */
 } grd_params;
+
+#define GRD_POLICY_FIXED   0
+#define GRD_POLICY_LEARNED 1
 
 typedef struct grd_stats {
   uint32_t rounds;            /* reference "Iterations" statistic          */
@@ -291,6 +297,79 @@ int grd_partition_edge_balanced(const grd_host_graph* g, uint32_t num_memory,
 int grd_write_partition_file(const uint32_t* part, uint32_t n, const char* path);
 int grd_read_partition_file(const char* path, uint32_t n, uint32_t num_memory,
                             uint32_t* part);
+
+/* Learned round policy ----------------------------------------------------
+ * No reference counterpart: the reference's only per-round decision engine
+ * is the disabled NDP/INC offload rule (include/offload_engine/
+ * NDPEngine.hpp:17-50).  An MLP 8 -> 64 -> 64 -> 4 (ReLU) predicts log2 of
+ * the round time of each round mode (GRD_ROUND_*) from the shape of the
+ * frontier entering the round; the round runs in the allowed mode with the
+ * smallest prediction.  Weights are IEEE fp16 (bit patterns), biases and
+ * accumulation fp32.  Inputs, each then mapped x = (f - mean) * scale:
+ *   f0 log2(1+|F|)            f1 log2(1+out-edges of F)
+ *   f2 log2(1+unvisited out-edges, SSSP; 0 otherwise)
+ *   f3 log2(1+mean degree in F) f4 log2(1+max degree in F)
+ *   f5 log2(1+round index)    f6 log2(V)   f7 log2(1+E/V)
+ * The choice never changes CC/SSSP results (min fixed points; every mode
+ * computes the same values, dirty sets and round counts). */
+#define GRD_POLICY_IN  8
+#define GRD_POLICY_HID 64
+#define GRD_POLICY_OUT 4
+#define GRD_POLICY_NPARAM (GRD_POLICY_HID * GRD_POLICY_IN + GRD_POLICY_HID + \
+                           GRD_POLICY_HID * GRD_POLICY_HID + GRD_POLICY_HID + \
+                           GRD_POLICY_OUT * GRD_POLICY_HID + GRD_POLICY_OUT)
+
+typedef struct grd_policy_model {
+  float mean[GRD_POLICY_IN], scale[GRD_POLICY_IN];
+  uint16_t w1[GRD_POLICY_HID * GRD_POLICY_IN];   /* [out][in], fp16 */
+  float b1[GRD_POLICY_HID];
+  uint16_t w2[GRD_POLICY_HID * GRD_POLICY_HID];  /* [out][in], fp16 */
+  float b2[GRD_POLICY_HID];
+  uint16_t w3[GRD_POLICY_OUT * GRD_POLICY_HID];  /* [out][in], fp16 */
+  float b3[GRD_POLICY_OUT];
+} grd_policy_model;
+
+/* Uploads a model for GRD_POLICY_LEARNED runs (NULL clears it). */
+int grd_set_policy(grd_ctx* ctx, const grd_policy_model* model);
+
+/* Raw features f0..f7 of n rounds from their frontier shape (host helper,
+ * same formulas as the device). */
+int grd_policy_features(const uint64_t* frontier, const uint64_t* frontier_edges,
+                        const uint64_t* unvisited, const uint64_t* max_degree,
+                        const uint32_t* round, uint32_t num_vertices,
+                        uint64_t num_edges, size_t n, float* features);
+
+typedef struct grd_policy_train_cfg {
+  uint32_t steps;       /* full-batch Adam steps                            */
+  float lr;             /* Adam step size                                   */
+  float weight_decay;   /* L2 on weights (not biases)                       */
+  uint64_t seed;        /* initialisation                                   */
+  int device;
+} grd_policy_train_cfg;
+
+/* Trains on the GPU (own forward/backward kernels, Adam, fp32 master
+ * weights rounded to fp16 for every forward pass).  x: n x 8 raw features;
+ * y: n x 4 log2(round ms) targets; mask: n x 4 (1 = target measured).
+ * mean/scale of `model` are computed from x.  loss_curve (optional, `steps`
+ * entries) receives the masked MSE before each step. */
+int grd_policy_train(const float* x, const float* y, const uint8_t* mask,
+                     size_t n, const grd_policy_train_cfg* cfg,
+                     grd_policy_model* model, float* loss_curve);
+
+/* One forward + backward pass on the GPU: masked MSE and its gradient with
+ * respect to every parameter, in the order w1, b1, w2, b2, w3, b3
+ * (GRD_POLICY_NPARAM floats; fp16 weights are differentiated as values). */
+int grd_policy_grad(const grd_policy_model* model, const float* x,
+                    const float* y, const uint8_t* mask, size_t n, int device,
+                    float* loss, float* grad);
+
+/* GPU inference: out = n x 4 predictions, choice = argmin over the modes
+ * whose bit is set in allowed_mask (bit m = mode m). */
+int grd_policy_predict(const grd_policy_model* model, const float* x, size_t n,
+                       uint32_t allowed_mask, int device, float* out,
+                       int32_t* choice);
+/* Error text of the most recent failed grd_policy_* call on this thread. */
+const char* grd_policy_error(void);
 
 #ifdef __cplusplus
 }

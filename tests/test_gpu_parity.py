@@ -122,7 +122,7 @@ def test_round_log_modes_follow_policy(gpu):
         tile = 8192  # slots per partition are padded to whole compaction tiles
         S = sum(-(-(no + npx) // tile) * tile for no, npx, _ in (ctx.layout_info(p) for p in range(2)))
         for r in log:
-            big = r["frontier_in"] * 32 >= S or r["frontier_edges_in"] * 32 >= G.num_edges
+            big = r["frontier_in"] * 8 >= S or r["frontier_edges_in"] * 8 >= G.num_edges
             assert r["mode"] == (g.GRD_ROUND_PUSH_BITVEC if big else g.GRD_ROUND_PUSH_LIST)
         assert {r["mode"] for r in log} == {g.GRD_ROUND_PUSH_BITVEC, g.GRD_ROUND_PUSH_LIST}
 
