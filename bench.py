@@ -52,6 +52,11 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=512)
     ap.add_argument("--batch-sources", type=int, default=64)
+    ap.add_argument("--policy", choices=["auto", "fixed", "learned"], default="auto",
+                    help="round policy of the measured runs (auto: learned when the model file is present)")
+    ap.add_argument("--kernel-run", action="store_true",
+                    help="only run the workload's steps with the rounds driven from the host (plain kernel "
+                         "launches, no CUDA graphs) and print a short summary: the target of per-kernel profilers")
     return ap.parse_args()
 
 
@@ -76,8 +81,11 @@ def bench_batch(g, args, local) -> dict:
     tune_cc = autotune.tune(Uc.graph, g.GRD_CC, lambda c: c.init(), device=local, reps=2)
     best = tune_cc.best
     part = Uc.graph.partition_edge_balanced(best.num_memory) if best.num_memory > 1 else None
+    model = load_policy_model()
+    pol = g.GRD_POLICY_LEARNED if model is not None else g.GRD_POLICY_FIXED
     ctx_c = g.Context(Uc.graph, part, best.num_memory, local)
-    ctx_c.set_algo(g.GRD_CC, **best.params())
+    ctx_c.set_algo(g.GRD_CC, policy=pol, **best.params())
+    ctx_c.set_policy(model)
     part = Up.graph.partition_edge_balanced(best.num_memory) if best.num_memory > 1 else None
     ctx_p = g.Context(Up.graph, part, best.num_memory, local)
     ctx_p.set_algo(g.GRD_PR_PULL, max_rounds=20, tolerance=0.0)
@@ -118,7 +126,8 @@ def bench_batch(g, args, local) -> dict:
     c1.close()
     U = B.Union([G] * len(sources))
     c2 = g.Context(U.graph, None, 1, local)
-    c2.set_algo(g.GRD_SSSP_W)
+    c2.set_algo(g.GRD_SSSP_W, policy=pol)
+    c2.set_policy(model)
     srcs = U.bases + sources
     c2.init_sources(srcs)
     c2.run()
@@ -136,7 +145,10 @@ def bench_batch(g, args, local) -> dict:
     total_plain, total_batched = plain_s + plain2, batched_s + batched2
     return {"part1_graphs": part1, "part2_sssp_sources": part2,
             "end_to_end_speedup": total_plain / total_batched,
-            "note": "batched and plain both use the fixed per-round heuristic; timings exclude layout build"}
+            "policy": "learned" if model is not None else "fixed",
+            "note": "plain: one ctx per graph (per source) with the fixed per-round rule; batched: one union per "
+                    "algorithm, autotuned schedule and the learned round policy (CC, SSSP; PageRank is Jacobi "
+                    "pull); timings exclude layout build"}
 
 
 def bench_pagerank(g, args, local, hbm_peak, barrier, ws) -> dict:
@@ -262,6 +274,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def load_policy_model():
+    """The shipped learned round-policy model, or None."""
+    from grudon_gb300 import policy as P
+    return P.load_model() if P.MODEL_FILE.exists() else None
+
+
 def make_graphs(scale: int, threads: int):
     import grudon_gb300 as g
     a, b, c = RMAT_ABC
@@ -328,7 +346,8 @@ def run_reference(args):
 def workload_config(scale, seed, G_cc, G_ss) -> dict:
     return {
         "workload": f"CC (symmetrised) + weighted SSSP (w in [1,255], source 0) to convergence, RMAT-{scale} "
-                    f"ef{EF} a/b/c/d .57/.19/.19/.05, 1 compute + {NUM_MEMORY} memory partitions, bitvector sync",
+                    f"ef{EF} a/b/c/d .57/.19/.19/.05, 1 compute + {NUM_MEMORY} memory partitions, bitvector or list "
+                    f"sync and push or pull chosen per round",
         "scale": scale, "edge_factor": EF, "seed": seed, "num_vertices": G_cc.num_vertices,
         "E_cc_symmetrised": G_cc.num_edges, "E_sssp": G_ss.num_edges,
         "partitions": f"1C+{NUM_MEMORY}M edge-balanced contiguous",
@@ -355,8 +374,20 @@ def main():
     p_ss = G_ss.partition_edge_balanced(NUM_MEMORY)
     ctx_cc = g.Context(G_cc, p_cc, num_memory=NUM_MEMORY, device=local)
     ctx_ss = g.Context(G_ss, p_ss, num_memory=NUM_MEMORY, device=local)
-    ctx_cc.set_algo(g.GRD_CC)
-    ctx_ss.set_algo(g.GRD_SSSP_W)
+    model = load_policy_model()
+
+    def set_policy(policy):
+        for c, a in ((ctx_cc, g.GRD_CC), (ctx_ss, g.GRD_SSSP_W)):
+            c.set_algo(a, policy=policy)
+            c.set_policy(model if policy == g.GRD_POLICY_LEARNED else None)
+
+    # the product configuration: the shipped learned round policy when its
+    # model file is present, else the fixed threshold rule.  The plain method
+    # (fixed rule, push only: no in-edge view yet) is timed first.
+    policy = g.GRD_POLICY_LEARNED if model is not None else g.GRD_POLICY_FIXED
+    if args.policy == "fixed" or (args.policy == "learned" and model is None):
+        policy = g.GRD_POLICY_FIXED
+    set_policy(g.GRD_POLICY_FIXED)
     E = G_cc.num_edges + G_ss.num_edges
     slots = {id(c): sum(sum(c.layout_info(p)[:2]) for p in range(NUM_MEMORY)) for c in (ctx_cc, ctx_ss)}
 
@@ -372,33 +403,67 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        step()
+    if args.kernel_run:
+        set_policy(policy)
+        for _ in range(args.warmup + args.steps):
+            sts = step(host_loop=True)
+        barrier()
+        if rank == 0:
+            print(json.dumps({"kernel_run": True, "workload": workload_config(args.scale, seed, G_cc, G_ss)["workload"],
+                              "policy": "learned" if policy == g.GRD_POLICY_LEARNED else "fixed",
+                              "rounds": [st["rounds"] for st in sts],
+                              "launches_per_step": sum(st["kernel_launches"] for st in sts)}), flush=True)
+        ctx_cc.close()
+        ctx_ss.close()
+        return
 
-    # Timed region: every step runs both algorithms to convergence, each as
-    # one device-driven CUDA-graph launch.
     s_cc = torch.cuda.ExternalStream(ctx_cc.stream())
     s_ss = torch.cuda.ExternalStream(ctx_ss.stream())
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(local)
-    clocks.start()
-    barrier()
-    ev0.record(s_cc)
-    agg = {"edges": 0, "launches": 0, "rounds": [], "device_loop": []}
-    for _ in range(args.steps):
-        for st in step():
-            agg["edges"] += st["edges_scanned"]
-            agg["launches"] += st["kernel_launches"]
-            agg["rounds"].append(st["rounds"])
-            agg["device_loop"].append(st["device_loop"])
-    ev1.record(s_ss)
-    barrier()
-    clk = clocks.stop()
     from grudon_gb300.replicas import job_throughput
     dev = torch.device("cuda", local) if ws > 1 else None
-    thr, secs, _ = job_throughput(args.steps * E, ev0.elapsed_time(ev1) / 1e3, dev)
-    dt_ms = secs * 1e3
-    value = thr / 1e9
+
+    def timed():
+        """W warm-up steps, then K timed steps: every step runs both
+        algorithms to convergence, each as one device-driven CUDA-graph
+        launch; CUDA events on the ctx streams."""
+        for _ in range(args.warmup):
+            step()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        ev0.record(s_cc)
+        agg = {"edges": 0, "launches": 0, "rounds": [], "device_loop": [], "push_rounds": 0, "pull_rounds": 0}
+        for _ in range(args.steps):
+            for st in step():
+                agg["edges"] += st["edges_scanned"]
+                agg["launches"] += st["kernel_launches"]
+                agg["rounds"].append(st["rounds"])
+                agg["device_loop"].append(st["device_loop"])
+                agg["push_rounds"] += st["push_rounds"]
+                agg["pull_rounds"] += st["pull_rounds"]
+        ev1.record(s_ss)
+        barrier()
+        thr, secs, _ = job_throughput(args.steps * E, ev0.elapsed_time(ev1) / 1e3, dev)
+        return thr / 1e9, secs * 1e3, agg
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    plain = None
+    if policy == g.GRD_POLICY_LEARNED:
+        pv, pms, pagg = timed()
+        plain = {"value": pv, "ms_per_step": pms / args.steps, "rounds_per_step": pagg["rounds"][:2],
+                 "push_rounds_per_step": pagg["push_rounds"] / args.steps,
+                 "pull_rounds_per_step": pagg["pull_rounds"] / args.steps, "gpu_launches": pagg["launches"]}
+        set_policy(policy)
+    value, dt_ms, agg = timed()
+    clk = clocks.stop()
+    results_identical = True
+    if plain is not None:  # the learned schedule leaves every result bit-identical
+        outs = []
+        for pol in (g.GRD_POLICY_FIXED, policy):
+            set_policy(pol)
+            outs.append([(c.init(), c.run(), c.read_props())[2] for c in (ctx_cc, ctx_ss)])
+        results_identical = all(bool((a == b).all()) for a, b in zip(*outs))
+        set_policy(policy)
 
     # Stage timing for the roofline: the same steps driven from the host with
     # CUDA events around every stage of every round (same kernels, same
@@ -467,6 +532,13 @@ def main():
             "e2e": e2e, "gpu_launches": agg["launches"], "roofline": roofline, "clocks": clk,
             "rounds_per_step": agg["rounds"][:2], "device_loop": all(agg["device_loop"]),
             "edges_scanned_gteps": ws * agg["edges"] / (dt_ms / 1e3) / 1e9,
+            "policy": {"kind": "learned" if policy == g.GRD_POLICY_LEARNED else "fixed",
+                       "model": "grudon_gb300/policy_model.json" if model is not None else None,
+                       "push_rounds_per_step": agg["push_rounds"] / args.steps,
+                       "pull_rounds_per_step": agg["pull_rounds"] / args.steps,
+                       "plain_fixed_rule": plain,
+                       "speedup_vs_fixed": (value / plain["value"]) if plain else None,
+                       "results_bit_identical": results_identical},
         }
         if ws == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(G_cc, G_ss, p_cc, p_ss)

@@ -115,6 +115,8 @@ SIGNATURES = {
     "grd_policy_predict": (C.c_int, [C.POINTER(grd_policy_model), f32p, C.c_size_t, C.c_uint32, C.c_int, f32p,
                                      C.POINTER(C.c_int32)]),
     "grd_policy_error": (C.c_char_p, []),
+    "grd_policy_load": (C.c_int, [C.c_char_p, C.POINTER(grd_policy_model)]),
+    "grd_policy_save": (C.c_int, [C.c_char_p, C.POINTER(grd_policy_model)]),
     "grd_run": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(grd_stats)]),
     "grd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(grd_stats)]),
     "grd_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),

@@ -27,7 +27,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wa
              "-Wno-unused-function"]
 
 CU_SOURCES = ["abi.cu", "pull.cu", "graph_run.cu", "noalloc.cu", "policy.cu"]
-CPP_SOURCES = ["graph_tools.cpp", "layout.cpp"]
+CPP_SOURCES = ["graph_tools.cpp", "layout.cpp", "policy_io.cpp"]
 
 
 def _nvcc() -> str:

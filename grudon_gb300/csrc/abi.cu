@@ -137,16 +137,7 @@ int grd_upload_layout(grd_ctx* ctx) {
   for (uint32_t p = 0; p < L.M; ++p) T[p] = L.T(p);
   TRY(upload(ctx, (uint32_t*)g.part_T, T));
   TRY(upload(ctx, (uint32_t*)g.part_owned, L.n_owned));
-  {
-    // gid -> owned global slot (the first n_owned slots of each partition).
-    std::vector<uint32_t> own(L.V);
-    for (uint32_t p = 0; p < L.M; ++p)
-      for (uint32_t k = 0; k < L.n_owned[p]; ++k) own[L.slot_gid[L.slot_base[p] + k]] = L.slot_base[p] + k;
-    CK(cudaMemcpyAsync(ctx->st.own_slot, own.data(), sizeof(uint32_t) * own.size(), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));  // `own` is a temporary
-    ctx->upload_bytes += sizeof(uint32_t) * own.size();
-  }
+  TRY(upload(ctx, ctx->st.own_slot, ctx->own_slot_host));
   if (ctx->in_edges_alloc) {
     TRY(upload(ctx, (uint32_t*)g.in_off, L.in_off));
     TRY(upload(ctx, (uint32_t*)g.in_src, L.in_src));
@@ -164,6 +155,7 @@ int grd_ensure_in_edges(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, (uint32_t**)&ctx->g.in_src, std::max<size_t>(L.E, 4)));
   if (L.weighted) TRY(dev_alloc(ctx, (uint32_t**)&ctx->g.in_wgt, std::max<size_t>(L.E, 4)));
   ctx->in_edges_alloc = true;
+  grd_pin_host(ctx, {&ctx->L.in_off, &ctx->L.in_src, &ctx->L.in_wgt});
   TRY(upload(ctx, (uint32_t*)ctx->g.in_off, L.in_off));
   TRY(upload(ctx, (uint32_t*)ctx->g.in_src, L.in_src));
   if (L.weighted) TRY(upload(ctx, (uint32_t*)ctx->g.in_wgt, L.in_wgt));
@@ -274,6 +266,11 @@ static int host_loop_mode(grd_ctx* ctx, int* mode) {
     *mode = grd_choose_round_mode(ctx);
     return GRD_OK;
   }
+  const PolicyArgs a = grd_policy_args(ctx);
+  if (policy_tiny(ctx->last_frontier, ctx->last_fedges, policy_allowed(a.direction, a.format, a.has_in != 0))) {
+    *mode = RM_PUSH_LIST;  // k_policy decides the same without inference
+    return GRD_OK;
+  }
   k_policy<false><<<1, P_HID, 0, ctx->stream>>>(ctx->g, ctx->st, 0, grd_policy_args(ctx), m);
   CK_LAUNCH();
   CK(cudaMemcpyAsync(ctx->h_seed + 7, ctx->st.counters + C_MODE, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
@@ -307,6 +304,7 @@ uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
 
 // Kernels of a whole round in each mode (edge-map + syncs + update).
 uint32_t grd_round_launches(const grd_ctx* ctx, int mode) {
+  if (mode == RM_PUSH_TINY) return 1;
   const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
   const uint32_t groups = ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1;
   const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (3 /*fwd*/ + 2 + groups /*bwd*/ + 1 /*update*/);
@@ -433,6 +431,20 @@ int grd_enqueue_bwd_update_list(grd_ctx* ctx) {
 
 // One whole round in a given mode (host loop and loop-graph branches).
 int grd_enqueue_round(grd_ctx* ctx, int mode) {
+  if (mode == RM_PUSH_TINY) {  // the whole round counts as edge-map time
+    grd_prof_mark(ctx, 1);
+    TRY(dispatch(ctx->algo, [&](auto a) -> int {
+      constexpr int A = decltype(a)::value;
+      k_round_tiny<A><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
+                                                             ctx->params.damping);
+      CK_LAUNCH();
+      return GRD_OK;
+    }));
+    grd_prof_mark(ctx, 2);
+    grd_prof_mark(ctx, 3);
+    ctx->stats.kernel_launches += 1;
+    return GRD_OK;
+  }
   const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
   const uint64_t launches = ctx->stats.kernel_launches;
   if (list) {
@@ -790,11 +802,12 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
                      un_in = ctx->h_counters[C_UNVISITED];
       int mode;
       TRY(host_loop_mode(ctx, &mode));
+      const int branch = rm_branch(mode, ctx->last_frontier, ctx->last_fedges);
       grd_prof_mark(ctx, 0);
       if (ctx->profiling)
-        TRY(grd_round_graph_launch(ctx, mode));
+        TRY(grd_round_graph_launch(ctx, branch));
       else
-        TRY(grd_enqueue_round(ctx, mode));
+        TRY(grd_enqueue_round(ctx, branch));
       grd_prof_mark(ctx, 4);
       ctx->last_mode = mode;
       if (rm_is_pull(mode)) {
@@ -1005,16 +1018,25 @@ int grd_ctx_init_device(grd_ctx* ctx) {
   std::memset(ctx->h_counters, 0, sizeof(unsigned long long) * (NUM_COUNTERS + 8));
   ctx->h_seed = ctx->h_counters + NUM_COUNTERS;
   TRY(alloc_and_upload(ctx));
-  // Pin the large host layout arrays so grd_upload copies run at full
-  // host->device bandwidth; pageable copies still work if pinning fails.
-  for (auto* v : {&ctx->L.col, &ctx->L.wgt, &ctx->L.row_off, &ctx->L.slot_gid}) {
+  // gid -> owned global slot (the first n_owned slots of each partition).
+  const Layout& L = ctx->L;
+  ctx->own_slot_host.assign(L.V, 0);
+  for (uint32_t p = 0; p < L.M; ++p)
+    for (uint32_t k = 0; k < L.n_owned[p]; ++k) ctx->own_slot_host[L.slot_gid[L.slot_base[p] + k]] = L.slot_base[p] + k;
+  grd_pin_host(ctx, {&ctx->L.col, &ctx->L.wgt, &ctx->L.row_off, &ctx->L.slot_gid, &ctx->own_slot_host});
+  return grd_upload_layout(ctx);
+}
+
+// Pins large host layout arrays so grd_upload copies run at full
+// host->device bandwidth; pageable copies still work if pinning fails.
+void grd_pin_host(grd_ctx* ctx, std::initializer_list<std::vector<uint32_t>*> arrays) {
+  for (auto* v : arrays) {
     if (v->size() * sizeof(uint32_t) < (1u << 20)) continue;
     if (cudaHostRegister(v->data(), v->size() * sizeof(uint32_t), cudaHostRegisterDefault) == cudaSuccess)
       ctx->host_registered.push_back(v->data());
     else
       (void)cudaGetLastError();
   }
-  return grd_upload_layout(ctx);
 }
 
 int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks) {

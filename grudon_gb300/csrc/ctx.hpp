@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <initializer_list>
 #include <string>
 #include <vector>
 
@@ -43,7 +44,7 @@ struct grd_ctx {
   int last_mode = -1;          // edge-map mode of the round in flight (host loop)
   cudaGraph_t run_graph = nullptr;     // device-driven round loop (graph_run.cu)
   cudaGraphExec_t run_exec = nullptr;
-  cudaGraphExec_t round_exec[4] = {};  // one round per mode (profiled host loop)
+  cudaGraphExec_t round_exec[5] = {};  // one round per branch (profiled host loop)
   bool graph_failed = false;           // building it failed here: host loop
   std::string graph_error;
   uint32_t* agg_buf = nullptr; // staging of grd_aggregate_values (gids, values)
@@ -51,6 +52,7 @@ struct grd_ctx {
   bool profiling = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<void*> host_registered;  // layout arrays pinned for H2D uploads
+  std::vector<uint32_t> own_slot_host;  // gid -> owned global slot (uploaded)
   grd_policy_model* policy_dev = nullptr;  // learned round policy (device copy)
   bool has_policy = false;
 };
@@ -81,6 +83,7 @@ struct grd_ctx {
   } while (0)
 
 int grd_ctx_init_device(grd_ctx* ctx);
+void grd_pin_host(grd_ctx* ctx, std::initializer_list<std::vector<uint32_t>*> arrays);
 int grd_dev_alloc_bytes(grd_ctx* ctx, void** p, size_t bytes);
 void grd_prof_mark(grd_ctx* ctx, int i);
 void grd_prof_collect(grd_ctx* ctx);
@@ -98,8 +101,17 @@ enum RoundMode {
   RM_PUSH_LIST = GRD_ROUND_PUSH_LIST,
   RM_PULL_BITVEC = GRD_ROUND_PULL_BITVEC,
   RM_PULL_LIST = GRD_ROUND_PULL_LIST,
-  NUM_ROUND_MODES = 4
+  NUM_ROUND_MODES = 4,
+  // push + list for a frontier small enough for one CTA (k_round_tiny); an
+  // implementation of RM_PUSH_LIST, chosen by size, not by the policy
+  RM_PUSH_TINY = 4,
+  NUM_BRANCHES = 5
 };
+// The branch that runs a round the policy gave `mode`.
+__host__ __device__ inline int rm_branch(int mode, unsigned long long frontier, unsigned long long fedges) {
+  return (mode == RM_PUSH_LIST && frontier <= grd::K_TINY_ACTIVE && fedges <= grd::K_TINY_EDGES) ? (int)RM_PUSH_TINY
+                                                                                                  : mode;
+}
 __host__ __device__ inline bool rm_is_pull(int m) { return m == RM_PULL_BITVEC || m == RM_PULL_LIST; }
 int grd_choose_round_mode(const grd_ctx* ctx);
 int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode);

@@ -92,18 +92,18 @@ int build(grd_ctx* ctx) {
   }
   CK(cudaGraphConditionalHandleCreate(&sw, loop_body, 0, 0));
   PolicyArgs pa = grd_policy_args(ctx);
-  for (int m = 0; m < NUM_ROUND_MODES; ++m) pa.launches[m] = 2 /*policy, round end*/ + grd_round_launches(ctx, m);
+  for (int m = 0; m < NUM_BRANCHES; ++m) pa.launches[m] = 2 /*policy, round end*/ + grd_round_launches(ctx, m);
 
   int rc = capture_into(ctx, loop_body);
   if (rc != GRD_OK) return rc;
-  cudaGraph_t branches[NUM_ROUND_MODES] = {};
+  cudaGraph_t branches[NUM_BRANCHES] = {};
   k_policy<true><<<1, P_HID, 0, ctx->stream>>>(ctx->g, ctx->st, sw, pa, grd_policy_model_dev(ctx));
-  rc = add_conditional(ctx, ctx->stream, sw, cudaGraphCondTypeSwitch, NUM_ROUND_MODES, branches);
+  rc = add_conditional(ctx, ctx->stream, sw, cudaGraphCondTypeSwitch, NUM_BRANCHES, branches);
   if (rc == GRD_OK) k_round_end<<<1, 32, 0, ctx->stream>>>(ctx->st, wh, ctx->params.max_rounds);
   const int rc_end = end_capture(ctx, loop_body);
   if (rc != GRD_OK) return rc;
   if (rc_end != GRD_OK) return rc_end;
-  for (int m = 0; m < NUM_ROUND_MODES; ++m) {
+  for (int m = 0; m < NUM_BRANCHES; ++m) {
     if (rm_is_pull(m) && !ctx->in_edges_alloc) continue;  // never selected: empty branch
     TRY(capture_into(ctx, branches[m]));
     rc = grd_enqueue_round(ctx, m);

@@ -182,6 +182,39 @@ __device__ __forceinline__ void mark_listed(uint32_t* bm, uint32_t i, uint32_t* 
   list_append(list, counter, i);
 }
 
+// Block-aggregated append of up to N flagged values per thread; every
+// thread of the block calls it (block-uniform control flow).  One counter
+// update per block and call.
+template <int N>
+__device__ __forceinline__ void block_append_n(uint32_t* list, uint32_t* counter, const bool (&flag)[N],
+                                               const uint32_t (&value)[N]) {
+  __shared__ uint32_t s_ws[32];
+  __shared__ uint32_t s_b;
+  const uint32_t w = threadIdx.x >> 5, lane = lane_id();
+  uint32_t cnt = 0;
+#pragma unroll
+  for (int k = 0; k < N; ++k) cnt += flag[k] ? 1u : 0u;
+  const uint32_t incl = warp_incl_scan(cnt);
+  if (lane == 31) s_ws[w] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t nw = (blockDim.x + 31) >> 5;
+    uint32_t t = 0;
+    for (uint32_t k = 0; k < nw; ++k) {
+      const uint32_t c = s_ws[k];
+      s_ws[k] = t;
+      t += c;
+    }
+    s_b = t ? atomicAdd(counter, t) : 0u;
+  }
+  __syncthreads();
+  uint32_t pos = s_b + s_ws[w] + incl - cnt;
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+    if (flag[k]) list[pos++] = value[k];
+  __syncthreads();
+}
+
 // Sets bit i of bm; true for the thread that set it.
 __device__ __forceinline__ bool claim_bit(uint32_t* bm, uint32_t i) {
   const uint32_t bit = 1u << (i & 31);
@@ -829,20 +862,23 @@ static __global__ void __launch_bounds__(256) k_deg_down(DevGraph g, DevState st
 // One warp per 256-edge chunk.  The warp stages a window of LBS_WIN
 // consecutive actives (their DP, row start and source value) in shared memory
 // with 8 independent coalesced loads per lane — one window covers the whole
-// chunk unless more than LBS_WIN actives fall inside it — then each lane
-// finds the source of each of its 8 edges by an 8-step binary search in
-// shared memory, so lanes read consecutive edge slots.  All 8 edges of a lane
-// are loaded (index, weight, current value) before any update is issued,
-// keeping 8 independent memory chains in flight per lane.
+// chunk unless more than LBS_WIN actives fall inside it.  The source of each
+// of the window's edge positions comes from a mark-and-scan in shared memory
+// (every active marks the position where its row starts, then a running max
+// over the 256 positions), so an edge costs one shared load to find its row
+// and lanes read consecutive edge slots.  All 8 edges of a lane are loaded
+// (index, weight, current value) before any update is issued, keeping 8
+// independent memory chains in flight per lane.
 constexpr uint32_t LBS_WIN = 256;
 
 template <int A, bool kDense>
-__global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
+__global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
   constexpr int B = LBS_CHUNK / 32;
   constexpr int SW = LBS_WIN / 32;
-  __shared__ uint32_t s_dp[8][LBS_WIN + 1];
+  __shared__ uint32_t s_dp[8][LBS_WIN];
   __shared__ uint32_t s_rb[8][LBS_WIN];
   __shared__ uint32_t s_sv[8][LBS_WIN];
+  __shared__ uint32_t s_src[8][LBS_CHUNK];
   const uint32_t K = (uint32_t)__ldcg(&st.counters[C_ACTIVE]);
   const uint32_t m = (uint32_t)__ldcg(&st.counters[C_MEDGES]);
   const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
@@ -851,6 +887,7 @@ __global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
   uint32_t* dp = s_dp[w];
   uint32_t* rbs = s_rb[w];
   uint32_t* svs = s_sv[w];
+  uint32_t* srcs = s_src[w];
   for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + w; c < nchunks; c += nwarps) {
     uint32_t e = c * LBS_CHUNK;
     const uint32_t e_end = min(m, e + LBS_CHUNK);
@@ -865,15 +902,48 @@ __global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
         v[k] = idx < K ? st.SV[idx] : 0u;
       }
       const uint32_t tail = (lane == 0) ? (i0 + LBS_WIN < K ? st.DP[i0 + LBS_WIN] : m) : 0u;
+      const uint32_t wend = min(e_end, __shfl_sync(FULL, tail, 0));
+      static_assert(LBS_CHUNK == 8 * 32, "each lane owns 8 consecutive edge positions");
+#pragma unroll
+      for (int q = 0; q < 8; ++q) srcs[8 * lane + q] = 0;
 #pragma unroll
       for (int k = 0; k < SW; ++k) {
         dp[k * 32 + lane] = a[k];
         rbs[k * 32 + lane] = b[k];
         svs[k * 32 + lane] = source_value<A>(v[k]);
       }
-      if (lane == 0) dp[LBS_WIN] = tail;
       __syncwarp();
-      const uint32_t wend = min(e_end, dp[LBS_WIN]);
+      // mark: the row of window active j starts at position dp[j] - e (the
+      // first active's row may start before the window: position 0).  Only
+      // rows with edges mark, so no two actives share a position.
+      const uint32_t tailv = __shfl_sync(FULL, tail, 0);
+#pragma unroll
+      for (int k = 0; k < SW; ++k) {
+        const uint32_t j = k * 32 + lane;
+        const uint32_t next = j + 1 < LBS_WIN ? dp[j + 1] : tailv;
+        if (a[k] < wend && next > a[k]) srcs[(a[k] > e ? a[k] : e) - e] = j;
+      }
+      __syncwarp();
+      // scan: running max over the positions (lane-local 8, then the warp)
+      {
+        uint32_t loc[8], run = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          run = max(run, srcs[8 * lane + q]);
+          loc[q] = run;
+        }
+        uint32_t inc = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t n = __shfl_up_sync(FULL, inc, o);
+          if (lane >= (uint32_t)o) inc = max(inc, n);
+        }
+        uint32_t ex = __shfl_up_sync(FULL, inc, 1);
+        if (lane == 0) ex = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) srcs[8 * lane + q] = max(ex, loc[q]);
+      }
+      __syncwarp();
       uint32_t dst[B], cand[B], cur[B];
 #pragma unroll
       for (int k = 0; k < B; ++k) {
@@ -881,13 +951,10 @@ __global__ void __launch_bounds__(256) k_push_lbs(DevGraph g, DevState st) {
         dst[k] = 0xFFFFFFFFu;
         cand[k] = 0;
         if (eid < wend) {
-          uint32_t lo = 0;
-#pragma unroll
-          for (uint32_t step = LBS_WIN / 2; step; step >>= 1)
-            if (dp[lo + step] <= eid) lo += step;
-          const uint32_t ed = rbs[lo] + (eid - dp[lo]);
+          const uint32_t j = srcs[k * 32 + lane];
+          const uint32_t ed = rbs[j] + (eid - dp[j]);
           dst[k] = __ldg(&g.col[ed]);
-          cand[k] = svs[lo];
+          cand[k] = svs[j];
           if (A == A_SSSP_W) cand[k] = relax_cand<A>(cand[k], __ldg(&g.wgt[ed]));
         }
       }
@@ -1311,6 +1378,160 @@ __global__ void __launch_bounds__(256) k_update_list(DevGraph g, DevState st, do
       st.counters[C_DONE] = 0;
     }
   }
+}
+
+// ------------------------------------------------------------ tiny round --
+// A whole push + list round in one CTA of 1024 threads, for frontiers of at
+// most K_TINY_ACTIVE vertices and K_TINY_EDGES out-edges (every row of such a
+// frontier, hub or not, runs here).  The phases are those of k_fwd_list,
+// the push edge-map, k_bwd_list and k_update_list, separated by block
+// barriers instead of kernel boundaries, so a small round costs one launch.
+// Values, dirty sets, lists and statistics equal the multi-kernel round's.
+constexpr uint32_t K_TINY_ACTIVE = 2048;
+constexpr uint32_t K_TINY_EDGES = 16384;
+constexpr int K_TINY_THREADS = 1024;
+
+template <int A>
+__global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevState st, double tol, double damping) {
+  __shared__ uint32_t s_dp[K_TINY_ACTIVE + 1];
+  __shared__ uint32_t s_rb[K_TINY_ACTIVE];
+  __shared__ uint32_t s_sv[K_TINY_ACTIVE];
+  __shared__ uint32_t s_carry;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t K = __ldcg(&st.lc[L_FL]);
+  if (K > K_TINY_ACTIVE) {  // never chosen for such a frontier; refuse rather than drop actives
+    if (tid == 0) atomicCAS(&st.counters[C_ERR], 0ull, 3ull);
+    return;
+  }
+  // forward sync + per-round counters
+  if (tid == 0) {
+    st.counters[C_ACTIVE] = K;
+    st.counters[C_BYTES] += g.bv_bytes + 4ull * K;
+    st.counters[C_REFBYTES] += g.bv_refbytes + 4ull * K;
+    reset_round_counters(st);
+    st.lc[L_DL] = 0;
+    s_carry = 0;
+  }
+  __syncthreads();
+  // degree prefix of the actives (block scan, 1024 at a time)
+  for (uint32_t b = 0; b < K; b += K_TINY_THREADS) {
+    const uint32_t j = b + tid;
+    uint32_t d = 0;
+    if (j < K) {
+      const uint32_t gid = st.FL[j];
+      const uint32_t s = st.own_slot[gid];
+      const uint32_t v = st.prop[gid];
+      st.AL[j] = s;
+      st.mprop[s] = v;
+      const uint32_t r0 = __ldg(&g.row_off[s]);
+      d = __ldg(&g.row_off[s + 1]) - r0;
+      s_rb[j] = r0;
+      s_sv[j] = source_value<A>(v);
+    }
+    const uint32_t incl = warp_incl_scan(d);
+    __shared__ uint32_t s_w[32];
+    if (lane_id() == 31) s_w[tid >> 5] = incl;
+    __syncthreads();
+    if (tid < 32) {
+      const uint32_t x = s_w[tid];
+      s_w[tid] = warp_incl_scan(x) - x;
+    }
+    __syncthreads();
+    const uint32_t carry = s_carry;
+    if (j < K) s_dp[j] = carry + s_w[tid >> 5] + incl - d;
+    __syncthreads();
+    if (tid == K_TINY_THREADS - 1) s_carry = carry + s_w[tid >> 5] + incl;
+    __syncthreads();
+  }
+  const uint32_t m = s_carry;  // frontier out-edges
+  if (tid == 0) {
+    s_dp[K] = m;
+    st.counters[C_EDGES] += m;
+  }
+  __syncthreads();
+  // push edge-map over the m edges, 4 per thread per step
+  constexpr int N = 4;
+  for (uint32_t e0 = 0; e0 < m; e0 += K_TINY_THREADS * N) {
+    uint32_t dst[N], cand[N], cur[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const uint32_t e = e0 + k * K_TINY_THREADS + tid;
+      dst[k] = 0xFFFFFFFFu;
+      cand[k] = 0;
+      if (e < m) {
+        uint32_t lo = 0, hi = K;  // last i with s_dp[i] <= e
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (s_dp[mid] <= e) lo = mid; else hi = mid;
+        }
+        const uint32_t ed = s_rb[lo] + (e - s_dp[lo]);
+        dst[k] = __ldg(&g.col[ed]);
+        cand[k] = relax_cand<A>(s_sv[lo], A == A_SSSP_W ? __ldg(&g.wgt[ed]) : 0u);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek<A>(st, dst[k]) : 0u;
+    bool nd[N];
+    relax_sparse<A, N>(st, dst, cand, cur, nd);
+    block_append_n<N>(st.DL, st.lc + L_DL, nd, dst);
+  }
+  __syncthreads();
+  // backward sync: retire the old frontier, send and aggregate the dirty slots
+  const uint32_t n = __ldcg(&st.lc[L_DL]);
+  if (tid == 0) {
+    st.counters[C_BYTES] += g.bv_bytes + 4ull * n;
+    st.counters[C_REFBYTES] += g.bv_refbytes + 4ull * n;
+  }
+  for (uint32_t j = tid; j < K; j += K_TINY_THREADS) {
+    const uint32_t gid = st.FL[j];
+    atomicAnd(&st.F[gid >> 5], ~(1u << (gid & 31)));
+  }
+  for (uint32_t b = 0; b < n; b += K_TINY_THREADS) {
+    const uint32_t j = b + tid;
+    bool listed = false;
+    uint32_t gid = 0;
+    if (j < n) {
+      const uint32_t s = st.DL[j];
+      const uint32_t v = st.mupd[s];
+      gid = __ldg(&g.slot_gid[s]);
+      retire_update<A>(st, s, v);
+      st.BV[j] = v;
+      atomicAnd(&st.MD[s >> 5], ~(1u << (s & 31)));
+      if (A == A_PR_DELTA) {
+        atomicAdd(reinterpret_cast<float*>(st.upd) + gid, __uint_as_float(v));
+        listed = claim_bit(st.UD, gid);
+      } else if (v < __ldcg(&st.upd[gid])) {
+        if (v < atomicMin(&st.upd[gid], v)) listed = claim_bit(st.UD, gid);
+      }
+    }
+    block_append(st.UL, st.lc + L_UL, listed, gid);
+  }
+  if (tid == 0) st.lc[L_FL] = 0;
+  __syncthreads();
+  // update over the updated-gid list
+  const uint32_t nu = __ldcg(&st.lc[L_UL]);
+  uint32_t fcount = 0, fedges = 0, fmax = 0, visited = 0;
+  for (uint32_t b = 0; b < nu; b += K_TINY_THREADS) {
+    const uint32_t j = b + tid;
+    bool nf = false;
+    uint32_t v = 0;
+    if (j < nu) {
+      v = st.UL[j];
+      atomicAnd(&st.UD[v >> 5], ~(1u << (v & 31)));
+      nf = update_one<A>(g, st, v, tol, damping, visited);
+      if (nf) {
+        atomicOr(&st.F[v >> 5], 1u << (v & 31));
+        const uint32_t d = g.outdeg[v];
+        ++fcount;
+        fedges += d;
+        fmax = max(fmax, d);
+      }
+    }
+    block_append(st.FL, st.lc + L_FL, nf, v);
+  }
+  flush_frontier_shape(st, fcount, fedges, fmax, visited);
+  __syncthreads();
+  if (tid == 0) st.lc[L_UL] = 0;
 }
 
 // Update over the whole dirty bitmap (bitvector rounds): rebuilds the

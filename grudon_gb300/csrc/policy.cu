@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(P_HID) k_mlp_grad(const grd_policy_model* m, c
   for (uint32_t s = blockIdx.x; s < n; s += gridDim.x) {
     if (j < P_IN) s_x[j] = (x[(size_t)s * P_IN + j] - m->mean[j]) * m->scale[j];
     __syncthreads();
-    // forward (same arithmetic as policy_mlp_block)
+    // forward (same arithmetic as mlp_eval)
     float a = m->b1[j];
 #pragma unroll
     for (int i = 0; i < P_IN; ++i) a = fmaf(h2f(m->w1[j * P_IN + i]), s_x[i], a);
@@ -152,11 +152,13 @@ __global__ void k_adam(float* p, const float* g, float* mo, float* ve, float lr,
 __global__ void __launch_bounds__(P_HID) k_mlp_predict(const grd_policy_model* m, const float* x, uint32_t n,
                                                        uint32_t allowed, float* out, int32_t* choice) {
   __shared__ float s_x[P_IN], s_h1[P_HID], s_h2[P_HID], s_out[P_OUT];
+  MlpRegs r;
+  mlp_load(m, r);
   for (uint32_t s = blockIdx.x; s < n; s += gridDim.x) {
     if (threadIdx.x < P_IN) s_x[threadIdx.x] = (x[(size_t)s * P_IN + threadIdx.x] - m->mean[threadIdx.x]) *
                                                 m->scale[threadIdx.x];
     __syncthreads();
-    policy_mlp_block(m, s_x, s_h1, s_h2, s_out);
+    mlp_eval(r, s_x, s_h1, s_h2, s_out);
     if (threadIdx.x == 0) {
       int best = -1;
       for (int o = 0; o < P_OUT; ++o) {

@@ -7,6 +7,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include "../../include/grudon_gpu.h"
 #include "kernels.cuh"
 
@@ -18,22 +20,27 @@ static_assert(P_OUT == 4, "one output per round mode");
 struct PolicyArgs {
   int direction, format, has_in;
   uint32_t dense_div, pull_div;
-  uint32_t launches[4];     // kernels of one round per mode (device loop stats)
+  uint32_t launches[5];     // kernels of one round per branch (device loop stats)
   unsigned long long edges; // E
   uint32_t round;           // round index (host loop; the device loop counts)
 };
 
 // Raw policy features (grd_policy_features computes the same on the host).
+// Sizes enter as log2 fractions of the graph (frontier of V, its edges and
+// the unvisited edges of E, its largest degree of V) plus the graph's own
+// log2 size and degree, so one model covers graphs of any scale.
 __host__ __device__ inline void policy_features(double frontier, double fedges, double unvisited, double maxdeg,
                                                 double round, double V, double E, float* f) {
-  f[0] = log2f((float)(1.0 + frontier));
-  f[1] = log2f((float)(1.0 + fedges));
-  f[2] = log2f((float)(1.0 + unvisited));
+  const double v = V > 1.0 ? V : 1.0;
+  const float lv = log2f((float)v), le = log2f((float)(1.0 + E));
+  f[0] = log2f((float)(1.0 + frontier)) - lv;
+  f[1] = log2f((float)(1.0 + fedges)) - le;
+  f[2] = log2f((float)(1.0 + unvisited)) - le;
   f[3] = log2f((float)(1.0 + fedges / (frontier > 1.0 ? frontier : 1.0)));
-  f[4] = log2f((float)(1.0 + maxdeg));
+  f[4] = log2f((float)(1.0 + maxdeg)) - lv;
   f[5] = log2f((float)(1.0 + round));
-  f[6] = log2f((float)(V > 1.0 ? V : 1.0));
-  f[7] = log2f((float)(1.0 + E / (V > 1.0 ? V : 1.0)));
+  f[6] = lv;
+  f[7] = log2f((float)(1.0 + E / v));
 }
 
 // Modes the round may use: forced direction / format, and pull only with
@@ -51,26 +58,61 @@ __host__ __device__ inline uint32_t policy_allowed(int direction, int format, bo
 
 __device__ __forceinline__ float h2f(uint16_t b) { return __half2float(__ushort_as_half(b)); }
 
+// Weights of hidden unit j (thread j) and, for threads below P_OUT, of
+// output j, held in registers: every load is issued at once, so one memory
+// latency covers the whole model (the struct keeps each row 16-byte aligned).
+static_assert(offsetof(grd_policy_model, w1) % 16 == 0 && offsetof(grd_policy_model, w2) % 16 == 0 &&
+                  offsetof(grd_policy_model, w3) % 16 == 0,
+              "16-byte aligned weight rows");
+
+struct MlpRegs {
+  uint4 w1;     // 8 fp16
+  uint4 w2[8];  // 64 fp16
+  uint4 w3[8];  // 64 fp16 (threads < P_OUT)
+  float b1, b2, b3;
+};
+
+__device__ __forceinline__ void mlp_load(const grd_policy_model* m, MlpRegs& r) {
+  const int j = threadIdx.x;
+  r.w1 = __ldg(reinterpret_cast<const uint4*>(m->w1 + j * P_IN));
+  const uint4* w2 = reinterpret_cast<const uint4*>(m->w2 + j * P_HID);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) r.w2[q] = __ldg(w2 + q);
+  const uint4* w3 = reinterpret_cast<const uint4*>(m->w3 + (j < P_OUT ? j : 0) * P_HID);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) r.w3[q] = __ldg(w3 + q);
+  r.b1 = m->b1[j];
+  r.b2 = m->b2[j];
+  r.b3 = m->b3[j < P_OUT ? j : 0];
+}
+
+// acc += w[0..7] . x[0..7] as fmaf in index order.
+__device__ __forceinline__ float dot8(uint4 w, const float* x, float acc) {
+  const uint32_t u[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    acc = fmaf(h2f((uint16_t)(u[q] & 0xFFFFu)), x[2 * q], acc);
+    acc = fmaf(h2f((uint16_t)(u[q] >> 16)), x[2 * q + 1], acc);
+  }
+  return acc;
+}
+
 // MLP forward for one input by a block of exactly P_HID threads.  xs: the
 // normalised input (shared), out: P_OUT predictions (shared).  Fixed
 // summation order (fmaf chains in index order).
-__device__ __forceinline__ void policy_mlp_block(const grd_policy_model* m, const float* xs, float* h1, float* h2,
-                                                 float* out) {
+__device__ __forceinline__ void mlp_eval(const MlpRegs& r, const float* xs, float* h1, float* h2, float* out) {
   const int j = threadIdx.x;
-  float a = m->b1[j];
-#pragma unroll
-  for (int i = 0; i < P_IN; ++i) a = fmaf(h2f(m->w1[j * P_IN + i]), xs[i], a);
-  h1[j] = fmaxf(a, 0.0f);
+  h1[j] = fmaxf(dot8(r.w1, xs, r.b1), 0.0f);
   __syncthreads();
-  a = m->b2[j];
-#pragma unroll 8
-  for (int k = 0; k < P_HID; ++k) a = fmaf(h2f(m->w2[j * P_HID + k]), h1[k], a);
+  float a = r.b2;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) a = dot8(r.w2[q], h1 + 8 * q, a);
   h2[j] = fmaxf(a, 0.0f);
   __syncthreads();
   if (j < P_OUT) {
-    float o = m->b3[j];
-#pragma unroll 8
-    for (int k = 0; k < P_HID; ++k) o = fmaf(h2f(m->w3[j * P_HID + k]), h2[k], o);
+    float o = r.b3;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) o = dot8(r.w3[q], h2 + 8 * q, o);
     out[j] = o;
   }
   __syncthreads();
@@ -87,12 +129,23 @@ __device__ __forceinline__ int policy_fixed(const DevGraph& g, const PolicyArgs&
               : (list ? GRD_ROUND_PUSH_LIST : GRD_ROUND_PUSH_BITVEC);
 }
 
+// A frontier that fits one CTA runs as push + list (one kernel, k_round_tiny)
+// whatever the model would say: no other mode comes close for it, and the
+// round skips the inference.
+__host__ __device__ inline bool policy_tiny(unsigned long long f, unsigned long long fe, uint32_t allowed) {
+  return f <= K_TINY_ACTIVE && fe <= K_TINY_EDGES && ((allowed >> GRD_ROUND_PUSH_LIST) & 1u);
+}
+
 // Mode of the next round, by a block of P_HID threads (valid in thread 0).
 __device__ __forceinline__ int policy_choose(const DevGraph& g, const DevState& st, const PolicyArgs& a,
                                              const grd_policy_model* model, uint32_t round) {
   __shared__ float s_x[P_IN], s_h1[P_HID], s_h2[P_HID], s_out[P_OUT];
   const unsigned long long f = st.counters[C_FRONTIER], fe = st.counters[C_FEDGES];
   if (model == nullptr) return policy_fixed(g, a, f, fe);
+  const uint32_t allowed = policy_allowed(a.direction, a.format, a.has_in != 0);
+  if (policy_tiny(f, fe, allowed)) return GRD_ROUND_PUSH_LIST;
+  MlpRegs r;
+  mlp_load(model, r);
   if (threadIdx.x == 0) {
     float raw[P_IN];
     policy_features((double)f, (double)fe, (double)st.counters[C_UNVISITED], (double)st.counters[C_FMAXDEG],
@@ -100,8 +153,7 @@ __device__ __forceinline__ int policy_choose(const DevGraph& g, const DevState& 
     for (int i = 0; i < P_IN; ++i) s_x[i] = (raw[i] - model->mean[i]) * model->scale[i];
   }
   __syncthreads();
-  policy_mlp_block(model, s_x, s_h1, s_h2, s_out);
-  const uint32_t allowed = policy_allowed(a.direction, a.format, a.has_in != 0);
+  mlp_eval(r, s_x, s_h1, s_h2, s_out);
   int best = -1;
   for (int m = 0; m < P_OUT; ++m)
     if (((allowed >> m) & 1u) && (best < 0 || s_out[m] < s_out[best])) best = m;
@@ -125,8 +177,11 @@ static __global__ void __launch_bounds__(P_HID) k_policy(DevGraph g, DevState st
     } else {
       st.counters[C_PUSH_ROUNDS] += 1;
     }
-    st.counters[C_LAUNCHES] += a.launches[mode];
-    cudaGraphSetConditional(sw, (unsigned)mode);
+    // push + list rounds of a small frontier run as one CTA (branch 4)
+    const unsigned long long f = st.counters[C_FRONTIER], fe = st.counters[C_FEDGES];
+    const int branch = (mode == GRD_ROUND_PUSH_LIST && f <= K_TINY_ACTIVE && fe <= K_TINY_EDGES) ? 4 : mode;
+    st.counters[C_LAUNCHES] += a.launches[branch];
+    cudaGraphSetConditional(sw, (unsigned)branch);
   }
 }
 

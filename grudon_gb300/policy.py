@@ -30,6 +30,9 @@ NIN, NHID, NOUT = _ffi.GRD_POLICY_IN, _ffi.GRD_POLICY_HID, _ffi.GRD_POLICY_OUT
 FORCED = [(GRD_DIR_PUSH, GRD_FMT_BITVEC), (GRD_DIR_PUSH, GRD_FMT_LIST), (GRD_DIR_PULL, GRD_FMT_BITVEC),
           (GRD_DIR_PULL, GRD_FMT_LIST)]
 ALL_MODES = 0xF
+# A frontier this small runs push + list in one CTA without inference (the
+# device rule, K_TINY_ACTIVE / K_TINY_EDGES).
+TINY_ACTIVE, TINY_EDGES = 2048, 16384
 
 
 def _f32p(a: np.ndarray):
@@ -107,11 +110,16 @@ class RoundTable:
     x: np.ndarray            # [n, 8] raw features
     ms: np.ndarray           # [n, 4] round time per mode (NaN: not measured)
     fixed_mode: np.ndarray   # [n] mode the fixed rule chose
+    tiny: np.ndarray         # [n] the frontier fits one CTA (mode fixed: push + list)
     info: dict = field(default_factory=dict)
 
     def targets(self) -> Tuple[np.ndarray, np.ndarray]:
+        """log2 round times relative to the mean over the measured modes of
+        the same round (only the ordering of the modes matters)."""
         ok = np.isfinite(self.ms) & (self.ms > 0)
-        y = np.where(ok, np.log2(np.where(ok, self.ms, 1.0)), 0.0).astype(np.float32)
+        lg = np.where(ok, np.log2(np.where(ok, self.ms, 1.0)), 0.0)
+        mean = lg.sum(axis=1, keepdims=True) / np.maximum(ok.sum(axis=1, keepdims=True), 1)
+        y = np.where(ok, lg - mean, 0.0).astype(np.float32)
         return y, ok.astype(np.uint8)
 
 
@@ -128,7 +136,11 @@ def _profiled_run(ctx: Context, algo: int, init, reps: int, **kw) -> List[dict]:
             best = log
         else:
             if len(log) != len(best):
-                raise RuntimeError("round count changed between identical runs")
+                if algo != GRD_PR_DELTA:
+                    raise RuntimeError("round count changed between identical runs")
+                # float atomics: delta PageRank may end a round sooner or later
+                n = min(len(log), len(best))
+                best, log = best[:n], log[:n]
             for a, b in zip(best, log):
                 a["ms"] = [min(u, v) for u, v in zip(a["ms"], b["ms"])]
     return best
@@ -165,16 +177,20 @@ def collect(graph: Graph, algo: int, name: str = "", num_memory: int = 3, reps: 
     x = log_features([base[i] for i in idx], graph.num_vertices, graph.num_edges)
     ms = np.array([[logs[m][i]["ms"][4] for m in range(NOUT)] for i in idx], dtype=np.float64)
     fm = np.array([fixed[i]["mode"] for i in idx], dtype=np.int32)
-    return RoundTable(name, algo, x, ms, fm, {"rounds": n, "V": graph.num_vertices, "E": graph.num_edges})
+    tiny = np.array([base[i]["frontier_in"] <= TINY_ACTIVE and base[i]["frontier_edges_in"] <= TINY_EDGES
+                     for i in idx], dtype=bool)
+    return RoundTable(name, algo, x, ms, fm, tiny, {"rounds": n, "V": graph.num_vertices, "E": graph.num_edges})
 
 
 def stack(tables: Iterable[RoundTable]) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Training arrays of the rounds the model decides (not the tiny ones)."""
     xs, ys, ms = [], [], []
     for t in tables:
         y, m = t.targets()
-        xs.append(t.x)
-        ys.append(y)
-        ms.append(m)
+        keep = ~t.tiny
+        xs.append(t.x[keep])
+        ys.append(y[keep])
+        ms.append(m[keep])
     return (np.ascontiguousarray(np.concatenate(xs), dtype=np.float32),
             np.ascontiguousarray(np.concatenate(ys), dtype=np.float32),
             np.ascontiguousarray(np.concatenate(ms), dtype=np.uint8))
@@ -216,6 +232,13 @@ def predict(model, x: np.ndarray, allowed: int = ALL_MODES, device: int = 0) -> 
 
 
 # -------------------------------------------------------------- evaluation --
+def choose(model, t: RoundTable, allowed: int = ALL_MODES) -> np.ndarray:
+    """The learned policy's mode for every round of a table, as the device
+    applies it (tiny frontiers: push + list)."""
+    _, ch = predict(model, t.x, allowed)
+    return np.where(t.tiny, 1, ch).astype(np.int32)
+
+
 def table_totals(t: RoundTable, choice: np.ndarray) -> dict:
     """Measured time of the rounds under a per-round choice, next to the
     fixed rule, each forced mode and the per-round best."""

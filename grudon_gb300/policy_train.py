@@ -60,8 +60,7 @@ def training_tables(scales, avals, grids, reps: int, log=print):
 def summarize(tabs, model) -> dict:
     out, tot = {}, {"chosen_ms": 0.0, "fixed_ms": 0.0, "best_ms": 0.0}
     for t in tabs:
-        _, ch = P.predict(model, t.x)
-        r = P.table_totals(t, ch)
+        r = P.table_totals(t, P.choose(model, t))
         r["rounds"] = len(t.x)
         out[t.name] = {k: round(v, 4) if isinstance(v, float) else v for k, v in r.items()}
         for k in tot:

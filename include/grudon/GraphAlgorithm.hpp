@@ -193,6 +193,15 @@ class GraphAlgorithm {
   // termination (C7), until the frontier is empty or MAX_ITERATIONS rounds.
   void run() {
     grd_ctx* c = graph->ctx();
+    if (fused) {  // the whole loop as one device-driven launch (grd_run)
+      grd_stats st{};
+      check(grd_run(c, 0, &st), c, "grd_run");
+      net.getBytesMoved() = st.reference_bytes_moved;
+      iterations = st.rounds;
+      std::printf("STAT %s Iterations %u\nSTAT %s TotalBytesMoved %llu\n", algorithm_name.c_str(), st.rounds,
+                  algorithm_name.c_str(), (unsigned long long)st.reference_bytes_moved);
+      return;
+    }
     uint32_t iteration = 0;
     bool done = false;
     while (!done && iteration < max_rounds) {
@@ -212,6 +221,19 @@ class GraphAlgorithm {
                 algorithm_name.c_str(), (unsigned long long)st.reference_bytes_moved);
   }
 
+  // Per-round schedule (results never depend on it): GRD_DIR_*, GRD_FMT_*,
+  // GRD_POLICY_* and the learned model (copied; NULL: none).  With a schedule
+  // set, run() drives the rounds as one device-side loop (grd_run) instead
+  // of stage by stage, and prints the same statistics.
+  void setSchedule(int direction, int frontier_format, int policy, const grd_policy_model* model) {
+    sched_direction = direction;
+    sched_format = frontier_format;
+    sched_policy = policy;
+    has_model = model != nullptr;
+    if (model) sched_model = *model;
+    fused = true;
+  }
+
   uint32_t getIterations() const { return iterations; }
   DistributedGraph& distributedGraph() { return *graph; }
   void setMaxRounds(uint32_t r) { max_rounds = r; }
@@ -229,13 +251,21 @@ class GraphAlgorithm {
   uint32_t iterations = 0;
   uint32_t max_rounds = MAX_ITERATIONS;
   bool clear_updates = false;
+  bool fused = false;
+  int sched_direction = GRD_DIR_AUTO, sched_format = GRD_FMT_AUTO, sched_policy = GRD_POLICY_FIXED;
+  bool has_model = false;
+  grd_policy_model sched_model{};
 
   grd_ctx* ctx() const { return graph->ctx(); }
   uint32_t V() const { return (uint32_t)graph->getNumVertices(); }
 
   // Shared plumbing of the GPU plugins below.
-  void gpu_init(int algo, const grd_params& p) {
+  void gpu_init(int algo, grd_params p) {
+    p.direction = sched_direction;
+    p.frontier_format = sched_format;
+    p.policy = sched_policy;
     check(grd_set_algo(ctx(), algo, &p), ctx(), "grd_set_algo");
+    check(grd_set_policy(ctx(), has_model ? &sched_model : nullptr), ctx(), "grd_set_policy");
     check(grd_init(ctx()), ctx(), "grd_init");
     last_frontier = 1;
   }

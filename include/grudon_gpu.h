@@ -301,15 +301,18 @@ int grd_read_partition_file(const char* path, uint32_t n, uint32_t num_memory,
 /* Learned round policy ----------------------------------------------------
  * No reference counterpart: the reference's only per-round decision engine
  * is the disabled NDP/INC offload rule (include/offload_engine/
- * NDPEngine.hpp:17-50).  An MLP 8 -> 64 -> 64 -> 4 (ReLU) predicts log2 of
- * the round time of each round mode (GRD_ROUND_*) from the shape of the
- * frontier entering the round; the round runs in the allowed mode with the
- * smallest prediction.  Weights are IEEE fp16 (bit patterns), biases and
- * accumulation fp32.  Inputs, each then mapped x = (f - mean) * scale:
- *   f0 log2(1+|F|)            f1 log2(1+out-edges of F)
- *   f2 log2(1+unvisited out-edges, SSSP; 0 otherwise)
- *   f3 log2(1+mean degree in F) f4 log2(1+max degree in F)
- *   f5 log2(1+round index)    f6 log2(V)   f7 log2(1+E/V)
+ * NDPEngine.hpp:17-50).  An MLP 8 -> 64 -> 64 -> 4 (ReLU) predicts the
+ * log2 round time of each round mode (GRD_ROUND_*), relative to their mean,
+ * from the shape of the frontier entering the round; the round runs in the
+ * allowed mode with the smallest prediction (a frontier of at most 2048
+ * vertices and 16384 edges always runs push + list in one CTA, without
+ * inference).  Weights are IEEE
+ * fp16 (bit patterns), biases and accumulation fp32.  Inputs, each then
+ * mapped x = (f - mean) * scale:
+ *   f0 log2(1+|F|) - log2 V            f1 log2(1+out-edges of F) - log2(1+E)
+ *   f2 log2(1+unvisited out-edges) - log2(1+E)   (SSSP; 0 edges otherwise)
+ *   f3 log2(1+mean degree in F)        f4 log2(1+max degree in F) - log2 V
+ *   f5 log2(1+round index)             f6 log2 V     f7 log2(1+E/V)
  * The choice never changes CC/SSSP results (min fixed points; every mode
  * computes the same values, dirty sets and round counts). */
 #define GRD_POLICY_IN  8
@@ -370,6 +373,10 @@ int grd_policy_predict(const grd_policy_model* model, const float* x, size_t n,
                        int32_t* choice);
 /* Error text of the most recent failed grd_policy_* call on this thread. */
 const char* grd_policy_error(void);
+/* Model files (the JSON layout grudon_gb300/policy_model.json uses): load
+ * returns GRD_E_IO for a missing file or a missing / short field. */
+int grd_policy_load(const char* path, grd_policy_model* out);
+int grd_policy_save(const char* path, const grd_policy_model* model);
 
 #ifdef __cplusplus
 }

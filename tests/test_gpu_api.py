@@ -53,15 +53,19 @@ def test_aggregate_values(gpu):
         assert rc == g._ffi.GRD_E_INVALID
 
 
+@pytest.mark.parametrize("schedule", [[], ["--policy", "learned", "--policy-model", "MODEL"],
+                                      ["--frontier", "list", "--direction", "push"]], ids=["stages", "learned", "list"])
 @pytest.mark.parametrize("algo", ["cc", "sssp", "sssp_w", "pr"])
-def test_cli_plugin_api_matches_oracle(gpu, tmp_path, algo):
+def test_cli_plugin_api_matches_oracle(gpu, tmp_path, algo, schedule):
     G = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
     path = str(tmp_path / "g.gr")
     G.write_gr(path)
     part = G.partition_edge_balanced(3)
     pf = str(tmp_path / "parts.txt")
     g.write_partition_file(part, pf)
-    r = subprocess.run([str(CLI), "-g", path, "-c", "1", "-m", "3", "-p", pf, "-a", algo, "--verify"],
+    from grudon_gb300 import policy as P
+    schedule = [str(P.MODEL_FILE) if a == "MODEL" else a for a in schedule]
+    r = subprocess.run([str(CLI), "-g", path, "-c", "1", "-m", "3", "-p", pf, "-a", algo, "--verify"] + schedule,
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     out = dict(line.split(" ", 1) for line in r.stdout.splitlines() if line.startswith(("CHECKSUM", "VERIFY")))
