@@ -69,7 +69,8 @@ class grd_policy_model(C.Structure):
     _fields_ = [("mean", C.c_float * GRD_POLICY_IN), ("scale", C.c_float * GRD_POLICY_IN),
                 ("w1", C.c_uint16 * (GRD_POLICY_HID * GRD_POLICY_IN)), ("b1", C.c_float * GRD_POLICY_HID),
                 ("w2", C.c_uint16 * (GRD_POLICY_HID * GRD_POLICY_HID)), ("b2", C.c_float * GRD_POLICY_HID),
-                ("w3", C.c_uint16 * (GRD_POLICY_OUT * GRD_POLICY_HID)), ("b3", C.c_float * GRD_POLICY_OUT)]
+                ("w3", C.c_uint16 * (GRD_POLICY_OUT * GRD_POLICY_HID)), ("b3", C.c_float * GRD_POLICY_OUT),
+                ("lo", C.c_float * GRD_POLICY_IN), ("hi", C.c_float * GRD_POLICY_IN)]
 
 
 class grd_policy_train_cfg(C.Structure):

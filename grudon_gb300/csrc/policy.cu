@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(P_HID) k_mlp_grad(const grd_policy_model* m, c
   for (int o = 0; o < P_OUT; ++o) gw3[o] = 0.0f;
   float gb1 = 0.0f, gb2 = 0.0f, gb3 = 0.0f, loss = 0.0f;
   for (uint32_t s = blockIdx.x; s < n; s += gridDim.x) {
-    if (j < P_IN) s_x[j] = (x[(size_t)s * P_IN + j] - m->mean[j]) * m->scale[j];
+    if (j < P_IN) s_x[j] = policy_input(m, j, x[(size_t)s * P_IN + j]);
     __syncthreads();
     // forward (same arithmetic as mlp_eval)
     float a = m->b1[j];
@@ -155,8 +155,7 @@ __global__ void __launch_bounds__(P_HID) k_mlp_predict(const grd_policy_model* m
   MlpRegs r;
   mlp_load(m, r);
   for (uint32_t s = blockIdx.x; s < n; s += gridDim.x) {
-    if (threadIdx.x < P_IN) s_x[threadIdx.x] = (x[(size_t)s * P_IN + threadIdx.x] - m->mean[threadIdx.x]) *
-                                                m->scale[threadIdx.x];
+    if (threadIdx.x < P_IN) s_x[threadIdx.x] = policy_input(m, threadIdx.x, x[(size_t)s * P_IN + threadIdx.x]);
     __syncthreads();
     mlp_eval(r, s_x, s_h1, s_h2, s_out);
     if (threadIdx.x == 0) {
@@ -289,18 +288,24 @@ int grd_policy_train(const float* x, const float* y, const uint8_t* mask, size_t
     g_policy_error = "no measured targets";
     return GRD_E_INVALID;
   }
-  // Input normalisation from the data (mean 0, unit spread).
+  // Input normalisation from the data (mean 0, unit spread) and the
+  // training range every input is clamped to.
   grd_policy_model host{};
   for (int i = 0; i < P_IN; ++i) {
     double s = 0.0, s2 = 0.0;
+    float lo = x[i], hi = x[i];
     for (size_t k = 0; k < n; ++k) {
       const double v = x[k * P_IN + i];
       s += v;
       s2 += v * v;
+      lo = std::min(lo, x[k * P_IN + i]);
+      hi = std::max(hi, x[k * P_IN + i]);
     }
     const double mu = s / (double)n, var = std::max(0.0, s2 / (double)n - mu * mu);
     host.mean[i] = (float)mu;
     host.scale[i] = (float)(1.0 / std::max(std::sqrt(var), 1e-3));
+    host.lo[i] = lo;
+    host.hi[i] = hi;
   }
   // He-uniform weights, zero biases, output biases at the mean target.
   std::vector<float> p(NPARAM, 0.0f);

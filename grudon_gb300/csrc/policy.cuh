@@ -58,6 +58,12 @@ __host__ __device__ inline uint32_t policy_allowed(int direction, int format, bo
 
 __device__ __forceinline__ float h2f(uint16_t b) { return __half2float(__ushort_as_half(b)); }
 
+// Normalised input i of the model from raw feature f (clamped to the
+// training range).
+__device__ __forceinline__ float policy_input(const grd_policy_model* m, int i, float f) {
+  return (fminf(fmaxf(f, m->lo[i]), m->hi[i]) - m->mean[i]) * m->scale[i];
+}
+
 // Weights of hidden unit j (thread j) and, for threads below P_OUT, of
 // output j, held in registers: every load is issued at once, so one memory
 // latency covers the whole model (the struct keeps each row 16-byte aligned).
@@ -129,6 +135,11 @@ __device__ __forceinline__ int policy_fixed(const DevGraph& g, const PolicyArgs&
               : (list ? GRD_ROUND_PUSH_LIST : GRD_ROUND_PUSH_BITVEC);
 }
 
+// The model overrides the plain method's choice (the fixed rule without the
+// in-edge view, i.e. push only, unless pull is forced) only when it predicts
+// that round to be faster by more than this margin (log2 units, ~7 %).
+constexpr float P_MARGIN = 0.1f;
+
 // A frontier that fits one CTA runs as push + list (one kernel, k_round_tiny)
 // whatever the model would say: no other mode comes close for it, and the
 // round skips the inference.
@@ -150,14 +161,18 @@ __device__ __forceinline__ int policy_choose(const DevGraph& g, const DevState& 
     float raw[P_IN];
     policy_features((double)f, (double)fe, (double)st.counters[C_UNVISITED], (double)st.counters[C_FMAXDEG],
                     (double)round, (double)g.V, (double)a.edges, raw);
-    for (int i = 0; i < P_IN; ++i) s_x[i] = (raw[i] - model->mean[i]) * model->scale[i];
+    for (int i = 0; i < P_IN; ++i) s_x[i] = policy_input(model, i, raw[i]);
   }
   __syncthreads();
   mlp_eval(r, s_x, s_h1, s_h2, s_out);
   int best = -1;
   for (int m = 0; m < P_OUT; ++m)
     if (((allowed >> m) & 1u) && (best < 0 || s_out[m] < s_out[best])) best = m;
-  return best < 0 ? policy_fixed(g, a, f, fe) : best;
+  PolicyArgs plain = a;
+  if (a.direction != GRD_DIR_PULL) plain.has_in = 0;
+  const int fm = policy_fixed(g, plain, f, fe);
+  if (best < 0) return fm;
+  return s_out[best] + P_MARGIN < s_out[fm] ? best : fm;
 }
 
 // The round's policy kernel (one block of P_HID threads).  In the device

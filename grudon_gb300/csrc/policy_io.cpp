@@ -79,6 +79,12 @@ int grd_policy_load(const char* path, grd_policy_model* out) {
                   parse_field(s, m, "w3", t.w3, GRD_POLICY_OUT * GRD_POLICY_HID) &&
                   parse_field(s, m, "b3", t.b3, GRD_POLICY_OUT);
   if (!ok) return GRD_E_IO;
+  // files without a training range: no clamping
+  if (s.find("\"lo\"", m) == std::string::npos && s.find("\"hi\"", m) == std::string::npos) {
+    for (int i = 0; i < GRD_POLICY_IN; ++i) t.lo[i] = -1e30f, t.hi[i] = 1e30f;
+  } else if (!parse_field(s, m, "lo", t.lo, GRD_POLICY_IN) || !parse_field(s, m, "hi", t.hi, GRD_POLICY_IN)) {
+    return GRD_E_IO;
+  }
   *out = t;
   return GRD_OK;
 }
@@ -95,7 +101,9 @@ int grd_policy_save(const char* path, const grd_policy_model* m) {
   write_field(f, "w2", m->w2, GRD_POLICY_HID * GRD_POLICY_HID, true, false);
   write_field(f, "b2", m->b2, GRD_POLICY_HID, false, false);
   write_field(f, "w3", m->w3, GRD_POLICY_OUT * GRD_POLICY_HID, true, false);
-  write_field(f, "b3", m->b3, GRD_POLICY_OUT, false, true);
+  write_field(f, "b3", m->b3, GRD_POLICY_OUT, false, false);
+  write_field(f, "lo", m->lo, GRD_POLICY_IN, false, false);
+  write_field(f, "hi", m->hi, GRD_POLICY_IN, false, true);
   std::fprintf(f, "}, \"meta\": {}}\n");
   const bool ok = std::fclose(f) == 0;
   return ok ? GRD_OK : GRD_E_IO;

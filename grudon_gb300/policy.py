@@ -51,6 +51,9 @@ def model_to_dict(m: _ffi.grd_policy_model) -> dict:
 
 def model_from_dict(d: dict) -> _ffi.grd_policy_model:
     m = _ffi.grd_policy_model()
+    d = dict(d)
+    d.setdefault("lo", [-1e30] * NIN)  # files without a training range: no clamping
+    d.setdefault("hi", [1e30] * NIN)
     for f, t in _ffi.grd_policy_model._fields_:
         arr = getattr(m, f)
         vals = d[f]
@@ -80,7 +83,8 @@ def model_arrays(m: _ffi.grd_policy_model) -> Dict[str, np.ndarray]:
     return {"mean": np.array(m.mean, dtype=np.float64), "scale": np.array(m.scale, dtype=np.float64),
             "w1": half(m.w1, (NHID, NIN)), "b1": np.array(m.b1, dtype=np.float64),
             "w2": half(m.w2, (NHID, NHID)), "b2": np.array(m.b2, dtype=np.float64),
-            "w3": half(m.w3, (NOUT, NHID)), "b3": np.array(m.b3, dtype=np.float64)}
+            "w3": half(m.w3, (NOUT, NHID)), "b3": np.array(m.b3, dtype=np.float64),
+            "lo": np.array(m.lo, dtype=np.float64), "hi": np.array(m.hi, dtype=np.float64)}
 
 
 # ---------------------------------------------------------------- features --
@@ -232,11 +236,33 @@ def predict(model, x: np.ndarray, allowed: int = ALL_MODES, device: int = 0) -> 
 
 
 # -------------------------------------------------------------- evaluation --
+MARGIN = 0.1  # = P_MARGIN of the device rule (log2 units)
+
+
+def fixed_rule_mode(frontier, frontier_edges, num_slots: int, num_edges: int, dense_div: int = 8) -> np.ndarray:
+    """The plain method's choice (fixed rule without the in-edge view)."""
+    f = np.asarray(frontier, dtype=np.float64)
+    fe = np.asarray(frontier_edges, dtype=np.float64)
+    lst = (f * dense_div < num_slots) & (fe * dense_div < num_edges)
+    return np.where(lst, 1, 0).astype(np.int32)
+
+
+def decide(out: np.ndarray, fallback: np.ndarray, tiny: np.ndarray, allowed: int = ALL_MODES) -> np.ndarray:
+    """The device rule: the fastest predicted allowed mode when it beats the
+    fallback's prediction by more than MARGIN, else the fallback; push + list
+    for tiny frontiers."""
+    o = np.where([(allowed >> m) & 1 for m in range(NOUT)], out, np.inf)
+    best = np.argmin(o, axis=1)
+    rows = np.arange(len(out))
+    ch = np.where(o[rows, best] + MARGIN < out[rows, fallback], best, fallback)
+    return np.where(tiny, 1, ch).astype(np.int32)
+
+
 def choose(model, t: RoundTable, allowed: int = ALL_MODES) -> np.ndarray:
     """The learned policy's mode for every round of a table, as the device
-    applies it (tiny frontiers: push + list)."""
-    _, ch = predict(model, t.x, allowed)
-    return np.where(t.tiny, 1, ch).astype(np.int32)
+    applies it."""
+    out, _ = predict(model, t.x, allowed)
+    return decide(out, t.fixed_mode, t.tiny, allowed)
 
 
 def table_totals(t: RoundTable, choice: np.ndarray) -> dict:

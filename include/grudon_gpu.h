@@ -304,11 +304,12 @@ int grd_read_partition_file(const char* path, uint32_t n, uint32_t num_memory,
  * NDPEngine.hpp:17-50).  An MLP 8 -> 64 -> 64 -> 4 (ReLU) predicts the
  * log2 round time of each round mode (GRD_ROUND_*), relative to their mean,
  * from the shape of the frontier entering the round; the round runs in the
- * allowed mode with the smallest prediction (a frontier of at most 2048
- * vertices and 16384 edges always runs push + list in one CTA, without
- * inference).  Weights are IEEE
- * fp16 (bit patterns), biases and accumulation fp32.  Inputs, each then
- * mapped x = (f - mean) * scale:
+ * allowed mode with the smallest prediction when it beats the plain
+ * method's choice (the fixed rule, push only) by more than 0.1 in log2
+ * units, else the plain choice (a frontier of at most 2048 vertices and
+ * 16384 edges always runs push + list in one CTA, without inference).
+ * Weights are IEEE fp16 (bit patterns), biases and accumulation fp32.
+ * Inputs, each then mapped x = (clamp(f, lo, hi) - mean) * scale:
  *   f0 log2(1+|F|) - log2 V            f1 log2(1+out-edges of F) - log2(1+E)
  *   f2 log2(1+unvisited out-edges) - log2(1+E)   (SSSP; 0 edges otherwise)
  *   f3 log2(1+mean degree in F)        f4 log2(1+max degree in F) - log2 V
@@ -330,6 +331,10 @@ typedef struct grd_policy_model {
   float b2[GRD_POLICY_HID];
   uint16_t w3[GRD_POLICY_OUT * GRD_POLICY_HID];  /* [out][in], fp16 */
   float b3[GRD_POLICY_OUT];
+  /* Raw features are clamped to [lo, hi] (the training range) before the
+   * mapping, so graphs beyond the training scales are seen as the nearest
+   * trained ones rather than extrapolated. */
+  float lo[GRD_POLICY_IN], hi[GRD_POLICY_IN];
 } grd_policy_model;
 
 /* Uploads a model for GRD_POLICY_LEARNED runs (NULL clears it). */
@@ -353,7 +358,7 @@ typedef struct grd_policy_train_cfg {
 /* Trains on the GPU (own forward/backward kernels, Adam, fp32 master
  * weights rounded to fp16 for every forward pass).  x: n x 8 raw features;
  * y: n x 4 log2(round ms) targets; mask: n x 4 (1 = target measured).
- * mean/scale of `model` are computed from x.  loss_curve (optional, `steps`
+ * mean/scale/lo/hi of `model` are computed from x.  loss_curve (optional, `steps`
  * entries) receives the masked MSE before each step. */
 int grd_policy_train(const float* x, const float* y, const uint8_t* mask,
                      size_t n, const grd_policy_train_cfg* cfg,

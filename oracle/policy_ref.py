@@ -1,7 +1,7 @@
 """FP64 CPU restatement of the round-policy MLP (test infrastructure only).
 
 The learned policy has no counterpart in the reference, so this oracle is the
-mathematics of the model itself: x = (f - mean) * scale, h1 = relu(W1 x + b1),
+mathematics of the model itself: x = (clamp(f, lo, hi) - mean) * scale, h1 = relu(W1 x + b1),
 h2 = relu(W2 h1 + b2), out = W3 h2 + b3, masked mean squared error against
 log2 round times, and its exact gradient by backpropagation.  It checks the
 GPU forward/backward kernels (grd_policy_grad, grd_policy_predict) and the
@@ -15,7 +15,10 @@ import numpy as np
 def forward(p: dict, x: np.ndarray):
     """p: float64 arrays (mean, scale, w1 [64,8], b1, w2 [64,64], b2, w3 [4,64],
     b3).  Returns (out [n,4], cache)."""
-    xs = (np.asarray(x, dtype=np.float64) - p["mean"]) * p["scale"]
+    f = np.asarray(x, dtype=np.float64)
+    if "lo" in p:
+        f = np.clip(f, p["lo"], p["hi"])
+    xs = (f - p["mean"]) * p["scale"]
     a1 = xs @ p["w1"].T + p["b1"]
     h1 = np.maximum(a1, 0.0)
     a2 = h1 @ p["w2"].T + p["b2"]

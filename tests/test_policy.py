@@ -23,6 +23,7 @@ def random_model(seed: int, spread: float = 1.0) -> _ffi.grd_policy_model:
         d[k] = np.asarray(d[k], dtype=np.float16).view(np.uint16).tolist()
     for k in ("mean", "scale", "b1", "b2", "b3"):
         d[k] = np.asarray(d[k], dtype=np.float32).tolist()
+    d["lo"], d["hi"] = [-1e30] * 8, [1e30] * 8
     return P.model_from_dict(d)
 
 
@@ -123,6 +124,14 @@ def test_gpu_inference_matches_oracle(gpu):
     for allowed in (0x3, 0x5, 0xA, 0xC):
         _, ch2 = P.predict(m, x, allowed)
         assert np.all((allowed >> ch2) & 1)
+    # inputs outside the training range are clamped to it
+    for i in range(8):
+        m.lo[i], m.hi[i] = 6.0, 10.0
+    out, _ = P.predict(m, x)
+    ref, _ = R.forward(P.model_arrays(m), x)
+    np.testing.assert_allclose(out, ref, rtol=1e-4, atol=1e-4)
+    out_c, _ = P.predict(m, np.clip(x, 6.0, 10.0))
+    np.testing.assert_array_equal(out, out_c)
 
 
 @pytest.mark.gpu
@@ -186,12 +195,18 @@ def test_fused_inference_follows_the_model(gpu):
         ctx.init()
         ctx.run()
         log = ctx.round_log()
+        tile = 8192  # slots per partition are padded to whole compaction tiles
+        S = sum(-(-(no + npx) // tile) * tile for no, npx, _ in (ctx.layout_info(p) for p in range(2)))
     x = P.log_features(log, G.num_vertices, G.num_edges)
-    out, ch = P.predict(m, x)
+    out, _ = P.predict(m, x)
     tiny = np.array([r["frontier_in"] <= P.TINY_ACTIVE and r["frontier_edges_in"] <= P.TINY_EDGES for r in log])
-    ch = np.where(tiny, g.GRD_ROUND_PUSH_LIST, ch)
+    fallback = P.fixed_rule_mode([r["frontier_in"] for r in log], [r["frontier_edges_in"] for r in log], S,
+                                 G.num_edges)
+    ch = P.decide(out, fallback, tiny)
+    # rounds whose decision is not within rounding of a tie
     srt = np.sort(out, axis=1)
-    clear = (srt[:, 1] - srt[:, 0] > 1e-4) | tiny
+    gap = np.abs(out.min(axis=1) + P.MARGIN - out[np.arange(len(out)), fallback])
+    clear = ((srt[:, 1] - srt[:, 0] > 1e-4) & (gap > 1e-4)) | tiny
     modes = np.array([r["mode"] for r in log])
     np.testing.assert_array_equal(modes[clear], ch[clear])
     assert (~tiny).any()  # some rounds were decided by the model
