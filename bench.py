@@ -492,8 +492,9 @@ def main():
     h2d = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for c in (ctx_cc, ctx_ss):
+        for c in (ctx_cc, ctx_ss):  # queued on each ctx's stream: SSSP's copy overlaps CC's run
             h2d += c.upload()
+        for c in (ctx_cc, ctx_ss):
             c.init()
             c.run()
             c.read_props()

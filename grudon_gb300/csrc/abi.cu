@@ -143,7 +143,8 @@ int grd_upload_layout(grd_ctx* ctx) {
     TRY(upload(ctx, (uint32_t*)g.in_src, L.in_src));
     if (L.weighted) TRY(upload(ctx, (uint32_t*)g.in_wgt, L.in_wgt));
   }
-  CK(cudaStreamSynchronize(ctx->stream));
+  // stream-ordered: the pinned host arrays belong to the ctx and outlive the
+  // copies; the small pageable ones are staged before the copy call returns
   return GRD_OK;
 }
 
@@ -1032,10 +1033,14 @@ int grd_ctx_init_device(grd_ctx* ctx) {
 void grd_pin_host(grd_ctx* ctx, std::initializer_list<std::vector<uint32_t>*> arrays) {
   for (auto* v : arrays) {
     if (v->size() * sizeof(uint32_t) < (1u << 20)) continue;
-    if (cudaHostRegister(v->data(), v->size() * sizeof(uint32_t), cudaHostRegisterDefault) == cudaSuccess)
+    const cudaError_t e = cudaHostRegister(v->data(), v->size() * sizeof(uint32_t), cudaHostRegisterDefault);
+    if (e == cudaSuccess) {
       ctx->host_registered.push_back(v->data());
-    else
+    } else {
       (void)cudaGetLastError();
+      std::fprintf(stderr, "grudon: pinning %zu B of host layout failed (%s); uploads use pageable copies\n",
+                   v->size() * sizeof(uint32_t), cudaGetErrorString(e));
+    }
   }
 }
 

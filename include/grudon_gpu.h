@@ -147,7 +147,9 @@ const char* grd_last_error(const grd_ctx* ctx);
 const char* grd_create_error(void);
 
 /* Re-uploads the layout arrays from the host copy kept at create time
- * (timed host->device traffic for end-to-end runs). Returns bytes copied. */
+ * (timed host->device traffic for end-to-end runs). Returns bytes copied.
+ * The copies are queued on the ctx stream (pinned host memory) and the call
+ * returns at once; every later call on the ctx sees the new data. */
 int grd_upload(grd_ctx* ctx, uint64_t* bytes_copied);
 
 /* Algorithm selection and per-stage round API -----------------------------*/
