@@ -859,10 +859,11 @@ static __global__ void __launch_bounds__(256) k_deg_down(DevGraph g, DevState st
   }
 }
 
-// One warp per 256-edge chunk.  The warp stages a window of LBS_WIN
-// consecutive actives (their DP, row start and source value) in shared memory
-// with 8 independent coalesced loads per lane — one window covers the whole
-// chunk unless more than LBS_WIN actives fall inside it.  The source of each
+// One warp per 256-edge chunk.  The warp stages a window of up to LBS_WIN
+// consecutive actives (their DP, row start and source value) in shared
+// memory, 32 at a time with coalesced loads, only as many as the chunk's
+// edges need (one group of 32 for a typical degree) — one window covers the
+// whole chunk unless more than LBS_WIN actives fall inside it.  The source of each
 // of the window's edge positions comes from a mark-and-scan in shared memory
 // (every active marks the position where its row starts, then a running max
 // over the 256 positions), so an edge costs one shared load to find its row
@@ -893,35 +894,38 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
     const uint32_t e_end = min(m, e + LBS_CHUNK);
     uint32_t i0 = st.chunk_start[c];
     while (e < e_end) {
-      uint32_t a[SW], b[SW], v[SW];
-#pragma unroll
-      for (int k = 0; k < SW; ++k) {
-        const uint32_t idx = i0 + k * 32 + lane;
-        a[k] = idx < K ? st.DP[idx] : m;
-        b[k] = idx < K ? st.RB[idx] : 0u;
-        v[k] = idx < K ? st.SV[idx] : 0u;
-      }
-      const uint32_t tail = (lane == 0) ? (i0 + LBS_WIN < K ? st.DP[i0 + LBS_WIN] : m) : 0u;
-      const uint32_t wend = min(e_end, __shfl_sync(FULL, tail, 0));
+      // Load the window 32 actives at a time, only as far as the chunk
+      // needs: `cover` is the DP of the first active not loaded.
       static_assert(LBS_CHUNK == 8 * 32, "each lane owns 8 consecutive edge positions");
 #pragma unroll
       for (int q = 0; q < 8; ++q) srcs[8 * lane + q] = 0;
-#pragma unroll
-      for (int k = 0; k < SW; ++k) {
-        dp[k * 32 + lane] = a[k];
-        rbs[k * 32 + lane] = b[k];
-        svs[k * 32 + lane] = source_value<A>(v[k]);
-      }
+      uint32_t nw = 0, cover;
+      do {
+        const uint32_t idx = i0 + nw * 32 + lane;
+        const uint32_t av = idx < K ? st.DP[idx] : m;
+        const uint32_t bv = idx < K ? st.RB[idx] : 0u;
+        const uint32_t vv = idx < K ? st.SV[idx] : 0u;
+        const uint32_t nx = i0 + nw * 32 + 32;
+        const uint32_t tl = (lane == 31) ? (nx < K ? st.DP[nx] : m) : 0u;
+        dp[nw * 32 + lane] = av;
+        rbs[nw * 32 + lane] = bv;
+        svs[nw * 32 + lane] = source_value<A>(vv);
+        cover = __shfl_sync(FULL, tl, 31);
+        ++nw;
+      } while (nw < (uint32_t)SW && cover < e_end);
+      const uint32_t wend = min(e_end, cover);
       __syncwarp();
       // mark: the row of window active j starts at position dp[j] - e (the
       // first active's row may start before the window: position 0).  Only
       // rows with edges mark, so no two actives share a position.
-      const uint32_t tailv = __shfl_sync(FULL, tail, 0);
 #pragma unroll
       for (int k = 0; k < SW; ++k) {
         const uint32_t j = k * 32 + lane;
-        const uint32_t next = j + 1 < LBS_WIN ? dp[j + 1] : tailv;
-        if (a[k] < wend && next > a[k]) srcs[(a[k] > e ? a[k] : e) - e] = j;
+        if ((uint32_t)k < nw) {
+          const uint32_t aj = dp[j];
+          const uint32_t next = j + 1 < nw * 32 ? dp[j + 1] : cover;
+          if (aj < wend && next > aj) srcs[(aj > e ? aj : e) - e] = j;
+        }
       }
       __syncwarp();
       // scan: running max over the positions (lane-local 8, then the warp)
@@ -971,7 +975,7 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
       }
       __syncwarp();
       e = wend;
-      i0 += LBS_WIN;
+      i0 += nw * 32;
     }
   }
 }
