@@ -52,8 +52,9 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=512)
     ap.add_argument("--batch-sources", type=int, default=64)
-    ap.add_argument("--policy", choices=["auto", "fixed", "learned"], default="auto",
-                    help="round policy of the measured runs (auto: learned when the model file is present)")
+    ap.add_argument("--policy", choices=["fixed", "learned"], default="fixed",
+                    help="round policy of the headline runs (the other one is timed beside it when the model "
+                         "file is present)")
     ap.add_argument("--kernel-run", action="store_true",
                     help="only run the workload's steps with the rounds driven from the host (plain kernel "
                          "launches, no CUDA graphs) and print a short summary: the target of per-kernel profilers")
@@ -381,12 +382,10 @@ def main():
             c.set_algo(a, policy=policy)
             c.set_policy(model if policy == g.GRD_POLICY_LEARNED else None)
 
-    # the product configuration: the shipped learned round policy when its
-    # model file is present, else the fixed threshold rule.  The plain method
-    # (fixed rule, push only: no in-edge view yet) is timed first.
-    policy = g.GRD_POLICY_LEARNED if model is not None else g.GRD_POLICY_FIXED
-    if args.policy == "fixed" or (args.policy == "learned" and model is None):
-        policy = g.GRD_POLICY_FIXED
+    # The headline runs the library's default schedule, the fixed threshold
+    # rule (push only: no in-edge view), unless --policy learned.  The shipped
+    # learned policy, when its model file is present, is timed next to it.
+    policy = g.GRD_POLICY_LEARNED if (args.policy == "learned" and model is not None) else g.GRD_POLICY_FIXED
     set_policy(g.GRD_POLICY_FIXED)
     E = G_cc.num_edges + G_ss.num_edges
     slots = {id(c): sum(sum(c.layout_info(p)[:2]) for p in range(NUM_MEMORY)) for c in (ctx_cc, ctx_ss)}
@@ -445,25 +444,20 @@ def main():
         thr, secs, _ = job_throughput(args.steps * E, ev0.elapsed_time(ev1) / 1e3, dev)
         return thr / 1e9, secs * 1e3, agg
 
+    def summary(v, ms, a):
+        return {"value": v, "ms_per_step": ms / args.steps, "rounds_per_step": a["rounds"][:2],
+                "push_rounds_per_step": a["push_rounds"] / args.steps,
+                "pull_rounds_per_step": a["pull_rounds"] / args.steps, "gpu_launches": a["launches"]}
+
     clocks = ClockSampler(local)
     clocks.start()
-    plain = None
-    if policy == g.GRD_POLICY_LEARNED:
-        pv, pms, pagg = timed()
-        plain = {"value": pv, "ms_per_step": pms / args.steps, "rounds_per_step": pagg["rounds"][:2],
-                 "push_rounds_per_step": pagg["push_rounds"] / args.steps,
-                 "pull_rounds_per_step": pagg["pull_rounds"] / args.steps, "gpu_launches": pagg["launches"]}
+    runs = {}
+    if policy == g.GRD_POLICY_LEARNED:  # the plain method first (before the in-edge view exists)
+        runs["fixed"] = summary(*timed())
         set_policy(policy)
     value, dt_ms, agg = timed()
     clk = clocks.stop()
-    results_identical = True
-    if plain is not None:  # the learned schedule leaves every result bit-identical
-        outs = []
-        for pol in (g.GRD_POLICY_FIXED, policy):
-            set_policy(pol)
-            outs.append([(c.init(), c.run(), c.read_props())[2] for c in (ctx_cc, ctx_ss)])
-        results_identical = all(bool((a == b).all()) for a, b in zip(*outs))
-        set_policy(policy)
+    runs["learned" if policy == g.GRD_POLICY_LEARNED else "fixed"] = summary(value, dt_ms, agg)
 
     # Stage timing for the roofline: the same steps driven from the host with
     # CUDA events around every stage of every round (same kernels, same
@@ -504,6 +498,19 @@ def main():
            "h2d_bytes_per_step": h2d // args.steps,
            "d2h_bytes_per_step": 4 * (G_cc.num_vertices + G_ss.num_vertices)}
 
+    # The other schedule on the same contexts; the learned one must leave
+    # every result bit-identical.
+    results_identical = None
+    if model is not None:
+        if "learned" not in runs:
+            set_policy(g.GRD_POLICY_LEARNED)
+            runs["learned"] = summary(*timed())
+        outs = []
+        for pol in (g.GRD_POLICY_FIXED, g.GRD_POLICY_LEARNED):
+            set_policy(pol)
+            outs.append([(c.init(), c.run(), c.read_props())[2] for c in (ctx_cc, ctx_ss)])
+        results_identical = all(bool((a == b).all()) for a, b in zip(*outs))
+
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -533,12 +540,11 @@ def main():
             "e2e": e2e, "gpu_launches": agg["launches"], "roofline": roofline, "clocks": clk,
             "rounds_per_step": agg["rounds"][:2], "device_loop": all(agg["device_loop"]),
             "edges_scanned_gteps": ws * agg["edges"] / (dt_ms / 1e3) / 1e9,
-            "policy": {"kind": "learned" if policy == g.GRD_POLICY_LEARNED else "fixed",
+            "policy": {"headline": "learned" if policy == g.GRD_POLICY_LEARNED else "fixed",
                        "model": "grudon_gb300/policy_model.json" if model is not None else None,
-                       "push_rounds_per_step": agg["push_rounds"] / args.steps,
-                       "pull_rounds_per_step": agg["pull_rounds"] / args.steps,
-                       "plain_fixed_rule": plain,
-                       "speedup_vs_fixed": (value / plain["value"]) if plain else None,
+                       **runs,
+                       "learned_speedup_vs_fixed": (runs["learned"]["value"] / runs["fixed"]["value"])
+                       if "learned" in runs else None,
                        "results_bit_identical": results_identical},
         }
         if ws == 1 and not args.no_cpu_baseline:
