@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--policy", choices=["fixed", "learned"], default="fixed",
                     help="round policy of the headline runs (the other one is timed beside it when the model "
                          "file is present)")
+    ap.add_argument("--kernel-run-pr", action="store_true",
+                    help="only run PageRank (Jacobi pull, RMAT-{pr-scale}) for warmup + steps iterations and print a "
+                         "short summary: the target of per-kernel profilers")
     ap.add_argument("--kernel-run", action="store_true",
                     help="only run the workload's steps with the rounds driven from the host (plain kernel "
                          "launches, no CUDA graphs) and print a short summary: the target of per-kernel profilers")
@@ -370,6 +373,17 @@ def main():
     import grudon_gb300 as g
 
     threads = max(1, (os.cpu_count() or 1) // ws)
+    if args.kernel_run_pr:
+        a, b, c = RMAT_ABC
+        G = g.Graph.rmat(args.pr_scale, EF, a, b, c, seed=g.rmat_seed(args.pr_scale, EF), threads=threads)
+        with g.Context(G, G.partition_edge_balanced(NUM_MEMORY), num_memory=NUM_MEMORY, device=local) as ctx:
+            ctx.set_algo(g.GRD_PR_PULL, max_rounds=args.warmup + args.steps, tolerance=0.0)
+            ctx.init()
+            st = ctx.run()
+        if rank == 0:
+            print(json.dumps({"kernel_run_pr": True, "scale": args.pr_scale, "iterations": st["rounds"],
+                              "edges": G.num_edges}), flush=True)
+        return
     seed, G_cc, G_ss = make_graphs(args.scale, threads)
     p_cc = G_cc.partition_edge_balanced(NUM_MEMORY)
     p_ss = G_ss.partition_edge_balanced(NUM_MEMORY)
