@@ -495,6 +495,13 @@ def main():
     for c in (ctx_cc, ctx_ss):
         c.set_profiling(False)
 
+    # Host->device bandwidth of the layout upload alone (both graphs).
+    barrier()
+    t0 = time.perf_counter()
+    up_bytes = sum(c.upload() for c in (ctx_cc, ctx_ss))
+    barrier()
+    upload_gbs = up_bytes / (time.perf_counter() - t0) / 1e9
+
     # End to end through the C ABI with host buffers.
     barrier()
     h2d = 0
@@ -510,7 +517,8 @@ def main():
     e2e_thr, _, _ = job_throughput(args.steps * E, time.perf_counter() - t0, dev)
     e2e = {"value": e2e_thr / 1e9, "unit": "GTEPS",
            "h2d_bytes_per_step": h2d // args.steps,
-           "d2h_bytes_per_step": 4 * (G_cc.num_vertices + G_ss.num_vertices)}
+           "d2h_bytes_per_step": 4 * (G_cc.num_vertices + G_ss.num_vertices),
+           "upload_alone_gbs": upload_gbs}
 
     # The other schedule on the same contexts; the learned one must leave
     # every result bit-identical.
