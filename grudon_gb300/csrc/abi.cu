@@ -165,6 +165,11 @@ int grd_ensure_in_edges(grd_ctx* ctx) {
   if (!L.in_hubs.empty())
     CK(cudaMemcpyAsync(ctx->pull.in_hubs, L.in_hubs.data(), sizeof(HubChunkD) * L.in_hubs.size(),
                        cudaMemcpyHostToDevice, ctx->stream));
+  ctx->pull.num_in_meds = (uint32_t)L.in_meds.size();
+  TRY(dev_alloc(ctx, &ctx->pull.in_meds, std::max<size_t>(L.in_meds.size(), 1)));
+  if (!L.in_meds.empty())
+    CK(cudaMemcpyAsync(ctx->pull.in_meds, L.in_meds.data(), sizeof(HubChunkD) * L.in_meds.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return GRD_OK;
 }
@@ -299,7 +304,8 @@ int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
 
 // Kernels of the edge-map of one round in each mode.
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
-  if (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST) return ctx->pull.num_in_hubs ? 2 : 1;
+  if (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)
+    return 1 + (ctx->pull.num_in_meds ? 1 : 0) + (ctx->pull.num_in_hubs ? 1 : 0);
   return 4 + (ctx->g.num_hubs ? 1 : 0) + (mode == RM_PUSH_BITVEC ? 1 : 0);
 }
 
@@ -332,8 +338,12 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
     const uint32_t pull_hub_grid = std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8));
+    const uint32_t pull_med_grid = std::min<uint32_t>((ctx->pull.num_in_meds + 7) / 8, grid_for(ctx, 8));
     if (mode == RM_PULL_BITVEC) {
       k_pull<A, false><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ctx->pull.num_in_meds)
+        k_pull_med<A, false><<<pull_med_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_meds,
+                                                                     ctx->pull.num_in_meds);
       if (ctx->pull.num_in_hubs)
         k_pull_hub<A, false><<<pull_hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_hubs,
                                                                      ctx->pull.num_in_hubs);
@@ -342,6 +352,9 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
     }
     if (mode == RM_PULL_LIST) {
       k_pull<A, true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ctx->pull.num_in_meds)
+        k_pull_med<A, true><<<pull_med_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_meds,
+                                                                    ctx->pull.num_in_meds);
       if (ctx->pull.num_in_hubs)
         k_pull_hub<A, true><<<pull_hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_hubs,
                                                                     ctx->pull.num_in_hubs);

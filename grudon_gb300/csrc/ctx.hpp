@@ -17,6 +17,8 @@ struct PullState {
   double* h_residual = nullptr;   // pinned mirror
   grd::HubChunkD* in_hubs = nullptr;  // destination slots with long in-lists
   uint32_t num_in_hubs = 0;
+  grd::HubChunkD* in_meds = nullptr;  // destination slots with medium in-lists
+  uint32_t num_in_meds = 0;
   uint64_t edges = 0;                 // in-edges read since init
 };
 

@@ -1072,6 +1072,7 @@ __global__ void __launch_bounds__(256) k_diff_dirty(DevGraph g, DevState st) {
 // ascending source order, so its sums are reproducible.  PR_PULL folds every
 // source with a Kahan sum.
 constexpr uint32_t K_PULL_HUB = 1024;  // = PULL_HUB of the layout
+constexpr uint32_t K_PULL_MED = 64;    // = PULL_MED of the layout
 constexpr uint32_t PULL_CH = 256;      // staged in-edges per warp step
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
@@ -1130,7 +1131,8 @@ __device__ __forceinline__ bool pull_commit(const DevState& st, uint32_t d, cons
 // concatenated (warp scan of in-degrees) and staged 256 at a time: lanes load
 // consecutive in_src entries (coalesced), gather the source values into
 // shared memory, then every lane folds its own slot's part of the stage in
-// ascending source order.  In-lists longer than K_PULL_HUB go to k_pull_hub.
+// ascending source order.  In-lists longer than K_PULL_MED go to k_pull_med
+// (up to K_PULL_HUB) and k_pull_hub.
 // The warp writes its 32 dirty bits as one word.
 template <int A, bool kList = false>
 __global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
@@ -1142,7 +1144,7 @@ __global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
     const uint32_t b = __ldg(&g.in_off[d]);
     uint32_t deg = __ldg(&g.in_off[d + 1]) - b;
     const bool has = deg > 0;
-    const bool hub = deg > K_PULL_HUB;
+    const bool hub = deg > K_PULL_MED;  // k_pull_med / k_pull_hub fold it
     if (hub) deg = 0;
     const uint32_t incl = warp_incl_scan(deg);
     const uint32_t excl = incl - deg;
@@ -1181,6 +1183,62 @@ __global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
     // S is a multiple of 256, so every warp of a block runs the same
     // iterations and the block-wide append is safe.
     if (kList) block_append(st.DL, st.lc + L_DL, dirty, d);
+  }
+}
+
+// Bit pattern of a fold's result (the value pull_commit stores).
+template <int A>
+__device__ __forceinline__ uint32_t pull_part(const PullAcc<A>& acc) {
+  if (A == A_PR_PULL) return __float_as_uint(__fsub_rn(acc.s, acc.c));
+  if (A == A_PR_DELTA) return __float_as_uint(acc.s);
+  return acc.best;
+}
+
+// Medium in-lists (more than K_PULL_MED, at most K_PULL_HUB in-edges): one
+// warp per destination; lane l folds the elements l, l+32, ... (coalesced),
+// then the 32 partials combine by a butterfly (a fixed order, so sums are
+// reproducible).  Keeps the per-lane fold of k_pull balanced: its longest
+// list is K_PULL_MED.  Runs after k_pull, whose dirty word for the slot is
+// already written: a dirty destination ORs its bit in.
+template <int A, bool kList = false>
+__global__ void __launch_bounds__(256) k_pull_med(DevGraph g, DevState st, const HubChunkD* meds, uint32_t n) {
+  const uint32_t lane = lane_id();
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += nw) {
+    const HubChunkD hc = meds[w];
+    PullAcc<A> acc;
+    uint32_t q = hc.e0 + lane;
+    for (; q + 3 * 32 < hc.e1; q += 4 * 32) {
+      uint32_t v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t e = q + u * 32;
+        v[u] = pull_value<A>(st, __ldg(&g.in_src[e]), A == A_SSSP_W ? __ldg(&g.in_wgt[e]) : 0u);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc.fold(v[u]);
+    }
+    for (; q < hc.e1; q += 32)
+      acc.fold(pull_value<A>(st, __ldg(&g.in_src[q]), A == A_SSSP_W ? __ldg(&g.in_wgt[q]) : 0u));
+    uint32_t part = pull_part<A>(acc);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const uint32_t other = __shfl_xor_sync(FULL, part, o);
+      if (A == A_PR_PULL || A == A_PR_DELTA)
+        part = __float_as_uint(__fadd_rn(__uint_as_float(part), __uint_as_float(other)));
+      else
+        part = min(part, other);
+    }
+    if (lane == 0) {
+      PullAcc<A> tot;
+      tot.fold(part);
+      if (pull_commit<A>(st, hc.slot, tot, true) && A != A_PR_PULL) {
+        if (kList)
+          mark_listed(st.MD, hc.slot, st.DL, st.lc + L_DL);
+        else
+          red_or(st.MD + (hc.slot >> 5), 1u << (hc.slot & 31));
+      }
+    }
   }
 }
 

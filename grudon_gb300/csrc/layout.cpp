@@ -211,8 +211,14 @@ void build_in_edges(Layout& L) {
     }
   }
   L.in_hubs.clear();
-  for (uint64_t s = 0; s < S; ++s)
-    if (L.in_off[s + 1] - L.in_off[s] > PULL_HUB) L.in_hubs.push_back(HubChunk{(uint32_t)s, L.in_off[s], L.in_off[s + 1]});
+  L.in_meds.clear();
+  for (uint64_t s = 0; s < S; ++s) {
+    const uint32_t d = L.in_off[s + 1] - L.in_off[s];
+    if (d > PULL_HUB)
+      L.in_hubs.push_back(HubChunk{(uint32_t)s, L.in_off[s], L.in_off[s + 1]});
+    else if (d > PULL_MED)
+      L.in_meds.push_back(HubChunk{(uint32_t)s, L.in_off[s], L.in_off[s + 1]});
+  }
 }
 
 }  // namespace grd

@@ -25,6 +25,7 @@ constexpr uint32_t INVALID = 0xFFFFFFFFu;
 constexpr uint32_t HUB_DEGREE = 2048;       // rows above this go to hub chunks
 constexpr uint32_t HUB_CHUNK = 4096;        // edges per hub work item
 constexpr uint32_t PULL_HUB = 1024;         // in-lists above this pull per block
+constexpr uint32_t PULL_MED = 64;           // in-lists above this (up to PULL_HUB) pull per warp
 
 struct HubChunk {
   uint32_t slot;   // global slot of the hub row
@@ -54,6 +55,7 @@ struct Layout {
   std::vector<uint32_t> in_src;  // [E]
   std::vector<uint32_t> in_wgt;  // [E]
   std::vector<HubChunk> in_hubs; // destinations with more than PULL_HUB in-edges
+  std::vector<HubChunk> in_meds; // destinations with PULL_MED+1 .. PULL_HUB in-edges
 
   std::vector<HubChunk> hubs;        // static hub work items (all partitions)
   std::vector<uint32_t> tile_part;   // [S/TILE_SLOTS] partition of each tile

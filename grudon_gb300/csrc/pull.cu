@@ -95,11 +95,14 @@ uint32_t sms(const grd_ctx* ctx, uint32_t per_sm) { return (uint32_t)ctx->num_sm
 
 int enqueue_pull_edge_map(grd_ctx* ctx) {
   k_pull<A_PR_PULL><<<sms(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+  if (ctx->pull.num_in_meds)
+    k_pull_med<A_PR_PULL><<<std::min<uint32_t>((ctx->pull.num_in_meds + 7) / 8, sms(ctx, 8)), 256, 0,
+                            ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_meds, ctx->pull.num_in_meds);
   if (ctx->pull.num_in_hubs)
     k_pull_hub<A_PR_PULL><<<std::min<uint32_t>(ctx->pull.num_in_hubs, sms(ctx, 8)), 256, 0, ctx->stream>>>(
         ctx->g, ctx->st, ctx->pull.in_hubs, ctx->pull.num_in_hubs);
   CK_LAUNCH();
-  ctx->stats.kernel_launches += ctx->pull.num_in_hubs ? 2 : 1;
+  ctx->stats.kernel_launches += 1 + (ctx->pull.num_in_meds ? 1 : 0) + (ctx->pull.num_in_hubs ? 1 : 0);
   ctx->stats.pull_rounds++;
   ctx->pull.edges += ctx->L.E;  // every in-edge is read once per iteration
   return GRD_OK;
