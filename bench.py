@@ -36,6 +36,10 @@ sys.path.insert(0, str(ROOT))
 METRIC = "GTEPS (PR/CC/SSSP, RMAT-24) & % HBM roofline; learned+batched vs plain GPU"
 SCALE, EF, NUM_MEMORY = 22, 16, 3
 RMAT_ABC = (0.57, 0.19, 0.19)
+# DRAM bytes (read + write) per edge of k_push_lbs in its ncu capture (CC
+# round 0 on RMAT-21, every vertex active): 249.9 MB for the 50.2 M edges of
+# non-hub rows.
+DRAM_BYTES_PER_PUSH_EDGE = 249.9e6 / 50.2e6
 
 
 def parse():
@@ -479,7 +483,8 @@ def main():
     for c in (ctx_cc, ctx_ss):
         c.set_profiling(True)
     prof = {"edge_map_ms": 0.0, "fwd_ms": 0.0, "bwd_ms": 0.0, "update_ms": 0.0, "rounds_ms": 0.0, "alg_bytes": 0.0,
-            "push_rounds": 0, "pull_rounds": 0}
+            "push_rounds": 0, "pull_rounds": 0, "lbs_ms": 0.0, "lbs_bytes": 0.0, "lbs_launches": 0,
+            "lbs_edges": 0}
     for _ in range(args.steps):
         for st, c, weighted, Eg in zip(step(host_loop=True), (ctx_cc, ctx_ss), (False, True),
                                         (G_cc.num_edges, G_ss.num_edges)):
@@ -492,6 +497,12 @@ def main():
                                   st["pull_rounds"] * (Eg * (8 + wb) + S * 8 + S / 8))
             prof["push_rounds"] += st["push_rounds"]
             prof["pull_rounds"] += st["pull_rounds"]
+            # the load-balanced push kernel alone: DP/RB/SV of each active,
+            # then per edge its column index (+ weight) and the destination peek
+            prof["lbs_ms"] += st["lbs_ms"]
+            prof["lbs_launches"] += st["lbs_launches"]
+            prof["lbs_edges"] += st["lbs_edges"]
+            prof["lbs_bytes"] += st["lbs_actives"] * 12 + st["lbs_edges"] * (8 + wb)
     for c in (ctx_cc, ctx_ss):
         c.set_profiling(False)
 
@@ -538,13 +549,21 @@ def main():
     if pk.exists():
         peaks = json.loads(pk.read_text())
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = prof["alg_bytes"] / (prof["edge_map_ms"] / 1e3) / 1e9 if prof["edge_map_ms"] > 0 else 0.0
-    roofline = {"bound": "hbm",
-                "kernel": "edge-map stage: push (k_deg_*, k_push_lbs, k_hub_push, k_diff_dirty) or pull "
-                          "(k_pull, k_pull_hub) per round",
-                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None,
-                "edge_map_share_of_rounds": prof["edge_map_ms"] / prof["rounds_ms"] if prof["rounds_ms"] else None,
+    stage_ach = prof["alg_bytes"] / (prof["edge_map_ms"] / 1e3) / 1e9 if prof["edge_map_ms"] > 0 else 0.0
+    nl = max(prof["lbs_launches"], 1)
+    lbs_ach = prof["lbs_bytes"] / (prof["lbs_ms"] / 1e3) / 1e9 if prof["lbs_ms"] > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": "k_push_lbs (load-balanced push edge-map)",
+                "achieved": lbs_ach, "peak": hbm_peak, "unit": "GB/s", "frac": lbs_ach / hbm_peak,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                # DRAM bytes per edge of the kernel in its ncu capture, times
+                # this run's average edges per launch
+                "traffic": DRAM_BYTES_PER_PUSH_EDGE * prof["lbs_edges"] / nl,
+                "alg_bytes_per_launch": prof["lbs_bytes"] / nl, "avg_launch_ms": prof["lbs_ms"] / nl,
+                "launches": prof["lbs_launches"],
+                "edge_map_stage": {"achieved": stage_ach, "frac": stage_ach / hbm_peak,
+                                   "kernels": "k_deg_*, k_push_lbs, k_hub_push, k_diff_dirty (push) or k_pull* (pull)",
+                                   "share_of_rounds": prof["edge_map_ms"] / prof["rounds_ms"]
+                                   if prof["rounds_ms"] else None},
                 "push_rounds_per_step": prof["push_rounds"] / args.steps,
                 "pull_rounds_per_step": prof["pull_rounds"] / args.steps,
                 "stage_ms_per_step": {k: prof[k] / args.steps for k in

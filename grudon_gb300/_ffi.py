@@ -56,7 +56,8 @@ class grd_stats(C.Structure):
                 ("bytes_synced", C.c_uint64), ("reference_bytes_moved", C.c_uint64),
                 ("last_residual", C.c_double), ("push_rounds", C.c_uint32), ("pull_rounds", C.c_uint32),
                 ("actives_total", C.c_uint64), ("kernel_launches", C.c_uint64), ("stage_ms", C.c_double * 5),
-                ("device_loop", C.c_uint32), ("push_actives", C.c_uint64)]
+                ("device_loop", C.c_uint32), ("push_actives", C.c_uint64), ("lbs_ms", C.c_double),
+                ("lbs_edges", C.c_uint64), ("lbs_actives", C.c_uint64), ("lbs_launches", C.c_uint64)]
 
 
 GRD_POLICY_FIXED, GRD_POLICY_LEARNED = 0, 1

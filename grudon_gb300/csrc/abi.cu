@@ -366,12 +366,15 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
     k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(ctx->st, B);
     k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
+    grd_prof_mark(ctx, 5);
     if (mode == RM_PUSH_BITVEC) {
       k_push_lbs<A, true><<<resident_grid(ctx, k_push_lbs<A, true>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      grd_prof_mark(ctx, 6);
       if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       k_diff_dirty<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     } else {
       k_push_lbs<A, false><<<resident_grid(ctx, k_push_lbs<A, false>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      grd_prof_mark(ctx, 6);
       if (ctx->g.num_hubs) k_hub_push<A, false><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     }
     CK_LAUNCH();
@@ -845,6 +848,16 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
         rec.unvisited_in = un_in;
         grd_prof_collect(ctx, rec.ms);
         ctx->round_log.push_back(rec);
+        if (branch == RM_PUSH_BITVEC || branch == RM_PUSH_LIST) {  // the push kernel ran this round
+          float ms = 0.0f;
+          if (cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]) == cudaSuccess) {
+            ctx->stats.lbs_ms += ms;
+            ctx->stats.lbs_edges += ctx->h_counters[C_MEDGES];
+            ctx->stats.lbs_actives += ctx->h_counters[C_ACTIVE];
+            ctx->stats.lbs_launches += 1;
+          }
+          (void)cudaGetLastError();
+        }
       }
       ctx->stats.rounds++;
       if (f == 0) break;

@@ -52,7 +52,9 @@ struct grd_ctx {
   uint32_t* agg_buf = nullptr; // staging of grd_aggregate_values (gids, values)
   size_t agg_cap = 0;
   bool profiling = false;
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // profiling events: [0..4] bracket the stages of a round, [5..6] the
+  // load-balanced push kernel
+  cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<void*> host_registered;  // layout arrays pinned for H2D uploads
   std::vector<uint32_t> own_slot_host;  // gid -> owned global slot (uploaded)
   grd_policy_model* policy_dev = nullptr;  // learned round policy (device copy)

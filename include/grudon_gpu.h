@@ -124,6 +124,11 @@ typedef struct grd_stats {
                                  launch (device-driven loop), 0 if the host
                                  drove the rounds                          */
   uint64_t push_actives;      /* actives_total restricted to push rounds   */
+  /* With profiling, host-driven rounds: the load-balanced push kernel alone
+   * (CUDA events around each launch), the edges of non-hub rows it ran and
+   * the actives of its rounds. */
+  double lbs_ms;
+  uint64_t lbs_edges, lbs_actives, lbs_launches;
 } grd_stats;
 
 typedef struct grd_ctx grd_ctx;
