@@ -248,6 +248,15 @@ class Context:
         self._check(self._lib.grd_set_algo(self._ctx, algo, C.byref(p)))
         self.algo = algo
 
+    def verify(self) -> dict:
+        """The reference's verify() checks on the device for the algorithm
+        last run (grd_verify): CC/SSSP edge invariants, PageRank top ranks."""
+        r = _ffi.grd_verify_result()
+        self._check(self._lib.grd_verify(self._ctx, C.byref(r)))
+        n = r.num_top
+        return {"errors": r.errors, "edges_checked": r.edges_checked, "count": r.count, "max_value": r.max_value,
+                "top_ids": list(r.top_ids[:n]), "top_values": list(r.top_values[:n])}
+
     def set_policy(self, model) -> None:
         """Uploads a learned round-policy model (a grd_policy_model, or None
         to clear it)."""

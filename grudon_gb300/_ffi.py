@@ -79,6 +79,15 @@ class grd_policy_train_cfg(C.Structure):
                 ("device", C.c_int)]
 
 
+GRD_VERIFY_TOPK = 20
+
+
+class grd_verify_result(C.Structure):
+    _fields_ = [("errors", C.c_uint64), ("edges_checked", C.c_uint64), ("count", C.c_uint64),
+                ("max_value", C.c_uint64), ("num_top", C.c_uint32), ("top_ids", C.c_uint32 * GRD_VERIFY_TOPK),
+                ("top_values", C.c_float * GRD_VERIFY_TOPK)]
+
+
 class grd_round_rec(C.Structure):
     _fields_ = [("round", C.c_uint32), ("mode", C.c_int32), ("frontier_in", C.c_uint64), ("actives", C.c_uint64),
                 ("edges", C.c_uint64), ("frontier_out", C.c_uint64), ("ms", C.c_double * 5),
@@ -117,6 +126,7 @@ SIGNATURES = {
     "grd_policy_predict": (C.c_int, [C.POINTER(grd_policy_model), f32p, C.c_size_t, C.c_uint32, C.c_int, f32p,
                                      C.POINTER(C.c_int32)]),
     "grd_policy_error": (C.c_char_p, []),
+    "grd_verify": (C.c_int, [C.c_void_p, C.POINTER(grd_verify_result)]),
     "grd_policy_load": (C.c_int, [C.c_char_p, C.POINTER(grd_policy_model)]),
     "grd_policy_save": (C.c_int, [C.c_char_p, C.POINTER(grd_policy_model)]),
     "grd_run": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(grd_stats)]),

@@ -58,6 +58,8 @@ struct grd_ctx {
   std::vector<void*> host_registered;  // layout arrays pinned for H2D uploads
   std::vector<uint32_t> own_slot_host;  // gid -> owned global slot (uploaded)
   grd_policy_model* policy_dev = nullptr;  // learned round policy (device copy)
+  unsigned long long* verify_buf = nullptr;  // grd_verify per-block top ranks
+  size_t verify_cap = 0;
   bool has_policy = false;
 };
 

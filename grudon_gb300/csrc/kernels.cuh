@@ -50,7 +50,8 @@ enum Counter : int {
   C_FMAXDEG = 17,    // largest out-degree in the frontier
   C_UNVISITED = 18,  // SSSP: out-edges of vertices not reached yet
   C_DONE = 19,       // finished-block count of k_update_list (last-block reset)
-  NUM_COUNTERS = 20
+  C_VERIFY = 20,     // [4] grd_verify accumulators
+  NUM_COUNTERS = 24
 };
 
 struct HubChunkD {

@@ -9,8 +9,9 @@
 //                        kernel, so apply_updates() has nothing left to do
 //                        (pr.cpp:63-147, cc.cpp:86-107, sssp.cpp:92-113)
 //   aggregate()       -> grd_aggregate_values        (pr.cpp:149-153, cc.cpp:109-113, sssp.cpp:115-119)
-//   verify()          -> the reference's invariants, checked on the host
-//                        (cc.cpp:139-177, sssp.cpp:145-189, pr.cpp:179-205)
+//   verify()          -> the reference's invariants, checked on the device by
+//                        grd_verify (cc.cpp:139-177, sssp.cpp:145-189,
+//                        pr.cpp:179-205)
 // Supported value types are the ones the GPU computes in: PageRank<float>,
 // CC<uint32_t>, SSSP<uint32_t>.
 #pragma once
@@ -77,13 +78,10 @@ class PageRank : public GraphAlgorithm<VertexProperty> {
   }
   // Top 20 PageRank values.
   void verify() override {
-    std::vector<float> r = ranks();
-    std::vector<uint32_t> idx(r.size());
-    for (uint32_t i = 0; i < idx.size(); ++i) idx[i] = i;
-    const size_t k = std::min<size_t>(20, idx.size());
-    std::partial_sort(idx.begin(), idx.begin() + k, idx.end(), [&](uint32_t a, uint32_t b) { return r[a] > r[b]; });
+    grd_verify_result r{};
+    check(grd_verify(this->ctx(), &r), this->ctx(), "grd_verify");
     std::printf("Top 20 PageRank Values:\n");
-    for (size_t i = 0; i < k; ++i) std::printf("Node: %u, PR: %g\n", idx[i], r[idx[i]]);
+    for (uint32_t i = 0; i < r.num_top; ++i) std::printf("Node: %u, PR: %g\n", r.top_ids[i], r.top_values[i]);
   }
 };
 
@@ -116,16 +114,14 @@ class CC : public GraphAlgorithm<VertexProperty> {
     for (uint32_t n = 0; n < l.size(); ++n) std::printf("Vertex/Dist: %u/%u\n", n, l[n]);
   }
   // Every edge's endpoints carry the same label; returns via the count.
-  void verify() override { errors = count_errors(); }
-  uint64_t count_errors() {
-    std::vector<uint32_t> l = labels();
-    const grd_host_graph& g = this->graph->host();
-    uint64_t bad = 0;
-    for (uint32_t u = 0; u < g.num_vertices; ++u)
-      for (uint64_t i = g.row_offsets[u]; i < g.row_offsets[u + 1]; ++i) bad += l[u] != l[g.col_indices[i]];
-    return bad;
+  // Edges whose endpoints hold different labels, counted on the device.
+  void verify() override {
+    grd_verify_result r{};
+    check(grd_verify(this->ctx(), &r), this->ctx(), "grd_verify");
+    errors = r.errors;
+    components = r.count;
   }
-  uint64_t errors = 0;
+  uint64_t errors = 0, components = 0;
 };
 
 template <typename VertexProperty>
@@ -162,21 +158,14 @@ class SSSP : public GraphAlgorithm<VertexProperty> {
   }
   // dist[dst] <= dist[src] + w(src,dst) for every reached src; also the
   // reference's max distance and visited count.
+  // Edge relaxation invariant, reached count and largest distance, on the
+  // device.
   void verify() override {
-    std::vector<uint32_t> d = distances();
-    const grd_host_graph& g = this->graph->host();
-    errors = 0;
-    max_dist = 0;
-    visited = 0;
-    for (uint32_t u = 0; u < g.num_vertices; ++u) {
-      if (d[u] == std::numeric_limits<uint32_t>::max()) continue;
-      for (uint64_t i = g.row_offsets[u]; i < g.row_offsets[u + 1]; ++i) {
-        uint64_t w = weighted ? g.weights[i] : 1;
-        errors += (uint64_t)d[g.col_indices[i]] > (uint64_t)d[u] + w;
-      }
-      ++visited;
-      max_dist = std::max(max_dist, d[u]);
-    }
+    grd_verify_result r{};
+    check(grd_verify(this->ctx(), &r), this->ctx(), "grd_verify");
+    errors = r.errors;
+    visited = r.count;
+    max_dist = (uint32_t)r.max_value;
     std::printf("Max Dist: %u\nTotal Visited Dist: %llu\n", max_dist, (unsigned long long)visited);
   }
   bool weighted;

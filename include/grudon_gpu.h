@@ -305,6 +305,29 @@ int grd_write_partition_file(const uint32_t* part, uint32_t n, const char* path)
 int grd_read_partition_file(const char* path, uint32_t n, uint32_t num_memory,
                             uint32_t* part);
 
+/* Validators ----------------------------------------------------------------
+ * The reference's verify() checks (cc.cpp:139-177, sssp.cpp:145-189,
+ * pr.cpp:179-205) as device kernels over the resident graph, for the
+ * algorithm last run on the ctx:
+ *   CC    errors = edges whose endpoints hold different labels;
+ *         count = components (vertices that are their own label);
+ *   SSSP  errors = edges (u,v) with u reached and dist[v] > dist[u] + w
+ *         (w = 1 for the hop count); count = reached vertices ("Total
+ *         Visited Dist"); max_value = largest distance ("Max Dist");
+ *   PR    the GRD_VERIFY_TOPK largest pr_vals, descending (ties: lower gid
+ *         first). */
+#define GRD_VERIFY_TOPK 20
+typedef struct grd_verify_result {
+  uint64_t errors;
+  uint64_t edges_checked;
+  uint64_t count;
+  uint64_t max_value;
+  uint32_t num_top;
+  uint32_t top_ids[GRD_VERIFY_TOPK];
+  float top_values[GRD_VERIFY_TOPK];
+} grd_verify_result;
+int grd_verify(grd_ctx* ctx, grd_verify_result* out);
+
 /* Learned round policy ----------------------------------------------------
  * No reference counterpart: the reference's only per-round decision engine
  * is the disabled NDP/INC offload rule (include/offload_engine/

@@ -84,3 +84,59 @@ def test_cli_plugin_api_matches_oracle(gpu, tmp_path, algo, schedule):
         assert iters == ref["stats"]["rounds"]
         moved = int([ln for ln in r.stdout.splitlines() if "TotalBytesMoved" in ln][0].split()[-1])
         assert moved == ref["stats"]["reference_bytes_moved"]
+
+
+def _host_violations(G, labels, kind):
+    ro = G.row_offsets.astype(np.int64)
+    src = np.repeat(np.arange(G.num_vertices), np.diff(ro))
+    dst = G.col_indices.astype(np.int64)
+    lu, lv = labels[src].astype(np.uint64), labels[dst].astype(np.uint64)
+    if kind == "cc":
+        return int(np.count_nonzero(lu != lv))
+    w = G.weights.astype(np.uint64) if kind == "sssp_w" else np.ones(len(dst), dtype=np.uint64)
+    reach = lu != 0xFFFFFFFF
+    return int(np.count_nonzero(reach & (lv > lu + w)))
+
+
+def test_device_verify(gpu):
+    """grd_verify: the reference's verify() invariants on the device, checked
+    against host counts, including on deliberately broken labels."""
+    Gs = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
+    part = Gs.partition_edge_balanced(3)
+    with g.Context(Gs, part, 3) as ctx:
+        ctx.set_algo(g.GRD_CC)
+        ctx.init()
+        ctx.run()
+        lab = ctx.read_props()
+        r = ctx.verify()
+        assert r["errors"] == 0 and r["edges_checked"] == Gs.num_edges
+        assert r["count"] == len(np.unique(lab))
+        # break one label through the aggregate + update stages
+        gid = int(np.flatnonzero(lab != 0)[0])
+        gids, vals = np.array([gid], dtype=np.uint32), np.array([0], dtype=np.uint32)
+        assert ctx._lib.grd_aggregate_values(ctx._ctx, gids.ctypes.data_as(g._ffi.u32p),
+                                             vals.ctypes.data_as(g._ffi.u32p), 1) == 0
+        ctx.update()
+        lab2 = ctx.read_props()
+        assert lab2[gid] == 0
+        r = ctx.verify()
+        assert r["errors"] == _host_violations(Gs, lab2, "cc") > 0
+    Gd = g.Graph.rmat(12, 8, weighted=True)
+    with g.Context(Gd, Gd.partition_edge_balanced(3), 3) as ctx:
+        for algo, kind in ((g.GRD_SSSP_W, "sssp_w"), (g.GRD_SSSP_HOP, "sssp")):
+            ctx.set_algo(algo)
+            ctx.init()
+            ctx.run()
+            d = ctx.read_props()
+            r = ctx.verify()
+            fin = d[d != 0xFFFFFFFF]
+            assert r["errors"] == 0 and r["count"] == len(fin) and r["max_value"] == int(fin.max())
+            assert r["edges_checked"] == int(np.diff(Gd.row_offsets.astype(np.int64))[d != 0xFFFFFFFF].sum())
+        ctx.set_algo(g.GRD_PR_DELTA)
+        ctx.init()
+        ctx.run()
+        ranks = ctx.read_ranks()
+        r = ctx.verify()
+        order = np.lexsort((np.arange(len(ranks)), -ranks.astype(np.float64)))[:20]
+        assert r["top_ids"] == [int(i) for i in order]
+        np.testing.assert_array_equal(np.array(r["top_values"], dtype=np.float32), ranks[order])
