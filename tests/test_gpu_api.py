@@ -101,7 +101,9 @@ def _host_violations(G, labels, kind):
 def test_device_verify(gpu):
     """grd_verify: the reference's verify() invariants on the device, checked
     against host counts, including on deliberately broken labels."""
-    Gs = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
+    from grudon_gb300.batch import Union
+    # two disjoint RMAT graphs: the second one's labels are all above 0
+    Gs = Union([g.Graph.rmat(11, 8, symmetrize=True, weighted=True)] * 2).graph
     part = Gs.partition_edge_balanced(3)
     with g.Context(Gs, part, 3) as ctx:
         ctx.set_algo(g.GRD_CC)
@@ -112,7 +114,8 @@ def test_device_verify(gpu):
         assert r["errors"] == 0 and r["edges_checked"] == Gs.num_edges
         assert r["count"] == len(np.unique(lab))
         # break one label through the aggregate + update stages
-        gid = int(np.flatnonzero(lab != 0)[0])
+        deg = np.diff(Gs.row_offsets.astype(np.int64))
+        gid = int(np.flatnonzero((lab != 0) & (deg > 0))[0])
         gids, vals = np.array([gid], dtype=np.uint32), np.array([0], dtype=np.uint32)
         assert ctx._lib.grd_aggregate_values(ctx._ctx, gids.ctypes.data_as(g._ffi.u32p),
                                              vals.ctypes.data_as(g._ffi.u32p), 1) == 0
