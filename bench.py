@@ -395,9 +395,9 @@ def main():
     ctx_ss = g.Context(G_ss, p_ss, num_memory=NUM_MEMORY, device=local)
     model = load_policy_model()
 
-    def set_policy(policy):
+    def set_policy(policy, offload=g.GRD_OFFLOAD_NDP):
         for c, a in ((ctx_cc, g.GRD_CC), (ctx_ss, g.GRD_SSSP_W)):
-            c.set_algo(a, policy=policy)
+            c.set_algo(a, policy=policy, offload=offload)
             c.set_policy(model if policy == g.GRD_POLICY_LEARNED else None)
 
     # The headline runs the library's default schedule, the fixed threshold
@@ -544,6 +544,24 @@ def main():
             outs.append([(c.init(), c.run(), c.read_props())[2] for c in (ctx_cc, ctx_ss)])
         results_identical = all(bool((a == b).all()) for a, b in zip(*outs))
 
+    # The reference's offload engine (NDPEngine: NO_OFFLOAD rounds, the
+    # compute partition pushing over the shipped adjacency, when the frontier
+    # holds at most V/20 vertices) against the all-NDP_OFFLOAD schedule it
+    # hard-codes, both with the fixed rule, timed back to back on the same
+    # contexts; results must be bit-identical.
+    set_policy(g.GRD_POLICY_FIXED)
+    ndp_run = summary(*timed())
+    base_props = [(c.init(), c.run(), c.read_props())[2] for c in (ctx_cc, ctx_ss)]
+    set_policy(g.GRD_POLICY_FIXED, g.GRD_OFFLOAD_ENGINE)
+    eng_run = summary(*timed())
+    sts = [(c.init(), c.run())[1] for c in (ctx_cc, ctx_ss)]
+    off_props = [c.read_props() for c in (ctx_cc, ctx_ss)]
+    offload = {"ndp": ndp_run,
+               "engine": eng_run | {"no_offload_rounds_per_step": [st["no_offload_rounds"] for st in sts]},
+               "engine_speedup_vs_ndp": eng_run["value"] / ndp_run["value"],
+               "results_bit_identical": all(bool((a == b).all()) for a, b in zip(base_props, off_props))}
+    set_policy(policy)
+
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -587,6 +605,7 @@ def main():
                        "learned_speedup_vs_fixed": (runs["learned"]["value"] / runs["fixed"]["value"])
                        if "learned" in runs else None,
                        "results_bit_identical": results_identical},
+            "offload": offload,
         }
         if ws == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(G_cc, G_ss, p_cc, p_ss)

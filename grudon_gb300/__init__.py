@@ -16,14 +16,16 @@ from . import _ffi
 from ._ffi import (GRD_CC, GRD_DIR_AUTO, GRD_DIR_PULL, GRD_DIR_PUSH, GRD_FMT_AUTO, GRD_FMT_BITVEC,
                    GRD_FMT_LIST, GRD_PR_DELTA, GRD_PR_PULL, GRD_ROUND_PULL_BITVEC, GRD_ROUND_PULL_LIST,
                    GRD_ROUND_PUSH_BITVEC, GRD_ROUND_PUSH_LIST, GRD_RUN_STRICT, GRD_SSSP_HOP, GRD_SSSP_W,
-                   GRD_POLICY_FIXED, GRD_POLICY_LEARNED)
+                   GRD_POLICY_FIXED, GRD_POLICY_LEARNED, GRD_ROUND_NO_OFFLOAD, GRD_OFFLOAD_NDP,
+                   GRD_OFFLOAD_ENGINE, GRD_OFFLOAD_NONE)
 
 __all__ = [
     "GrdError", "Graph", "Context", "lib", "device_count", "rmat_seed",
     "GRD_PR_DELTA", "GRD_PR_PULL", "GRD_CC", "GRD_SSSP_HOP", "GRD_SSSP_W",
     "GRD_DIR_AUTO", "GRD_DIR_PUSH", "GRD_DIR_PULL", "GRD_FMT_AUTO", "GRD_FMT_BITVEC", "GRD_FMT_LIST",
     "GRD_ROUND_PUSH_BITVEC", "GRD_ROUND_PUSH_LIST", "GRD_ROUND_PULL_BITVEC", "GRD_ROUND_PULL_LIST",
-    "GRD_POLICY_FIXED", "GRD_POLICY_LEARNED", "GRD_RUN_STRICT", "ALGO_NAMES",
+    "GRD_POLICY_FIXED", "GRD_POLICY_LEARNED", "GRD_RUN_STRICT", "ALGO_NAMES", "GRD_ROUND_NO_OFFLOAD",
+    "GRD_OFFLOAD_NDP", "GRD_OFFLOAD_ENGINE", "GRD_OFFLOAD_NONE",
 ]
 
 ALGO_NAMES = {"pr": GRD_PR_DELTA, "pr_delta": GRD_PR_DELTA, "pr_pull": GRD_PR_PULL, "cc": GRD_CC,
@@ -236,15 +238,20 @@ class Context:
     def set_algo(self, algo, source: int = 0, max_rounds: int = 1000, damping: float = 0.85,
                  tolerance: Optional[float] = None, direction: int = GRD_DIR_AUTO,
                  frontier_format: int = GRD_FMT_AUTO, dense_div: int = 0, pull_div: int = 0,
-                 push_blocks_per_sm: int = 0, policy: int = _ffi.GRD_POLICY_FIXED) -> None:
+                 push_blocks_per_sm: int = 0, policy: int = _ffi.GRD_POLICY_FIXED,
+                 offload: int = GRD_OFFLOAD_NDP) -> None:
         """policy=GRD_POLICY_LEARNED picks each round's mode with the model
-        given to set_policy (the fixed rule while none is set)."""
+        given to set_policy (the fixed rule while none is set).  offload:
+        GRD_OFFLOAD_NDP (every round in the memory partitions, the
+        reference's choice), GRD_OFFLOAD_ENGINE (the NDPEngine rule per
+        round) or GRD_OFFLOAD_NONE (every round pushed by the compute
+        partition over the shipped adjacency)."""
         if isinstance(algo, str):
             algo = ALGO_NAMES[algo]
         if tolerance is None:
             tolerance = 1e-7 if algo == GRD_PR_PULL else 1e-6
         p = _ffi.grd_params(source, max_rounds, damping, tolerance, direction, frontier_format, dense_div, pull_div,
-                            push_blocks_per_sm, policy)
+                            push_blocks_per_sm, policy, offload)
         self._check(self._lib.grd_set_algo(self._ctx, algo, C.byref(p)))
         self.algo = algo
 

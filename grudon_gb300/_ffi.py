@@ -25,6 +25,8 @@ GRD_SSSP_W = 4
 GRD_DIR_AUTO, GRD_DIR_PUSH, GRD_DIR_PULL = 0, 1, 2
 GRD_FMT_AUTO, GRD_FMT_BITVEC, GRD_FMT_LIST = 0, 1, 2
 GRD_ROUND_PUSH_BITVEC, GRD_ROUND_PUSH_LIST, GRD_ROUND_PULL_BITVEC, GRD_ROUND_PULL_LIST = 0, 1, 2, 3
+GRD_ROUND_NO_OFFLOAD = 5
+GRD_OFFLOAD_NDP, GRD_OFFLOAD_ENGINE, GRD_OFFLOAD_NONE = 0, 1, 2
 GRD_RUN_STRICT = 1
 GRD_RUN_HOST_LOOP = 2
 
@@ -48,7 +50,7 @@ class grd_params(C.Structure):
     _fields_ = [("source", C.c_uint32), ("max_rounds", C.c_uint32), ("damping", C.c_double),
                 ("tolerance", C.c_double), ("direction", C.c_int), ("frontier_format", C.c_int),
                 ("dense_div", C.c_uint32), ("pull_div", C.c_uint32), ("push_blocks_per_sm", C.c_uint32),
-                ("policy", C.c_int)]
+                ("policy", C.c_int), ("offload", C.c_int)]
 
 
 class grd_stats(C.Structure):
@@ -57,7 +59,8 @@ class grd_stats(C.Structure):
                 ("last_residual", C.c_double), ("push_rounds", C.c_uint32), ("pull_rounds", C.c_uint32),
                 ("actives_total", C.c_uint64), ("kernel_launches", C.c_uint64), ("stage_ms", C.c_double * 5),
                 ("device_loop", C.c_uint32), ("push_actives", C.c_uint64), ("lbs_ms", C.c_double),
-                ("lbs_edges", C.c_uint64), ("lbs_actives", C.c_uint64), ("lbs_launches", C.c_uint64)]
+                ("lbs_edges", C.c_uint64), ("lbs_actives", C.c_uint64), ("lbs_launches", C.c_uint64),
+                ("no_offload_rounds", C.c_uint32)]
 
 
 GRD_POLICY_FIXED, GRD_POLICY_LEARNED = 0, 1

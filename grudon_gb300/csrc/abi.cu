@@ -244,6 +244,7 @@ bool use_pull(const grd_ctx* ctx) {
 }  // namespace
 
 int grd_choose_round_mode(const grd_ctx* ctx) {
+  if (policy_no_offload(ctx->params.offload, ctx->last_frontier, ctx->g.V)) return RM_NO_OFFLOAD;
   const bool pull = use_pull(ctx), list = !use_dense(ctx);
   return pull ? (list ? RM_PULL_LIST : RM_PULL_BITVEC) : (list ? RM_PUSH_LIST : RM_PUSH_BITVEC);
 }
@@ -255,6 +256,7 @@ PolicyArgs grd_policy_args(const grd_ctx* ctx) {
   a.has_in = ctx->in_edges_alloc ? 1 : 0;
   a.dense_div = ctx->params.dense_div;
   a.pull_div = ctx->params.pull_div;
+  a.offload = ctx->params.offload;
   a.edges = ctx->L.E;
   a.round = ctx->stats.rounds;
   return a;
@@ -268,8 +270,8 @@ const grd_policy_model* grd_policy_model_dev(const grd_ctx* ctx) {
 // loop runs (so both loops choose identically), read back.
 static int host_loop_mode(grd_ctx* ctx, int* mode) {
   const grd_policy_model* m = grd_policy_model_dev(ctx);
-  if (!m) {
-    *mode = grd_choose_round_mode(ctx);
+  if (!m || policy_no_offload(ctx->params.offload, ctx->last_frontier, ctx->g.V)) {
+    *mode = grd_choose_round_mode(ctx);  // k_policy decides the offload the same way
     return GRD_OK;
   }
   const PolicyArgs a = grd_policy_args(ctx);
@@ -306,12 +308,13 @@ int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
   if (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)
     return 1 + (ctx->pull.num_in_meds ? 1 : 0) + (ctx->pull.num_in_hubs ? 1 : 0);
-  return 4 + (ctx->g.num_hubs ? 1 : 0) + (mode == RM_PUSH_BITVEC ? 1 : 0);
+  return 4 + (ctx->g.num_hubs ? 1 : 0) + (mode == RM_PUSH_BITVEC ? 1 : 0);  // push, NO_OFFLOAD too
 }
 
 // Kernels of a whole round in each mode (edge-map + syncs + update).
 uint32_t grd_round_launches(const grd_ctx* ctx, int mode) {
-  if (mode == RM_PUSH_TINY) return 1;
+  if (mode == RM_PUSH_TINY || mode == RM_NOOFF_TINY) return 1;
+  if (mode == RM_NO_OFFLOAD) return 3 /*fwd list, retire, update list*/ + grd_edge_map_launches(ctx, mode);
   const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
   const uint32_t groups = ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1;
   const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (3 /*fwd*/ + 2 + groups /*bwd*/ + 1 /*update*/);
@@ -372,6 +375,11 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
       grd_prof_mark(ctx, 6);
       if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       k_diff_dirty<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    } else if (mode == RM_NO_OFFLOAD) {  // compute-side push into vertex_updates
+      k_push_lbs<A, false, true><<<resident_grid(ctx, k_push_lbs<A, false, true>), 256, 0, ctx->stream>>>(ctx->g,
+                                                                                                          ctx->st);
+      grd_prof_mark(ctx, 6);
+      if (ctx->g.num_hubs) k_hub_push<A, false, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     } else {
       k_push_lbs<A, false><<<resident_grid(ctx, k_push_lbs<A, false>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       grd_prof_mark(ctx, 6);
@@ -446,20 +454,48 @@ int grd_enqueue_bwd_update_list(grd_ctx* ctx) {
   });
 }
 
+// NO_OFFLOAD round after its edge-map: retire the old frontier and count the
+// shipped adjacency, then the update over the updated-gid list.
+static int enqueue_retire_update_list(grd_ctx* ctx) {
+  return dispatch(ctx->algo, [&](auto a) -> int {
+    constexpr int A = decltype(a)::value;
+    k_retire_list<A><<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    grd_prof_mark(ctx, 3);
+    k_update_list<A><<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
+                                                                ctx->params.damping);
+    CK_LAUNCH();
+    return GRD_OK;
+  });
+}
+
 // One whole round in a given mode (host loop and loop-graph branches).
 int grd_enqueue_round(grd_ctx* ctx, int mode) {
-  if (mode == RM_PUSH_TINY) {  // the whole round counts as edge-map time
+  if (mode == RM_PUSH_TINY || mode == RM_NOOFF_TINY) {  // the whole round counts as edge-map time
     grd_prof_mark(ctx, 1);
     TRY(dispatch(ctx->algo, [&](auto a) -> int {
       constexpr int A = decltype(a)::value;
-      k_round_tiny<A><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
-                                                             ctx->params.damping);
+      if (mode == RM_NOOFF_TINY)
+        k_round_tiny<A, true><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
+                                                                     ctx->params.damping);
+      else
+        k_round_tiny<A><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
+                                                               ctx->params.damping);
       CK_LAUNCH();
       return GRD_OK;
     }));
     grd_prof_mark(ctx, 2);
     grd_prof_mark(ctx, 3);
     ctx->stats.kernel_launches += 1;
+    return GRD_OK;
+  }
+  if (mode == RM_NO_OFFLOAD) {
+    const uint64_t launches = ctx->stats.kernel_launches;
+    TRY(grd_enqueue_fwd_list(ctx));
+    grd_prof_mark(ctx, 1);
+    TRY(grd_enqueue_edge_map_mode(ctx, mode));
+    grd_prof_mark(ctx, 2);
+    TRY(enqueue_retire_update_list(ctx));
+    ctx->stats.kernel_launches = launches + grd_round_launches(ctx, mode);
     return GRD_OK;
   }
   const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
@@ -645,6 +681,14 @@ int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
     return GRD_E_INVALID;
   }
   if (p.pull_div == 0) p.pull_div = 2;
+  if (p.offload != GRD_OFFLOAD_NDP && p.offload != GRD_OFFLOAD_ENGINE && p.offload != GRD_OFFLOAD_NONE) {
+    ctx->err = "unknown offload setting";
+    return GRD_E_INVALID;
+  }
+  if (algo == GRD_PR_PULL && p.offload != GRD_OFFLOAD_NDP) {
+    ctx->err = "PR_PULL runs every round in the memory partitions (offload must be GRD_OFFLOAD_NDP)";
+    return GRD_E_INVALID;
+  }
   if (p.push_blocks_per_sm > 32) {
     ctx->err = "push_blocks_per_sm must be <= 32";
     return GRD_E_INVALID;
@@ -832,6 +876,7 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
         ctx->pull.edges += ctx->L.E;
       } else {
         ctx->stats.push_rounds++;
+        if (mode == RM_NO_OFFLOAD) ctx->stats.no_offload_rounds++;
       }
       TRY(grd_read_counters(ctx));
       f = ctx->h_counters[C_FRONTIER];
@@ -1041,8 +1086,8 @@ int grd_ctx_init_device(grd_ctx* ctx) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-  CK(cudaMallocHost((void**)&ctx->h_counters, sizeof(unsigned long long) * (NUM_COUNTERS + 8)));
-  std::memset(ctx->h_counters, 0, sizeof(unsigned long long) * (NUM_COUNTERS + 8));
+  CK(cudaMallocHost((void**)&ctx->h_counters, sizeof(unsigned long long) * (NUM_COUNTERS + 16)));
+  std::memset(ctx->h_counters, 0, sizeof(unsigned long long) * (NUM_COUNTERS + 16));
   ctx->h_seed = ctx->h_counters + NUM_COUNTERS;
   TRY(alloc_and_upload(ctx));
   // gid -> owned global slot (the first n_owned slots of each partition).

@@ -6,6 +6,8 @@
 //   --policy fixed|learned [--policy-model FILE]  --frontier auto|bitvec|list
 //   --direction auto|push|pull   (any of these: the rounds run as one
 //   device-driven loop with that per-round schedule)
+//   --offload ndp|engine|none    per-round offload decision (default ndp,
+//   the reference's; engine = its NDPEngine rule)
 // Runs one algorithm through the GraphAlgorithm plugin API on GPU 0 and
 // prints the reference's statistics (Iterations, TotalBytesMoved).
 #include <cstdio>
@@ -21,7 +23,7 @@ static void usage() {
   std::printf(
       "usage: grudon -g GRAPH -c 1 -m M [-p PARTFILE] [-a pr|cc|sssp|sssp_w] [--max-rounds N] [--verify] [--print]\n"
       "              [--policy fixed|learned] [--policy-model FILE] [--frontier auto|bitvec|list]\n"
-      "              [--direction auto|push|pull]\n");
+      "              [--direction auto|push|pull] [--offload ndp|engine|none]\n");
 }
 
 int main(int argc, char** argv) {
@@ -29,7 +31,7 @@ int main(int argc, char** argv) {
   size_t num_compute = 0, num_memory = 0;
   uint32_t max_rounds = MAX_ITERATIONS;
   bool do_verify = false, do_print = false, scheduled = false;
-  int direction = GRD_DIR_AUTO, format = GRD_FMT_AUTO, policy = GRD_POLICY_FIXED;
+  int direction = GRD_DIR_AUTO, format = GRD_FMT_AUTO, policy = GRD_POLICY_FIXED, offload = GRD_OFFLOAD_NDP;
   std::string model_path;
   for (int i = 1; i < argc; ++i) {
     std::string a = argv[i];
@@ -62,6 +64,13 @@ int main(int argc, char** argv) {
         usage();
         return 1;
       }
+    } else if (a == "--offload") {
+      const std::string v = next();
+      if (v != "ndp" && v != "engine" && v != "none") {
+        usage();
+        return 1;
+      }
+      offload = v == "engine" ? GRD_OFFLOAD_ENGINE : v == "none" ? GRD_OFFLOAD_NONE : GRD_OFFLOAD_NDP;
     } else if (a == "--policy-model") model_path = next();
     else if (a == "--verify") do_verify = true;
     else if (a == "--print") do_print = true;
@@ -97,6 +106,7 @@ int main(int argc, char** argv) {
   }
   auto schedule = [&](auto& alg) {
     if (scheduled) alg.setSchedule(direction, format, policy, has_model ? &model : nullptr);
+    alg.setOffload(offload);
   };
   try {
     GpuCore net(0);

@@ -35,7 +35,7 @@ struct grd_ctx {
   bool inited = false;
   grd_stats stats{};
   std::string err;
-  unsigned long long* h_counters = nullptr;  // pinned, NUM_COUNTERS + 8 entries
+  unsigned long long* h_counters = nullptr;  // pinned, NUM_COUNTERS + 16 entries
   unsigned long long* h_seed = nullptr;      // = h_counters + NUM_COUNTERS
   uint64_t upload_bytes = 0;
   bool in_edges_alloc = false;
@@ -46,7 +46,7 @@ struct grd_ctx {
   int last_mode = -1;          // edge-map mode of the round in flight (host loop)
   cudaGraph_t run_graph = nullptr;     // device-driven round loop (graph_run.cu)
   cudaGraphExec_t run_exec = nullptr;
-  cudaGraphExec_t round_exec[5] = {};  // one round per branch (profiled host loop)
+  cudaGraphExec_t round_exec[7] = {};  // one round per branch (profiled host loop)
   bool graph_failed = false;           // building it failed here: host loop
   std::string graph_error;
   uint32_t* agg_buf = nullptr; // staging of grd_aggregate_values (gids, values)
@@ -110,13 +110,18 @@ enum RoundMode {
   NUM_ROUND_MODES = 4,
   // push + list for a frontier small enough for one CTA (k_round_tiny); an
   // implementation of RM_PUSH_LIST, chosen by size, not by the policy
-  RM_PUSH_TINY = 4,
-  NUM_BRANCHES = 5
+  RM_PUSH_TINY = grd::P_BRANCH_TINY,
+  // NO_OFFLOAD round (compute-side push over the shipped adjacency), and its
+  // one-CTA form for the same small frontiers
+  RM_NO_OFFLOAD = GRD_ROUND_NO_OFFLOAD,
+  RM_NOOFF_TINY = grd::P_BRANCH_NOOFF_TINY,
+  NUM_BRANCHES = 7
 };
+static_assert(RM_NO_OFFLOAD == 5, "branch index of the NO_OFFLOAD round");
+static_assert(sizeof(grd_ctx::round_exec) / sizeof(cudaGraphExec_t) == NUM_BRANCHES, "one graph per branch");
 // The branch that runs a round the policy gave `mode`.
 __host__ __device__ inline int rm_branch(int mode, unsigned long long frontier, unsigned long long fedges) {
-  return (mode == RM_PUSH_LIST && frontier <= grd::K_TINY_ACTIVE && fedges <= grd::K_TINY_EDGES) ? (int)RM_PUSH_TINY
-                                                                                                  : mode;
+  return grd::policy_branch(mode, frontier, fedges);
 }
 __host__ __device__ inline bool rm_is_pull(int m) { return m == RM_PULL_BITVEC || m == RM_PULL_LIST; }
 int grd_choose_round_mode(const grd_ctx* ctx);

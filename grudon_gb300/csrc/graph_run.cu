@@ -2,14 +2,16 @@
 //
 // Top level: a conditional WHILE node whose body is one round of
 // GraphAlgorithm::run (src/GraphAlgorithm.cpp:177-690):
-//   k_policy -> SWITCH {push+bitvector, push+list, pull+bitvector, pull+list}
-//   -> k_round_end
+//   k_policy -> SWITCH {push+bitvector, push+list, pull+bitvector, pull+list,
+//                       push+list in one CTA, NO_OFFLOAD, NO_OFFLOAD in one
+//                       CTA} -> k_round_end
 // where every branch is a whole round (forward sync, edge-map, backward sync
-// + aggregate, update) in that mode.  k_policy applies the direction /
-// frontier-format rule on the device (the frontier size of the previous
-// update is already there) and selects the branch; k_round_end counts the
-// round and keeps the loop going while the frontier is non-empty and the
-// round cap is not reached, so the loop is always bounded.  One graph launch
+// + aggregate, update) in that mode.  k_policy applies the offload decision
+// and the direction / frontier-format rule on the device (the frontier size
+// of the previous update is already there) and selects the branch;
+// k_round_end counts the round and keeps the loop going while the frontier
+// is non-empty and the round cap is not reached, so the loop is always
+// bounded.  One graph launch
 // runs the whole algorithm with no host round trip; the host reads the
 // counters once at the end.
 #include <cuda_runtime.h>
@@ -103,8 +105,12 @@ int build(grd_ctx* ctx) {
   const int rc_end = end_capture(ctx, loop_body);
   if (rc != GRD_OK) return rc;
   if (rc_end != GRD_OK) return rc_end;
+  const int offload = ctx->params.offload;
   for (int m = 0; m < NUM_BRANCHES; ++m) {
-    if (rm_is_pull(m) && !ctx->in_edges_alloc) continue;  // never selected: empty branch
+    // never selected: empty branch
+    if (rm_is_pull(m) && !ctx->in_edges_alloc) continue;
+    const bool nooff = m == RM_NO_OFFLOAD || m == RM_NOOFF_TINY;
+    if (nooff ? offload == GRD_OFFLOAD_NDP : offload == GRD_OFFLOAD_NONE) continue;
     TRY(capture_into(ctx, branches[m]));
     rc = grd_enqueue_round(ctx, m);
     const int e = end_capture(ctx, branches[m]);
@@ -187,7 +193,10 @@ int grd_graph_run(grd_ctx* ctx, bool* used) {
   seed[4] = 0;  // C_MODE
   seed[5] = 0;  // C_LAUNCHES
   seed[6] = ctx->stats.push_actives;
+  seed[8] = ctx->stats.no_offload_rounds;
   CK(cudaMemcpyAsync(ctx->st.counters + C_ROUNDS, seed, sizeof(unsigned long long) * 7, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->st.counters + C_NOOFF_ROUNDS, seed + 8, sizeof(unsigned long long), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(cudaGraphLaunch(ctx->run_exec, ctx->stream));
   TRY(grd_read_counters(ctx));
@@ -197,6 +206,7 @@ int grd_graph_run(grd_ctx* ctx, bool* used) {
   ctx->stats.pull_rounds = (uint32_t)c[C_PULL_ROUNDS];
   ctx->stats.actives_total = c[C_ACTIVE_TOTAL];
   ctx->stats.push_actives = c[C_PUSH_ACTIVES];
+  ctx->stats.no_offload_rounds = (uint32_t)c[C_NOOFF_ROUNDS];
   ctx->stats.kernel_launches += c[C_LAUNCHES];
   ctx->stats.converged = c[C_FRONTIER] == 0;
   *used = true;

@@ -51,7 +51,8 @@ enum Counter : int {
   C_UNVISITED = 18,  // SSSP: out-edges of vertices not reached yet
   C_DONE = 19,       // finished-block count of k_update_list (last-block reset)
   C_VERIFY = 20,     // [4] grd_verify accumulators
-  NUM_COUNTERS = 24
+  C_NOOFF_ROUNDS = 24,  // device-driven loop: rounds run NO_OFFLOAD
+  NUM_COUNTERS = 26
 };
 
 struct HubChunkD {
@@ -754,6 +755,37 @@ __device__ __forceinline__ uint32_t source_value(uint32_t v) {
   return A == A_SSSP_HOP ? v + 1u : v;
 }
 
+// NO_OFFLOAD relaxation (src/GraphAlgorithm.cpp:582-637): the compute
+// partition applies the algorithm's own update for each shipped edge straight
+// to its vertex_updates (gid index) — the minUpdate / addUpdate that the
+// memory-side gen_updates and the compute-side aggregate would apply in two
+// steps — so the dirty set is that of the aggregate: a gid whose entry
+// lowered (PageRank: received anything).  d[k] holds gids (0xFFFFFFFF:
+// none); nd[k] is set for the one thread that claimed the gid's dirty bit.
+template <int A>
+__device__ __forceinline__ uint32_t relax_peek_gid(const DevState& st, uint32_t v) {
+  return A == A_PR_DELTA ? 0u : __ldcg(&st.upd[v]);
+}
+
+template <int A, int N>
+__device__ __forceinline__ void relax_compute(const DevState& st, const uint32_t (&d)[N],
+                                              const uint32_t (&cand)[N], const uint32_t (&cur)[N], bool (&nd)[N]) {
+  bool low[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    low[k] = false;
+    if (d[k] == 0xFFFFFFFFu) continue;
+    if (A == A_PR_DELTA) {
+      red_add_f32(reinterpret_cast<float*>(st.upd) + d[k], __uint_as_float(cand[k]));
+      low[k] = true;
+    } else if (cand[k] < cur[k]) {
+      low[k] = cand[k] < atomicMin(&st.upd[d[k]], cand[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < N; ++k) nd[k] = low[k] && claim_bit(st.UD, d[k]);
+}
+
 // ---- load-balanced push (gen_updates over the compacted active list) ------
 // The edge-map runs in three steps so that every warp gets the same number of
 // edges whatever the degree skew: (1) per-block sums of the (hub-capped)
@@ -873,8 +905,9 @@ static __global__ void __launch_bounds__(256) k_deg_down(DevGraph g, DevState st
 // independent memory chains in flight per lane.
 constexpr uint32_t LBS_WIN = 256;
 
-template <int A, bool kDense>
+template <int A, bool kDense, bool kCompute = false>
 __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
+  static_assert(!(kDense && kCompute), "NO_OFFLOAD rounds use the sparse form");
   constexpr int B = LBS_CHUNK / 32;
   constexpr int SW = LBS_WIN / 32;
   __shared__ uint32_t s_dp[8][LBS_WIN];
@@ -963,16 +996,27 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
           if (A == A_SSSP_W) cand[k] = relax_cand<A>(cand[k], __ldg(&g.wgt[ed]));
         }
       }
-#pragma unroll
-      for (int k = 0; k < B; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek<A>(st, dst[k]) : 0u;
-      if (kDense) {
+      if (kCompute) {  // destination slot -> gid: the shipped adjacency holds gids
 #pragma unroll
         for (int k = 0; k < B; ++k)
-          if (dst[k] != 0xFFFFFFFFu) relax_dense<A>(st, dst[k], cand[k], cur[k]);
-      } else {
+          if (dst[k] != 0xFFFFFFFFu) dst[k] = __ldg(&g.slot_gid[dst[k]]);
+#pragma unroll
+        for (int k = 0; k < B; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek_gid<A>(st, dst[k]) : 0u;
         bool nd[B];
-        relax_sparse<A, B>(st, dst, cand, cur, nd);
-        warp_append_n<B>(st.DL, st.lc + L_DL, nd, dst);
+        relax_compute<A, B>(st, dst, cand, cur, nd);
+        warp_append_n<B>(st.UL, st.lc + L_UL, nd, dst);
+      } else {
+#pragma unroll
+        for (int k = 0; k < B; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek<A>(st, dst[k]) : 0u;
+        if (kDense) {
+#pragma unroll
+          for (int k = 0; k < B; ++k)
+            if (dst[k] != 0xFFFFFFFFu) relax_dense<A>(st, dst[k], cand[k], cur[k]);
+        } else {
+          bool nd[B];
+          relax_sparse<A, B>(st, dst, cand, cur, nd);
+          warp_append_n<B>(st.DL, st.lc + L_DL, nd, dst);
+        }
       }
       __syncwarp();
       e = wend;
@@ -985,9 +1029,21 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
 // when its row is active this round (bit set in the forward bitvector) and
 // reads the aligned interior of the row with 128-bit loads.  All loops are
 // block-uniform (the sparse form appends warp-aggregated).
-template <int A, bool kDense, int N>
-__device__ __forceinline__ void hub_relax(const DevState& st, const uint32_t (&d)[N], const uint32_t (&c)[N]) {
+template <int A, bool kDense, int N, bool kCompute = false>
+__device__ __forceinline__ void hub_relax(const DevGraph& g, const DevState& st, const uint32_t (&d)[N],
+                                          const uint32_t (&c)[N]) {
   uint32_t cur[N];
+  if (kCompute) {
+    uint32_t v[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = d[k] != 0xFFFFFFFFu ? __ldg(&g.slot_gid[d[k]]) : 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < N; ++k) cur[k] = v[k] != 0xFFFFFFFFu ? relax_peek_gid<A>(st, v[k]) : 0u;
+    bool nd[N];
+    relax_compute<A, N>(st, v, c, cur, nd);
+    warp_append_n<N>(st.UL, st.lc + L_UL, nd, v);
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < N; ++k) cur[k] = d[k] != 0xFFFFFFFFu ? relax_peek<A>(st, d[k]) : 0u;
   if (kDense) {
@@ -1001,7 +1057,7 @@ __device__ __forceinline__ void hub_relax(const DevState& st, const uint32_t (&d
   }
 }
 
-template <int A, bool kDense>
+template <int A, bool kDense, bool kCompute = false>
 __global__ void __launch_bounds__(256) k_hub_push(DevGraph g, DevState st) {
   unsigned long long scanned = 0;
   for (uint32_t c = blockIdx.x; c < g.num_hubs; c += gridDim.x) {
@@ -1021,7 +1077,7 @@ __global__ void __launch_bounds__(256) k_hub_push(DevGraph g, DevState st) {
         d[0] = __ldg(&g.col[e]);
         cv[0] = relax_cand<A>(sv, A == A_SSSP_W ? __ldg(&g.wgt[e]) : 0u);
       }
-      hub_relax<A, kDense, 1>(st, d, cv);
+      hub_relax<A, kDense, 1, kCompute>(g, st, d, cv);
     }
     const uint4* c4 = reinterpret_cast<const uint4*>(g.col);
     const uint4* w4 = reinterpret_cast<const uint4*>(g.wgt);
@@ -1036,7 +1092,7 @@ __global__ void __launch_bounds__(256) k_hub_push(DevGraph g, DevState st) {
         cv[0] = relax_cand<A>(sv, w.x), cv[1] = relax_cand<A>(sv, w.y);
         cv[2] = relax_cand<A>(sv, w.z), cv[3] = relax_cand<A>(sv, w.w);
       }
-      hub_relax<A, kDense, 4>(st, d, cv);
+      hub_relax<A, kDense, 4, kCompute>(g, st, d, cv);
     }
     if (threadIdx.x == 0) scanned += h.e1 - h.e0;
   }
@@ -1363,6 +1419,32 @@ __global__ void __launch_bounds__(256) k_bwd_list(DevGraph g, DevState st) {
   }
 }
 
+// NO_OFFLOAD round, after the compute-side edge-map: retires the old
+// frontier (its FB and F bits; the update rebuilds the list) and counts the
+// shipped adjacency.  Per frontier vertex the owning memory partition sends
+// one message of its gid and its out-edges' destination gids (and, weighted
+// SSSP, their weights), 4 bytes each (src/GraphAlgorithm.cpp:426-474); the
+// reference's counter adds it at the send and again at the receive
+// (include/MPI.hpp:40-54), the true size counts it once.
+template <int A>
+__global__ void __launch_bounds__(256) k_retire_list(DevGraph g, DevState st) {
+  const uint32_t K = (uint32_t)__ldcg(&st.counters[C_ACTIVE]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) st.lc[L_FL] = 0;  // entries below are read by index
+  unsigned long long words = 0;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < K; j += gridDim.x * blockDim.x) {
+    const uint32_t s = st.AL[j], gid = st.FL[j];
+    atomicAnd(&st.FB[s >> 5], ~(1u << (s & 31)));
+    atomicAnd(&st.F[gid >> 5], ~(1u << (gid & 31)));
+    words += 1ull + (unsigned long long)g.outdeg[gid] * (A == A_SSSP_W ? 2ull : 1ull);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) words += __shfl_xor_sync(FULL, words, o);
+  if (lane_id() == 0 && words) {
+    atomicAdd(&st.counters[C_BYTES], 4ull * words);
+    atomicAdd(&st.counters[C_REFBYTES], 8ull * words);
+  }
+}
+
 // ------------------------------------------------------------------ update --
 // UpdateWorker::update = update_frontier() then apply_updates()
 // (src/Workers.cpp:77-82) for one vertex whose vertex_updates entry is dirty.
@@ -1450,11 +1532,15 @@ __global__ void __launch_bounds__(256) k_update_list(DevGraph g, DevState st, do
 // the push edge-map, k_bwd_list and k_update_list, separated by block
 // barriers instead of kernel boundaries, so a small round costs one launch.
 // Values, dirty sets, lists and statistics equal the multi-kernel round's.
+// kCompute: the same for a NO_OFFLOAD round (compute-side push straight into
+// vertex_updates, no backward sync), equal to the multi-kernel NO_OFFLOAD
+// round (k_fwd_list, the degree scan, k_push_lbs/k_hub_push<.., true>,
+// k_retire_list, k_update_list).
 constexpr uint32_t K_TINY_ACTIVE = 2048;
 constexpr uint32_t K_TINY_EDGES = 16384;
 constexpr int K_TINY_THREADS = 1024;
 
-template <int A>
+template <int A, bool kCompute = false>
 __global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevState st, double tol, double damping) {
   __shared__ uint32_t s_dp[K_TINY_ACTIVE + 1];
   __shared__ uint32_t s_rb[K_TINY_ACTIVE];
@@ -1532,18 +1618,35 @@ __global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevSt
         cand[k] = relax_cand<A>(s_sv[lo], A == A_SSSP_W ? __ldg(&g.wgt[ed]) : 0u);
       }
     }
-#pragma unroll
-    for (int k = 0; k < N; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek<A>(st, dst[k]) : 0u;
     bool nd[N];
-    relax_sparse<A, N>(st, dst, cand, cur, nd);
-    block_append_n<N>(st.DL, st.lc + L_DL, nd, dst);
+    if (kCompute) {  // NO_OFFLOAD: straight into the compute partition's vertex_updates
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        if (dst[k] != 0xFFFFFFFFu) dst[k] = __ldg(&g.slot_gid[dst[k]]);
+#pragma unroll
+      for (int k = 0; k < N; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek_gid<A>(st, dst[k]) : 0u;
+      relax_compute<A, N>(st, dst, cand, cur, nd);
+      block_append_n<N>(st.UL, st.lc + L_UL, nd, dst);
+    } else {
+#pragma unroll
+      for (int k = 0; k < N; ++k) cur[k] = dst[k] != 0xFFFFFFFFu ? relax_peek<A>(st, dst[k]) : 0u;
+      relax_sparse<A, N>(st, dst, cand, cur, nd);
+      block_append_n<N>(st.DL, st.lc + L_DL, nd, dst);
+    }
   }
   __syncthreads();
-  // backward sync: retire the old frontier, send and aggregate the dirty slots
-  const uint32_t n = __ldcg(&st.lc[L_DL]);
+  // backward sync: retire the old frontier, send and aggregate the dirty
+  // slots (NO_OFFLOAD: count the shipped adjacency instead, as k_retire_list)
+  const uint32_t n = kCompute ? 0u : __ldcg(&st.lc[L_DL]);
   if (tid == 0) {
-    st.counters[C_BYTES] += g.bv_bytes + 4ull * n;
-    st.counters[C_REFBYTES] += g.bv_refbytes + 4ull * n;
+    if (kCompute) {
+      const unsigned long long words = (unsigned long long)K + (unsigned long long)m * (A == A_SSSP_W ? 2ull : 1ull);
+      st.counters[C_BYTES] += 4ull * words;
+      st.counters[C_REFBYTES] += 8ull * words;
+    } else {
+      st.counters[C_BYTES] += g.bv_bytes + 4ull * n;
+      st.counters[C_REFBYTES] += g.bv_refbytes + 4ull * n;
+    }
   }
   for (uint32_t j = tid; j < K; j += K_TINY_THREADS) {
     const uint32_t gid = st.FL[j];

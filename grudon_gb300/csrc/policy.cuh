@@ -1,8 +1,8 @@
-// Per-round mode choice on the device: the fixed threshold rule and the
-// learned MLP (inference by one 64-thread block, fused into the round's
-// policy kernel).  No reference counterpart: the reference's only per-round
-// decision engine, the NDP/INC offload rule
-// (include/offload_engine/NDPEngine.hpp:17-50), is disabled in its run().
+// Per-round mode choice on the device: the offload decision (the reference's
+// NDPEngine rule, include/offload_engine/NDPEngine.hpp:10-51, which its run()
+// leaves disabled at src/GraphAlgorithm.cpp:189), then, for NDP_OFFLOAD
+// rounds, the fixed threshold rule or the learned MLP (inference by one
+// 64-thread block, fused into the round's policy kernel).
 #pragma once
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -20,10 +20,37 @@ static_assert(P_OUT == 4, "one output per round mode");
 struct PolicyArgs {
   int direction, format, has_in;
   uint32_t dense_div, pull_div;
-  uint32_t launches[5];     // kernels of one round per branch (device loop stats)
+  int offload;              // GRD_OFFLOAD_*
+  uint32_t launches[7];     // kernels of one round per branch (device loop stats)
   unsigned long long edges; // E
   uint32_t round;           // round index (host loop; the device loop counts)
 };
+
+// Offload decision of a round whose entering frontier has f vertices.
+// NDPEngine (include/offload_engine/NDPEngine.hpp:17-50) returns NO_OFFLOAD
+// when 0 < f <= V/20 (its threshold, src/GraphAlgorithm.cpp:172) and two
+// tests pass that always pass with one compute partition: every frontier
+// vertex is covered (coverage_vector[v]: all out-neighbours share v's master,
+// src/DistributedGraph.cpp:333-343 — every vertex's master is partition 0),
+// and the busiest memory partition holds at least the mean number of
+// frontier vertices over the partitions it touches (a maximum is never below
+// a mean).
+__host__ __device__ inline bool policy_no_offload(int offload, unsigned long long f, uint32_t V) {
+  if (offload == GRD_OFFLOAD_NONE) return true;
+  if (offload != GRD_OFFLOAD_ENGINE) return false;
+  return f != 0 && f <= (unsigned long long)(V / 20u);
+}
+
+// SWITCH branch of a round in `mode`: modes 0-3 and GRD_ROUND_NO_OFFLOAD are
+// their own branch; a frontier small enough for one CTA runs its push + list
+// round as branch 4 (k_round_tiny) and its NO_OFFLOAD round as branch 6.
+constexpr int P_BRANCH_TINY = 4, P_BRANCH_NOOFF_TINY = 6;
+__host__ __device__ inline int policy_branch(int mode, unsigned long long f, unsigned long long fe) {
+  const bool small = f <= K_TINY_ACTIVE && fe <= K_TINY_EDGES;
+  if (small && mode == GRD_ROUND_PUSH_LIST) return P_BRANCH_TINY;
+  if (small && mode == GRD_ROUND_NO_OFFLOAD) return P_BRANCH_NOOFF_TINY;
+  return mode;
+}
 
 // Raw policy features (grd_policy_features computes the same on the host).
 // Sizes enter as log2 fractions of the graph (frontier of V, its edges and
@@ -152,6 +179,7 @@ __device__ __forceinline__ int policy_choose(const DevGraph& g, const DevState& 
                                              const grd_policy_model* model, uint32_t round) {
   __shared__ float s_x[P_IN], s_h1[P_HID], s_h2[P_HID], s_out[P_OUT];
   const unsigned long long f = st.counters[C_FRONTIER], fe = st.counters[C_FEDGES];
+  if (policy_no_offload(a.offload, f, g.V)) return GRD_ROUND_NO_OFFLOAD;
   if (model == nullptr) return policy_fixed(g, a, f, fe);
   const uint32_t allowed = policy_allowed(a.direction, a.format, a.has_in != 0);
   if (policy_tiny(f, fe, allowed)) return GRD_ROUND_PUSH_LIST;
@@ -186,15 +214,14 @@ static __global__ void __launch_bounds__(P_HID) k_policy(DevGraph g, DevState st
   if (threadIdx.x != 0) return;
   st.counters[C_MODE] = (unsigned long long)mode;
   if (kGraph) {
-    if (mode >= GRD_ROUND_PULL_BITVEC) {
+    if (mode == GRD_ROUND_PULL_BITVEC || mode == GRD_ROUND_PULL_LIST) {
       st.counters[C_PULL_ROUNDS] += 1;
       st.counters[C_EDGES] += a.edges;
     } else {
       st.counters[C_PUSH_ROUNDS] += 1;
+      if (mode == GRD_ROUND_NO_OFFLOAD) st.counters[C_NOOFF_ROUNDS] += 1;
     }
-    // push + list rounds of a small frontier run as one CTA (branch 4)
-    const unsigned long long f = st.counters[C_FRONTIER], fe = st.counters[C_FEDGES];
-    const int branch = (mode == GRD_ROUND_PUSH_LIST && f <= K_TINY_ACTIVE && fe <= K_TINY_EDGES) ? 4 : mode;
+    const int branch = policy_branch(mode, st.counters[C_FRONTIER], st.counters[C_FEDGES]);
     st.counters[C_LAUNCHES] += a.launches[branch];
     cudaGraphSetConditional(sw, (unsigned)branch);
   }

@@ -234,6 +234,15 @@ class GraphAlgorithm {
     fused = true;
   }
 
+  // Offload decision per round (GRD_OFFLOAD_*), the reference's NDPEngine
+  // choice (include/offload_engine/NDPEngine.hpp:10-51) that its run()
+  // leaves at NDP_OFFLOAD.  Anything but GRD_OFFLOAD_NDP runs the rounds as
+  // one device-side loop (grd_run), like a schedule.
+  void setOffload(int offload) {
+    sched_offload = offload;
+    if (offload != GRD_OFFLOAD_NDP) fused = true;
+  }
+
   uint32_t getIterations() const { return iterations; }
   DistributedGraph& distributedGraph() { return *graph; }
   void setMaxRounds(uint32_t r) { max_rounds = r; }
@@ -253,6 +262,7 @@ class GraphAlgorithm {
   bool clear_updates = false;
   bool fused = false;
   int sched_direction = GRD_DIR_AUTO, sched_format = GRD_FMT_AUTO, sched_policy = GRD_POLICY_FIXED;
+  int sched_offload = GRD_OFFLOAD_NDP;
   bool has_model = false;
   grd_policy_model sched_model{};
 
@@ -264,6 +274,7 @@ class GraphAlgorithm {
     p.direction = sched_direction;
     p.frontier_format = sched_format;
     p.policy = sched_policy;
+    p.offload = sched_offload;
     check(grd_set_algo(ctx(), algo, &p), ctx(), "grd_set_algo");
     check(grd_set_policy(ctx(), has_model ? &sched_model : nullptr), ctx(), "grd_set_policy");
     check(grd_init(ctx()), ctx(), "grd_init");

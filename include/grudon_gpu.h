@@ -24,6 +24,9 @@
  *   grd_update          UpdateWorker::update (update_frontier + apply_updates)
  *                       + termination_check, src/GraphAlgorithm.cpp:643-662
  *   grd_run             GraphAlgorithm::run, src/GraphAlgorithm.cpp:145-701
+ *                       (offload choice per round: NDPEngine,
+ *                       include/offload_engine/NDPEngine.hpp:10-51; NO_OFFLOAD
+ *                       rounds: src/GraphAlgorithm.cpp:426-474, 582-637)
  *   grd_read_*          PageRank/CC/SSSP::printState output, pr.cpp:162-176
  *
  * Status convention: every int-returning call returns GRD_OK (0) or a negative
@@ -64,6 +67,23 @@ extern "C" {
 #define GRD_FMT_BITVEC  1
 #define GRD_FMT_LIST    2
 
+/* ---- offload decision per round (grd_params.offload) -------------------- */
+/* NDP_OFFLOAD rounds run the edge-map in the memory partitions and sync the
+ * dirty updates back (the reference's only live path: run() hard-codes
+ * NDP_OFFLOAD, src/GraphAlgorithm.cpp:189).  NO_OFFLOAD rounds ship the
+ * frontier's adjacency to the compute partition, which applies the
+ * algorithm's own update to its vertex_updates directly: no memory-side
+ * dirty tracking, backward sync or aggregate (src/GraphAlgorithm.cpp:426-474,
+ * 582-637).  Results are identical either way (PageRank: up to float
+ * summation order). */
+#define GRD_OFFLOAD_NDP     0 /* every round NDP_OFFLOAD (the reference)     */
+#define GRD_OFFLOAD_ENGINE  1 /* NDPEngine rule per round: NO_OFFLOAD when
+                                 0 < |frontier| <= V/20 and the coverage and
+                                 imbalance tests pass (NDPEngine.hpp:17-50)  */
+#define GRD_OFFLOAD_NONE    2 /* every round NO_OFFLOAD                      */
+/* grd_run applies the setting; the per-stage calls (grd_sync_fwd ...
+ * grd_update) always run an NDP_OFFLOAD round. */
+
 #define GRD_RUN_STRICT  1u /* flag: return GRD_E_ROUND_CAP at the round cap */
 #define GRD_RUN_HOST_LOOP 2u /* flag: drive rounds from the host (one
                                 synchronisation per round) instead of the
@@ -97,6 +117,10 @@ typedef struct grd_params {
   int policy;           /* GRD_POLICY_FIXED (threshold rule above) or
                            GRD_POLICY_LEARNED (model set by grd_set_policy;
                            the fixed rule when none is set)               */
+  int offload;          /* GRD_OFFLOAD_* (default NDP).  The direction,
+                           format and policy settings apply to NDP_OFFLOAD
+                           rounds; NO_OFFLOAD rounds push from the compute
+                           partition with list syncs.  Not for PR_PULL.   */
 } grd_params;
 
 #define GRD_POLICY_FIXED   0
@@ -107,10 +131,15 @@ typedef struct grd_stats {
   uint32_t converged;         /* 1 if the frontier emptied before the cap  */
   uint64_t edges_scanned;     /* out-edges (push) / in-edges (pull) read   */
   uint64_t bytes_synced;      /* bitvector words + packed values, both
-                                 directions, all partitions (true size)    */
+                                 directions, all partitions (true size);
+                                 NO_OFFLOAD rounds: forward sync plus the
+                                 shipped adjacency, 4 B per frontier vertex
+                                 and per edge (x2 with weights)            */
   uint64_t reference_bytes_moved; /* the reference's TotalBytesMoved
                                  formula (bitvector count inflated x8,
-                                 src/GraphAlgorithm.cpp:251-265)           */
+                                 src/GraphAlgorithm.cpp:251-265; MPI send
+                                 and recv of the shipped adjacency both
+                                 counted, include/MPI.hpp:40-54)           */
   double last_residual;       /* PR_PULL: last L1 residual / V (FP64)      */
   uint32_t push_rounds;       /* rounds that ran the push edge-map         */
   uint32_t pull_rounds;       /* rounds that ran the pull edge-map         */
@@ -129,6 +158,8 @@ typedef struct grd_stats {
    * the actives of its rounds. */
   double lbs_ms;
   uint64_t lbs_edges, lbs_actives, lbs_launches;
+  uint32_t no_offload_rounds; /* rounds run NO_OFFLOAD (counted in
+                                 push_rounds too)                          */
 } grd_stats;
 
 typedef struct grd_ctx grd_ctx;
@@ -210,10 +241,15 @@ int grd_set_profiling(grd_ctx* ctx, int enable);
 #define GRD_ROUND_PUSH_LIST   1
 #define GRD_ROUND_PULL_BITVEC 2
 #define GRD_ROUND_PULL_LIST   3
+/* NO_OFFLOAD round: frontier values forward (list form, as the reference
+ * still sends them), adjacency to the compute partition, compute-side push
+ * into vertex_updates, update.  Never predicted by the learned model. */
+#define GRD_ROUND_NO_OFFLOAD  5
 
 typedef struct grd_round_rec {
   uint32_t round;         /* 0-based round index                          */
-  int32_t mode;           /* GRD_ROUND_* (direction x sync format)        */
+  int32_t mode;           /* GRD_ROUND_* (direction x sync format, or
+                             GRD_ROUND_NO_OFFLOAD)                        */
   uint64_t frontier_in;   /* |frontier| entering the round                */
   uint64_t actives;       /* actives unpacked by the forward sync         */
   uint64_t edges;         /* edges the edge-map read this round           */

@@ -20,7 +20,13 @@ u64p = C.POINTER(C.c_uint64)
 
 class orc_stats(C.Structure):
     _fields_ = [("rounds", C.c_uint32), ("converged", C.c_uint32), ("edges_scanned", C.c_uint64),
-                ("bytes_synced", C.c_uint64), ("reference_bytes_moved", C.c_uint64)]
+                ("bytes_synced", C.c_uint64), ("reference_bytes_moved", C.c_uint64),
+                ("no_offload_rounds", C.c_uint32)]
+
+
+# offload decision per round: every round NDP_OFFLOAD (the reference), the
+# NDPEngine rule, every round NO_OFFLOAD
+ORC_OFFLOAD_NDP, ORC_OFFLOAD_ENGINE, ORC_OFFLOAD_NONE = 0, 1, 2
 
 
 _lib = None
@@ -44,6 +50,9 @@ def lib() -> C.CDLL:
         L.orc_run_layout.restype = C.c_int
         L.orc_run_layout.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_int,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(orc_stats)]
+        L.orc_run_layout_ex.restype = C.c_int
+        L.orc_run_layout_ex.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_double, C.c_double,
+                                        C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(orc_stats)]
         L.orc_layout_slots.restype = C.c_uint32
         L.orc_layout_slots.argtypes = [C.c_uint32, u64p, u32p, u32p, C.c_uint32, C.c_uint32, u32p, C.c_uint32, u32p]
         L.orc_bfs.restype = None
@@ -76,8 +85,13 @@ def _p32(a):
 
 
 def run(algo: int, ro, col, w=None, mirror=None, num_memory: int = 1, source: int = 0, max_rounds: int = 1000,
-        damping: float = 0.85, tol: float = 1e-6, threads: int = 1) -> dict:
+        damping: float = 0.85, tol: float = 1e-6, threads: int = 1, offload: int = ORC_OFFLOAD_NDP) -> dict:
     """Restated reference round protocol; returns props/updates/ranks/stats."""
+    if offload != ORC_OFFLOAD_NDP:
+        out = Layout(ro, col, w, mirror, num_memory).run(algo, source, max_rounds, damping, tol, threads, offload)
+        if algo != ORC_PR_DELTA:
+            del out["ranks"]
+        return out
     ro, col, w = _csr(ro, col, w)
     V = len(ro) - 1
     mir = None if mirror is None else np.ascontiguousarray(mirror, dtype=np.uint32)
@@ -111,15 +125,15 @@ class Layout:
             raise ValueError("oracle rejected the layout arguments")
 
     def run(self, algo: int, source: int = 0, max_rounds: int = 1000, damping: float = 0.85, tol: float = 1e-6,
-            threads: int = 1) -> dict:
+            threads: int = 1, offload: int = ORC_OFFLOAD_NDP) -> dict:
         dt = np.float32 if algo == ORC_PR_DELTA else np.uint32
         props = np.zeros(self.V, dtype=dt)
         upd = np.zeros(self.V, dtype=dt)
         ranks = np.zeros(self.V, dtype=np.float32)
         st = orc_stats()
-        rc = lib().orc_run_layout(self._h, algo, source, max_rounds, damping, tol, threads,
-                                  props.ctypes.data_as(C.c_void_p), ranks.ctypes.data_as(C.c_void_p),
-                                  upd.ctypes.data_as(C.c_void_p), C.byref(st))
+        rc = lib().orc_run_layout_ex(self._h, algo, source, max_rounds, damping, tol, threads, offload,
+                                     props.ctypes.data_as(C.c_void_p), ranks.ctypes.data_as(C.c_void_p),
+                                     upd.ctypes.data_as(C.c_void_p), C.byref(st))
         if rc != 0:
             raise ValueError("oracle rejected the run arguments")
         return {"props": props, "updates": upd, "ranks": ranks,

@@ -27,6 +27,8 @@
 //   include/DistributedGraph.hpp:91-214  PropertyList semantics
 //   src/DistributedGraph.cpp:285-775     proxies, translation tables
 //   include/partitioning_engine/Partitioner.hpp:11-205 master = gid % C
+//   include/offload_engine/NDPEngine.hpp:10-51 offload decision, and the
+//   NO_OFFLOAD round of src/GraphAlgorithm.cpp:426-474, 582-637
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -232,6 +234,7 @@ struct Layout {
   // partition) and rTrans[p][slot] = gid.
   std::vector<std::vector<uint32_t>> rTrans;
   std::vector<uint32_t> sOwned;  // slot of gid in mirror[gid]
+  std::vector<uint8_t> coverage;  // compute-side coverage_vector
 };
 
 // DistributedGraph ctor restated for C = 1 (src/DistributedGraph.cpp:13-785).
@@ -256,6 +259,14 @@ void build(Layout& L, uint32_t V, const uint64_t* ro, const uint32_t* col, const
   for (uint32_t u = 0; u < V; ++u)
     for (uint64_t i = ro[u]; i < ro[u + 1]; ++i)
       if (L.mirror[col[i]] != L.mirror[u]) cross[L.mirror[u]].set(col[i]);
+  // coverage_vector (:296-343): a vertex stays covered unless an out-edge
+  // leads to a vertex with another master.  The master partition is
+  // gid % C (Partitioner.hpp:11-205), i.e. 0 for every vertex with C = 1.
+  auto master = [](uint32_t) { return 0u; };
+  L.coverage.assign(V, 1);
+  for (uint32_t u = 0; u < V; ++u)
+    for (uint64_t i = ro[u]; i < ro[u + 1]; ++i)
+      if (master(col[i]) != master(u)) L.coverage[u] = 0;
   L.parts.assign(M, MemPart());
   L.rTrans.assign(M, {});
   L.sOwned.assign(V, 0);
@@ -300,11 +311,36 @@ struct Stats {
   uint64_t edges_scanned;
   uint64_t bytes_synced;
   uint64_t reference_bytes_moved;
+  uint32_t no_offload_rounds;
 };
+
+enum Offload { OFF_NDP = 0, OFF_ENGINE = 1, OFF_NONE = 2 };
+
+// NDPEngine (include/offload_engine/NDPEngine.hpp:10-51) on the compute
+// rank, with its threshold total_vertices / 20 (src/GraphAlgorithm.cpp:172).
+// True = NO_OFFLOAD.  The reference's call site (commented out at :189-190)
+// sizes mirrorCoverage by num_compute while indexing it by memory partition;
+// it is sized by M here.
+bool ndp_engine_no_offload(const Layout& L, const std::vector<uint32_t>& fr) {
+  const uint64_t threshold = L.V / 20;
+  if (fr.empty() || fr.size() > threshold) return false;
+  for (uint32_t v : fr)
+    if (!L.coverage[v]) return false;
+  std::vector<uint64_t> mc(L.M, 0);
+  for (uint32_t lid : fr) mc[L.mirror[lid]]++;  // lid = gid on the compute rank (C = 1)
+  uint64_t mx = 0, total = 0, touched = 0;
+  for (uint64_t c : mc) {
+    mx = std::max(mx, c);
+    total += c;
+    touched += c > 0;
+  }
+  if (touched == 0 || mx < total / touched) return false;
+  return true;
+}
 
 template <class T, int A>
 void run_protocol(const Layout& L, uint32_t source, uint32_t max_rounds, double damping, double tol, Pool& pool,
-                  T* props_out, float* ranks_out, T* updates_out, Stats& st) {
+                  int offload, T* props_out, float* ranks_out, T* updates_out, Stats& st) {
   const uint32_t V = L.V, M = L.M;
   const T MAXV = std::numeric_limits<T>::max();
   // Compute rank state.
@@ -375,12 +411,18 @@ void run_protocol(const Layout& L, uint32_t source, uint32_t max_rounds, double 
     bwd_bv[p].resize(L.parts[p].T());
   }
   uint64_t edges = 0, bytes = 0, refbytes = 0;
-  uint32_t iteration = 0;
+  uint32_t iteration = 0, no_offload_rounds = 0;
   bool done = false;
+  const uint64_t msg_words_per_edge = (A == ORC_SSSP_W) ? 2 : 1;  // dst gid (+ weight)
   while (!done && iteration < max_rounds) {
+    const std::vector<uint32_t> frontier_iter = frontier.offsets();
+    // C1: offload decision (the reference's run() fixes NDP_OFFLOAD, :189).
+    const bool no_off =
+        offload == OFF_NONE || (offload == OFF_ENGINE && ndp_engine_no_offload(L, frontier_iter));
+    no_offload_rounds += no_off;
     // C2: compute packs the frontier per mirror partition (ascending lid).
     for (uint32_t p = 0; p < M; ++p) fwd_buf[p].clear();
-    for (uint32_t lid : frontier.offsets()) {
+    for (uint32_t lid : frontier_iter) {
       uint32_t p = L.mirror[lid];
       fwd_bv[p].set(L.sOwned[lid]);
       fwd_buf[p].push_back(cprop.get(lid));
@@ -396,6 +438,19 @@ void run_protocol(const Layout& L, uint32_t source, uint32_t max_rounds, double 
       std::vector<uint32_t> bits = fwd_bv[p].offsets();
       for (size_t j = 0; j < bits.size(); ++j) mprop[p].set(bits[j], fwd_buf[p][j]);
       fwd_bv[p].reset();
+      if (no_off) {
+        // NO_OFFLOAD, memory side (:426-474): per updated vertex_properties
+        // entry one message [gid, destination gids...] (weighted SSSP: and
+        // the weights) to its compute rank; net.send counts it.
+        for (uint32_t lid : mprop[p].dirty.offsets()) {
+          const uint64_t r0 = lid ? P.row_end[lid - 1] : 0, r1 = P.row_end[lid];
+          const uint64_t words = 1 + (r1 - r0) * msg_words_per_edge;
+          bytes += words * 4;
+          refbytes += words * 4;
+        }
+        mprop[p].clear_uv();
+        continue;
+      }
       // C4 gen_updates over dirty vertex_properties, ascending lid.
       std::vector<uint32_t> act = mprop[p].dirty.offsets();
       std::atomic<uint64_t> scanned{0};
@@ -438,7 +493,47 @@ void run_protocol(const Layout& L, uint32_t source, uint32_t max_rounds, double 
         mupd[p].clear_uv();
       mprop[p].clear_uv();
     }
-    // C6 aggregate, partitions in ascending order.
+    if (no_off) {
+      // NO_OFFLOAD, compute side (:582-637): one message per frontier vertex
+      // from its mirror partition (net.recv counts it again), then the
+      // algorithm's update per shipped edge straight into vertex_updates.
+      // The reference hard-codes addUpdate(l_dst, vertex_properties[src])
+      // there (PageRank's gen_updates; :626 leaves "abstract this to the
+      // graph algorithm" as a TODO with minUpdate commented out beside it);
+      // each algorithm's own gen_updates relaxation is applied here.
+      std::atomic<uint64_t> scanned{0}, words{0};
+      pool.run(frontier_iter.size(), 64, [&](uint64_t b, uint64_t e) {
+        uint64_t sc = 0, wd = 0;
+        for (uint64_t k = b; k < e; ++k) {
+          const uint32_t src = frontier_iter[k];
+          const MemPart& P = L.parts[L.mirror[src]];
+          const uint32_t lid = L.sOwned[src];
+          const uint64_t r0 = lid ? P.row_end[lid - 1] : 0, r1 = P.row_end[lid];
+          sc += r1 - r0;
+          wd += 1 + (r1 - r0) * msg_words_per_edge;
+          const T pv = cprop.get(src);
+          for (uint64_t i = r0; i < r1; ++i) {
+            const uint32_t d = P.lid_gid[P.dst[i]];
+            if (A == ORC_PR_DELTA) {
+              cupd.addUpdate(d, pv);
+            } else if (A == ORC_CC) {
+              cupd.minUpdate(d, pv);
+            } else if (A == ORC_SSSP_HOP) {
+              cupd.minUpdate(d, (T)(pv + 1));
+            } else {
+              uint64_t c = (uint64_t)pv + P.w[i];
+              cupd.minUpdate(d, (T)std::min<uint64_t>(c, 0xFFFFFFFFull));
+            }
+          }
+        }
+        scanned.fetch_add(sc);
+        words.fetch_add(wd);
+      });
+      edges += scanned.load();
+      refbytes += words.load() * 4;
+    }
+    // C6 aggregate, partitions in ascending order (nothing was packed in a
+    // NO_OFFLOAD round).
     for (uint32_t p = 0; p < M; ++p) {
       std::vector<uint32_t> bits = bwd_bv[p].offsets();
       for (size_t j = 0; j < bits.size(); ++j) {
@@ -493,6 +588,7 @@ void run_protocol(const Layout& L, uint32_t source, uint32_t max_rounds, double 
   st.edges_scanned = edges;
   st.bytes_synced = bytes;
   st.reference_bytes_moved = refbytes;
+  st.no_offload_rounds = no_offload_rounds;
 }
 
 }  // namespace
@@ -505,6 +601,7 @@ struct orc_stats {
   uint64_t edges_scanned;
   uint64_t bytes_synced;
   uint64_t reference_bytes_moved;
+  uint32_t no_offload_rounds;
 };
 
 // Runs the restated round protocol.  props_out/updates_out receive V 32-bit
@@ -532,10 +629,12 @@ orc_layout* orc_layout_create(uint32_t V, const uint64_t* ro, const uint32_t* co
 
 void orc_layout_free(orc_layout* h) { delete h; }
 
-// Runs init() + run() of one algorithm on a prebuilt layout.
-int orc_run_layout(const orc_layout* h, int algo, uint32_t source, uint32_t max_rounds, double damping, double tol,
-                   int threads, void* props_out, float* ranks_out, void* updates_out, orc_stats* st) {
-  if (!h || !st) return -1;
+// Runs init() + run() of one algorithm on a prebuilt layout; offload: 0 every
+// round NDP_OFFLOAD (the reference), 1 the NDPEngine rule, 2 every round
+// NO_OFFLOAD.
+int orc_run_layout_ex(const orc_layout* h, int algo, uint32_t source, uint32_t max_rounds, double damping, double tol,
+                      int threads, int offload, void* props_out, float* ranks_out, void* updates_out, orc_stats* st) {
+  if (!h || !st || offload < OFF_NDP || offload > OFF_NONE) return -1;
   const Layout& L = h->L;
   if ((algo == ORC_SSSP_W) && !h->weighted) return -1;
   if ((algo == ORC_SSSP_HOP || algo == ORC_SSSP_W) && source >= L.V) return -1;
@@ -543,20 +642,20 @@ int orc_run_layout(const orc_layout* h, int algo, uint32_t source, uint32_t max_
   Stats s{};
   switch (algo) {
     case ORC_PR_DELTA:
-      run_protocol<float, ORC_PR_DELTA>(L, source, max_rounds, damping, tol, pool, (float*)props_out, ranks_out,
-                                        (float*)updates_out, s);
+      run_protocol<float, ORC_PR_DELTA>(L, source, max_rounds, damping, tol, pool, offload, (float*)props_out,
+                                        ranks_out, (float*)updates_out, s);
       break;
     case ORC_CC:
-      run_protocol<uint32_t, ORC_CC>(L, source, max_rounds, damping, tol, pool, (uint32_t*)props_out, nullptr,
-                                     (uint32_t*)updates_out, s);
+      run_protocol<uint32_t, ORC_CC>(L, source, max_rounds, damping, tol, pool, offload, (uint32_t*)props_out,
+                                     nullptr, (uint32_t*)updates_out, s);
       break;
     case ORC_SSSP_HOP:
-      run_protocol<uint32_t, ORC_SSSP_HOP>(L, source, max_rounds, damping, tol, pool, (uint32_t*)props_out, nullptr,
-                                           (uint32_t*)updates_out, s);
+      run_protocol<uint32_t, ORC_SSSP_HOP>(L, source, max_rounds, damping, tol, pool, offload,
+                                           (uint32_t*)props_out, nullptr, (uint32_t*)updates_out, s);
       break;
     case ORC_SSSP_W:
-      run_protocol<uint32_t, ORC_SSSP_W>(L, source, max_rounds, damping, tol, pool, (uint32_t*)props_out, nullptr,
-                                         (uint32_t*)updates_out, s);
+      run_protocol<uint32_t, ORC_SSSP_W>(L, source, max_rounds, damping, tol, pool, offload, (uint32_t*)props_out,
+                                         nullptr, (uint32_t*)updates_out, s);
       break;
     default:
       return -1;
@@ -566,7 +665,14 @@ int orc_run_layout(const orc_layout* h, int algo, uint32_t source, uint32_t max_
   st->edges_scanned = s.edges_scanned;
   st->bytes_synced = s.bytes_synced;
   st->reference_bytes_moved = s.reference_bytes_moved;
+  st->no_offload_rounds = s.no_offload_rounds;
   return 0;
+}
+
+int orc_run_layout(const orc_layout* h, int algo, uint32_t source, uint32_t max_rounds, double damping, double tol,
+                   int threads, void* props_out, float* ranks_out, void* updates_out, orc_stats* st) {
+  return orc_run_layout_ex(h, algo, source, max_rounds, damping, tol, threads, OFF_NDP, props_out, ranks_out,
+                           updates_out, st);
 }
 
 int orc_run(int algo, uint32_t V, uint64_t E, const uint64_t* ro, const uint32_t* col, const uint32_t* w,
