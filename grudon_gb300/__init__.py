@@ -214,7 +214,10 @@ def read_partition_file(path: str, n: int, num_memory: int) -> np.ndarray:
 class Context:
     """One partitioned graph resident on one GPU (grd_ctx)."""
 
-    def __init__(self, graph: Graph, mirror_part=None, num_memory: int = 1, device: int = 0):
+    def __init__(self, graph: Graph, mirror_part=None, num_memory: int = 1, device: int = 0,
+                 device_layout: bool = False):
+        """device_layout=True builds the partition layout on the GPU from the
+        uploaded CSR (grd_ctx_create_ex with GRD_CREATE_DEVICE_LAYOUT)."""
         self._lib = lib()
         self._ctx = C.c_void_p()
         self._graph = graph  # keeps host arrays alive for the create call
@@ -226,10 +229,12 @@ class Context:
                 raise ValueError("mirror_part must have one entry per vertex")
             mp = self._mp.ctypes.data_as(_ffi.u32p)
         csr = graph.csr_struct()
-        rc = self._lib.grd_ctx_create(C.byref(csr), mp, 1, num_memory, device, C.byref(self._ctx))
+        flags = _ffi.GRD_CREATE_DEVICE_LAYOUT if device_layout else 0
+        rc = self._lib.grd_ctx_create_ex(C.byref(csr), mp, 1, num_memory, device, flags, C.byref(self._ctx))
         if rc != 0:
             raise GrdError(rc, self._lib.grd_create_error().decode())
         self.algo = None
+        self.device_layout = device_layout
 
     def _check(self, rc: int) -> None:
         if rc != 0:
@@ -344,6 +349,30 @@ class Context:
         b = C.c_uint64()
         self._check(self._lib.grd_upload(self._ctx, C.byref(b)))
         return int(b.value)
+
+    def ingest(self, graph: Graph, mirror_part=None) -> int:
+        """Re-uploads a CSR of the same shape into a device-layout ctx and
+        rebuilds the layout on the GPU; returns the host->device bytes."""
+        mp = None
+        if mirror_part is not None:
+            keep = _u32(mirror_part)
+            mp = keep.ctypes.data_as(_ffi.u32p)
+        csr = graph.csr_struct()
+        b = C.c_uint64()
+        self._check(self._lib.grd_ingest(self._ctx, C.byref(csr), mp, C.byref(b)))
+        return int(b.value)
+
+    def read_layout(self, name: str) -> np.ndarray:
+        """One resident layout array (grd_read_layout): slot_gid, row_off,
+        col, wgt, outdeg, own_slot, hubs, in_off, in_src, in_wgt, in_hubs,
+        in_meds; hub lists come back as (n, 3) arrays of (slot, e0, e1)."""
+        which = _ffi.LAYOUT_ARRAYS[name]
+        n = C.c_size_t()
+        self._check(self._lib.grd_read_layout(self._ctx, which, None, 0, C.byref(n)))
+        out = np.empty(n.value // 4, dtype=np.uint32)
+        self._check(self._lib.grd_read_layout(self._ctx, which, out.ctypes.data_as(C.c_void_p), out.nbytes,
+                                              C.byref(n)))
+        return out.reshape(-1, 3) if name in ("hubs", "in_hubs", "in_meds") else out
 
     def _read(self, fn, dtype, n):
         out = np.empty(n, dtype=dtype)

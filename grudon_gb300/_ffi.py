@@ -27,6 +27,9 @@ GRD_FMT_AUTO, GRD_FMT_BITVEC, GRD_FMT_LIST = 0, 1, 2
 GRD_ROUND_PUSH_BITVEC, GRD_ROUND_PUSH_LIST, GRD_ROUND_PULL_BITVEC, GRD_ROUND_PULL_LIST = 0, 1, 2, 3
 GRD_ROUND_NO_OFFLOAD = 5
 GRD_OFFLOAD_NDP, GRD_OFFLOAD_ENGINE, GRD_OFFLOAD_NONE = 0, 1, 2
+GRD_CREATE_DEVICE_LAYOUT = 1
+LAYOUT_ARRAYS = {"slot_gid": 0, "row_off": 1, "col": 2, "wgt": 3, "outdeg": 4, "own_slot": 5, "hubs": 6,
+                 "in_off": 7, "in_src": 8, "in_wgt": 9, "in_hubs": 10, "in_meds": 11}
 GRD_RUN_STRICT = 1
 GRD_RUN_HOST_LOOP = 2
 
@@ -111,6 +114,10 @@ SIGNATURES = {
     "grd_last_error": (C.c_char_p, [C.c_void_p]),
     "grd_create_error": (C.c_char_p, []),
     "grd_upload": (C.c_int, [C.c_void_p, u64p]),
+    "grd_ctx_create_ex": (C.c_int, [C.POINTER(grd_csr), u32p, C.c_uint32, C.c_uint32, C.c_int, C.c_uint32,
+                                    C.POINTER(C.c_void_p)]),
+    "grd_ingest": (C.c_int, [C.c_void_p, C.POINTER(grd_csr), u32p, u64p]),
+    "grd_read_layout": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "grd_set_algo": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(grd_params)]),
     "grd_init": (C.c_int, [C.c_void_p]),
     "grd_init_sources": (C.c_int, [C.c_void_p, u32p, C.c_size_t]),

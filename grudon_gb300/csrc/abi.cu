@@ -52,7 +52,11 @@ int upload(grd_ctx* ctx, T* dst, const std::vector<T>& src) {
 // Blocks of the degree-scan kernels (fixed grid, segments sized on device).
 uint32_t lbs_blocks(const grd_ctx* ctx) { return (uint32_t)ctx->num_sms * 4; }
 
-int alloc_and_upload(grd_ctx* ctx) {
+}  // namespace
+
+// Allocates every resident array from the layout's sizes (the host build
+// uploads into them, the device build fills them).
+int grd_alloc_resident(grd_ctx* ctx) {
   const Layout& L = ctx->L;
   DevGraph& g = ctx->g;
   DevState& st = ctx->st;
@@ -75,7 +79,7 @@ int alloc_and_upload(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, (uint32_t**)&g.col, std::max<size_t>(E, 4)));
   if (L.weighted) TRY(dev_alloc(ctx, (uint32_t**)&g.wgt, std::max<size_t>(E, 4)));
   TRY(dev_alloc(ctx, (uint32_t**)&g.outdeg, V));
-  TRY(dev_alloc(ctx, (HubChunkD**)&g.hubs, L.hubs.size()));
+  if (!ctx->device_layout) TRY(dev_alloc(ctx, (HubChunkD**)&g.hubs, L.hubs.size()));  // device: sized when built
   TRY(dev_alloc(ctx, (uint32_t**)&g.tile_part, T));
   TRY(dev_alloc(ctx, (uint32_t**)&g.part_base, M));
   TRY(dev_alloc(ctx, (uint32_t**)&g.part_T, M));
@@ -114,8 +118,6 @@ int alloc_and_upload(grd_ctx* ctx) {
   return GRD_OK;
 }
 
-}  // namespace
-
 int grd_upload_layout(grd_ctx* ctx) {
   const Layout& L = ctx->L;
   DevGraph& g = ctx->g;
@@ -150,6 +152,7 @@ int grd_upload_layout(grd_ctx* ctx) {
 
 int grd_ensure_in_edges(grd_ctx* ctx) {
   if (ctx->in_edges_alloc) return GRD_OK;
+  if (ctx->device_layout) return grd_device_in_edges(ctx);
   build_in_edges(ctx->L);
   const Layout& L = ctx->L;
   TRY(dev_alloc(ctx, (uint32_t**)&ctx->g.in_off, L.S + 1));
@@ -631,6 +634,72 @@ int grd_ctx_create(const grd_csr* graph, const uint32_t* mirror_part, uint32_t n
   return GRD_OK;
 }
 
+int grd_ctx_create_ex(const grd_csr* graph, const uint32_t* mirror_part, uint32_t num_compute, uint32_t num_memory,
+                      int device, uint32_t flags, grd_ctx** out) {
+  if (!out) return GRD_E_INVALID;
+  if (!(flags & GRD_CREATE_DEVICE_LAYOUT))
+    return flags ? (g_create_error = "unknown create flags", GRD_E_INVALID)
+                 : grd_ctx_create(graph, mirror_part, num_compute, num_memory, device, out);
+  if (flags & ~GRD_CREATE_DEVICE_LAYOUT) {
+    g_create_error = "unknown create flags";
+    return GRD_E_INVALID;
+  }
+  *out = nullptr;
+  g_create_error.clear();
+  if (num_compute != 1) {
+    g_create_error = "num_compute must be 1";
+    return GRD_E_INVALID;
+  }
+  std::string why;
+  if (grd_device_layout_check(graph, num_memory, &why) != GRD_OK) {
+    g_create_error = why;
+    return GRD_E_INVALID;
+  }
+  const int ndev = grd_device_count();
+  if (ndev <= 0) {
+    g_create_error = "no CUDA device visible";
+    return GRD_E_CUDA;
+  }
+  if (device < 0 || device >= ndev) {
+    g_create_error = "device index out of range";
+    return GRD_E_INVALID;
+  }
+  grd_ctx* ctx = new (std::nothrow) grd_ctx();
+  if (!ctx) return GRD_E_OOM;
+  ctx->device = device;
+  ctx->device_layout = true;
+  ctx->L.V = graph->num_vertices;
+  ctx->L.E = graph->num_edges;
+  ctx->L.M = num_memory;
+  ctx->L.weighted = graph->weights != nullptr;
+  int rc = grd_ctx_init_stream(ctx);
+  if (rc == GRD_OK) rc = grd_device_layout_build(ctx, graph, mirror_part, true);
+  if (rc != GRD_OK) {
+    g_create_error = ctx->err;
+    grd_ctx_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return GRD_OK;
+}
+
+int grd_ingest(grd_ctx* ctx, const grd_csr* graph, const uint32_t* mirror_part, uint64_t* bytes_copied) {
+  if (!ctx) return GRD_E_INVALID;
+  if (!ctx->device_layout) {
+    ctx->err = "grd_ingest needs a ctx created with GRD_CREATE_DEVICE_LAYOUT";
+    return GRD_E_INVALID;
+  }
+  std::string why;
+  if (grd_device_layout_check(graph, ctx->L.M, &why) != GRD_OK) {
+    ctx->err = why;
+    return GRD_E_INVALID;
+  }
+  CK(cudaSetDevice(ctx->device));
+  const int rc = grd_device_layout_build(ctx, graph, mirror_part, false);
+  if (bytes_copied) *bytes_copied = ctx->upload_bytes;
+  return rc;
+}
+
 void grd_ctx_destroy(grd_ctx* ctx) {
   if (!ctx) return;
   if (ctx->stream) {
@@ -651,6 +720,10 @@ void grd_ctx_destroy(grd_ctx* ctx) {
 
 int grd_upload(grd_ctx* ctx, uint64_t* bytes_copied) {
   if (!ctx) return GRD_E_INVALID;
+  if (ctx->device_layout) {
+    ctx->err = "a device-built layout keeps no host copy: re-ingest the CSR with grd_ingest";
+    return GRD_E_INVALID;
+  }
   CK(cudaSetDevice(ctx->device));
   int rc = grd_upload_layout(ctx);
   if (bytes_copied) *bytes_copied = ctx->upload_bytes;
@@ -1037,7 +1110,49 @@ int grd_layout_slots(const grd_ctx* ctx, uint32_t part, uint32_t* host, size_t c
   if (!ctx || part >= ctx->L.M || !host) return GRD_E_INVALID;
   const uint32_t T = ctx->L.T(part);
   if (count < T) return GRD_E_INVALID;
+  if (ctx->device_layout) {  // resident copy only
+    if (cudaSetDevice(ctx->device) != cudaSuccess ||
+        cudaMemcpy(host, ctx->g.slot_gid + ctx->L.slot_base[part], sizeof(uint32_t) * T, cudaMemcpyDeviceToHost) !=
+            cudaSuccess) {
+      (void)cudaGetLastError();
+      return GRD_E_CUDA;
+    }
+    return GRD_OK;
+  }
   std::memcpy(host, ctx->L.slot_gid.data() + ctx->L.slot_base[part], sizeof(uint32_t) * T);
+  return GRD_OK;
+}
+
+int grd_read_layout(grd_ctx* ctx, int which, void* host, size_t cap_bytes, size_t* bytes) {
+  if (!ctx || !bytes) return GRD_E_INVALID;
+  const Layout& L = ctx->L;
+  const void* src = nullptr;
+  size_t n = 0;
+  const size_t u = sizeof(uint32_t);
+  switch (which) {
+    case GRD_LAYOUT_SLOT_GID: src = ctx->g.slot_gid, n = u * L.S; break;
+    case GRD_LAYOUT_ROW_OFF: src = ctx->g.row_off, n = u * (L.S + 1); break;
+    case GRD_LAYOUT_COL: src = ctx->g.col, n = u * L.E; break;
+    case GRD_LAYOUT_WGT: src = ctx->g.wgt, n = L.weighted ? u * L.E : 0; break;
+    case GRD_LAYOUT_OUTDEG: src = ctx->g.outdeg, n = u * L.V; break;
+    case GRD_LAYOUT_OWN_SLOT: src = ctx->st.own_slot, n = u * L.V; break;
+    case GRD_LAYOUT_HUBS: src = ctx->g.hubs, n = sizeof(HubChunkD) * ctx->g.num_hubs; break;
+    case GRD_LAYOUT_IN_OFF: src = ctx->g.in_off, n = ctx->in_edges_alloc ? u * (L.S + 1) : 0; break;
+    case GRD_LAYOUT_IN_SRC: src = ctx->g.in_src, n = ctx->in_edges_alloc ? u * L.E : 0; break;
+    case GRD_LAYOUT_IN_WGT: src = ctx->g.in_wgt, n = ctx->in_edges_alloc && L.weighted ? u * L.E : 0; break;
+    case GRD_LAYOUT_IN_HUBS: src = ctx->pull.in_hubs, n = sizeof(HubChunkD) * ctx->pull.num_in_hubs; break;
+    case GRD_LAYOUT_IN_MEDS: src = ctx->pull.in_meds, n = sizeof(HubChunkD) * ctx->pull.num_in_meds; break;
+    default: ctx->err = "unknown layout array"; return GRD_E_INVALID;
+  }
+  *bytes = n;
+  if (!host || n == 0) return GRD_OK;
+  if (cap_bytes < n) {
+    ctx->err = "buffer too small for the layout array";
+    return GRD_E_INVALID;
+  }
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(host, src, n, cudaMemcpyDeviceToHost));
   return GRD_OK;
 }
 
@@ -1082,14 +1197,19 @@ int grd_synchronize(grd_ctx* ctx) {
 }  // extern "C"
 
 // ------------------------------------------------------------ device setup --
-int grd_ctx_init_device(grd_ctx* ctx) {
+int grd_ctx_init_stream(grd_ctx* ctx) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaMallocHost((void**)&ctx->h_counters, sizeof(unsigned long long) * (NUM_COUNTERS + 16)));
   std::memset(ctx->h_counters, 0, sizeof(unsigned long long) * (NUM_COUNTERS + 16));
   ctx->h_seed = ctx->h_counters + NUM_COUNTERS;
-  TRY(alloc_and_upload(ctx));
+  return GRD_OK;
+}
+
+int grd_ctx_init_device(grd_ctx* ctx) {
+  TRY(grd_ctx_init_stream(ctx));
+  TRY(grd_alloc_resident(ctx));
   // gid -> owned global slot (the first n_owned slots of each partition).
   const Layout& L = ctx->L;
   ctx->own_slot_host.assign(L.V, 0);

@@ -61,6 +61,7 @@ struct grd_ctx {
   unsigned long long* verify_buf = nullptr;  // grd_verify per-block top ranks
   size_t verify_cap = 0;
   bool has_policy = false;
+  bool device_layout = false;  // layout built on the device (no host copy of its arrays)
 };
 
 // Error plumbing shared by the host translation units (expects a `ctx`).
@@ -88,7 +89,13 @@ struct grd_ctx {
     if (r_ != GRD_OK) return r_; \
   } while (0)
 
+int grd_ctx_init_stream(grd_ctx* ctx);
 int grd_ctx_init_device(grd_ctx* ctx);
+int grd_alloc_resident(grd_ctx* ctx);
+// On-device layout build (layout_dev.cu).
+int grd_device_layout_check(const grd_csr* graph, uint32_t M, std::string* why);
+int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* mirror_part, bool first);
+int grd_device_in_edges(grd_ctx* ctx);
 void grd_pin_host(grd_ctx* ctx, std::initializer_list<std::vector<uint32_t>*> arrays);
 int grd_dev_alloc_bytes(grd_ctx* ctx, void** p, size_t bytes);
 void grd_prof_mark(grd_ctx* ctx, int i);

@@ -178,6 +178,26 @@ int grd_ctx_create(const grd_csr* graph, const uint32_t* mirror_part,
                    uint32_t num_compute, uint32_t num_memory, int device,
                    grd_ctx** out);
 void grd_ctx_destroy(grd_ctx* ctx);
+
+/* grd_ctx_create with flags.  GRD_CREATE_DEVICE_LAYOUT uploads the CSR (and
+ * mirror_part) as given and builds the partition layout on the device —
+ * proxy discovery, translation slots, relabelled out-edges, hub work items
+ * and, when pull needs it, the in-edge view — instead of on the host
+ * (the DistributedGraph ctor, src/DistributedGraph.cpp:285-785).  Every
+ * resident array equals the host build's, so runs give identical results.
+ * Takes 1..64 memory partitions.  The ctx keeps no host copy of the layout:
+ * grd_upload is refused and grd_ingest re-uploads a CSR instead.  flags = 0
+ * is grd_ctx_create. */
+#define GRD_CREATE_DEVICE_LAYOUT 1u
+int grd_ctx_create_ex(const grd_csr* graph, const uint32_t* mirror_part,
+                      uint32_t num_compute, uint32_t num_memory, int device,
+                      uint32_t flags, grd_ctx** out);
+/* Re-uploads a CSR of the same shape (V, E, weights, and the same partition,
+ * proxy and hub counts) into a GRD_CREATE_DEVICE_LAYOUT ctx and rebuilds
+ * its layout on the device; *bytes_copied = host->device bytes.  Blocks
+ * until the layout is built. */
+int grd_ingest(grd_ctx* ctx, const grd_csr* graph, const uint32_t* mirror_part,
+               uint64_t* bytes_copied);
 const char* grd_last_error(const grd_ctx* ctx);
 /* Error text of the most recent failed grd_ctx_create on this thread. */
 const char* grd_create_error(void);
@@ -281,6 +301,25 @@ int grd_layout_info(const grd_ctx* ctx, uint32_t part, uint32_t* n_owned,
 /* slot -> gid of memory partition `part` (owned slots, then proxy slots). */
 int grd_layout_slots(const grd_ctx* ctx, uint32_t part, uint32_t* host,
                      size_t count);
+
+/* Copies one resident layout array to the host (either build).  *bytes gets
+ * its size; host == NULL only queries it.  The in-edge arrays exist once
+ * pull has been set up (GRD_PR_PULL, GRD_DIR_PULL or the learned policy).
+ * Hub entries are (slot, e0, e1) u32 triples. */
+#define GRD_LAYOUT_SLOT_GID 0 /* [S] gid of each slot, 0xFFFFFFFF padding  */
+#define GRD_LAYOUT_ROW_OFF  1 /* [S+1] out-edge offsets                    */
+#define GRD_LAYOUT_COL      2 /* [E] destination slot of each out-edge     */
+#define GRD_LAYOUT_WGT      3 /* [E] its weight (weighted graphs)          */
+#define GRD_LAYOUT_OUTDEG   4 /* [V] out-degree of each gid                */
+#define GRD_LAYOUT_OWN_SLOT 5 /* [V] owned slot of each gid                */
+#define GRD_LAYOUT_HUBS     6 /* hub work items of the push map            */
+#define GRD_LAYOUT_IN_OFF   7 /* [S+1] in-edge offsets                     */
+#define GRD_LAYOUT_IN_SRC   8 /* [E] source slot of each in-edge           */
+#define GRD_LAYOUT_IN_WGT   9 /* [E] its weight                            */
+#define GRD_LAYOUT_IN_HUBS 10 /* destinations pulled per block             */
+#define GRD_LAYOUT_IN_MEDS 11 /* destinations pulled per warp              */
+int grd_read_layout(grd_ctx* ctx, int which, void* host, size_t cap_bytes,
+                    size_t* bytes);
 
 /* Host-only preview of the same slot space without a device: writes the
  * slot -> gid order of partition `part` (up to cap entries) and its sizes. */
