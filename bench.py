@@ -236,9 +236,11 @@ def bench_ingest(g, args, G_cc, G_ss, p_cc, p_ss, local, barrier, dev) -> dict:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             for c, G, p in zip(dctx, (G_cc, G_ss), (p_cc, p_ss)):
-                c.ingest(G, p)
+                c.ingest(G, p)  # SSSP's upload and build overlap CC's run
                 c.init()
-                c.run()
+                c.run(wait=False)
+            for c in dctx:
+                c.wait()
                 c.read_props()
         barrier()
         thr, _, _ = job_throughput(args.steps * E, time.perf_counter() - t0, dev)
@@ -407,6 +409,7 @@ def workload_config(scale, seed, G_cc, G_ss) -> dict:
         "E_cc_symmetrised": G_cc.num_edges, "E_sssp": G_ss.num_edges,
         "partitions": f"1C+{NUM_MEMORY}M edge-balanced contiguous",
         "l2": "inputs larger than L2 (CSR indices 0.27-0.5 GB > 129 MB), no flush",
+        "streams": "CC then SSSP within a step, each on its own ctx stream",
     }
 
 
@@ -456,6 +459,9 @@ def main():
     slots = {id(c): sum(sum(c.layout_info(p)[:2]) for p in range(NUM_MEMORY)) for c in (ctx_cc, ctx_ss)}
 
     def step(host_loop=False):
+        """Both algorithms to convergence, one after the other (run
+        concurrently on their two streams they were slower: their full-wave
+        push kernels compete for the SMs and L2)."""
         out = []
         for c in (ctx_cc, ctx_ss):
             c.init()
@@ -565,9 +571,9 @@ def main():
     h2d = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for c in (ctx_cc, ctx_ss):  # queued on each ctx's stream: SSSP's copy overlaps CC's run
+        for c in (ctx_cc, ctx_ss):  # queued on each ctx's stream
             h2d += c.upload()
-        for c in (ctx_cc, ctx_ss):
+        for c in (ctx_cc, ctx_ss):  # SSSP's copy overlaps CC's run
             c.init()
             c.run()
             c.read_props()

@@ -315,13 +315,22 @@ class Context:
             out[f] = list(v) if isinstance(v, C.Array) else v
         return out
 
-    def run(self, strict: bool = False, host_loop: bool = False) -> dict:
+    def run(self, strict: bool = False, host_loop: bool = False, wait: bool = True) -> dict:
         """Runs to convergence (or the round cap).  By default the rounds run
         as one device-driven CUDA-graph launch; host_loop=True drives them
-        from the host instead."""
+        from the host instead.  wait=False queues the launch and returns at
+        once (GRD_RUN_ASYNC): call wait() for the finished statistics, so
+        that the runs of several contexts overlap on the GPU."""
         s = _ffi.grd_stats()
-        flags = (GRD_RUN_STRICT if strict else 0) | (_ffi.GRD_RUN_HOST_LOOP if host_loop else 0)
+        flags = ((GRD_RUN_STRICT if strict else 0) | (_ffi.GRD_RUN_HOST_LOOP if host_loop else 0) |
+                 (0 if wait else _ffi.GRD_RUN_ASYNC))
         self._check(self._lib.grd_run(self._ctx, flags, C.byref(s)))
+        return self._stats_dict(s)
+
+    def wait(self) -> dict:
+        """Completes a run started with wait=False; returns its statistics."""
+        s = _ffi.grd_stats()
+        self._check(self._lib.grd_wait(self._ctx, C.byref(s)))
         return self._stats_dict(s)
 
     def stats(self) -> dict:

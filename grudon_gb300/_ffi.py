@@ -32,6 +32,7 @@ LAYOUT_ARRAYS = {"slot_gid": 0, "row_off": 1, "col": 2, "wgt": 3, "outdeg": 4, "
                  "in_off": 7, "in_src": 8, "in_wgt": 9, "in_hubs": 10, "in_meds": 11}
 GRD_RUN_STRICT = 1
 GRD_RUN_HOST_LOOP = 2
+GRD_RUN_ASYNC = 4
 
 ERROR_NAMES = {
     GRD_E_INVALID: "GRD_E_INVALID", GRD_E_OOM: "GRD_E_OOM", GRD_E_CUDA: "GRD_E_CUDA",
@@ -117,6 +118,7 @@ SIGNATURES = {
     "grd_ctx_create_ex": (C.c_int, [C.POINTER(grd_csr), u32p, C.c_uint32, C.c_uint32, C.c_int, C.c_uint32,
                                     C.POINTER(C.c_void_p)]),
     "grd_ingest": (C.c_int, [C.c_void_p, C.POINTER(grd_csr), u32p, u64p]),
+    "grd_wait": (C.c_int, [C.c_void_p, C.POINTER(grd_stats)]),
     "grd_read_layout": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "grd_set_algo": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(grd_params)]),
     "grd_init": (C.c_int, [C.c_void_p]),

@@ -529,6 +529,11 @@ int grd_read_counters(grd_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->h_counters, ctx->st.counters, sizeof(unsigned long long) * NUM_COUNTERS,
                      cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return grd_fold_counters(ctx);
+}
+
+// Folds the host copy of the counters into the stats.
+int grd_fold_counters(grd_ctx* ctx) {
   ctx->stats.edges_scanned = ctx->h_counters[C_EDGES] + ctx->pull.edges;
   ctx->stats.bytes_synced = ctx->h_counters[C_BYTES];
   ctx->stats.reference_bytes_moved = ctx->h_counters[C_REFBYTES];
@@ -695,6 +700,7 @@ int grd_ingest(grd_ctx* ctx, const grd_csr* graph, const uint32_t* mirror_part, 
     return GRD_E_INVALID;
   }
   CK(cudaSetDevice(ctx->device));
+  TRY(grd_wait(ctx, nullptr));
   const int rc = grd_device_layout_build(ctx, graph, mirror_part, false);
   if (bytes_copied) *bytes_copied = ctx->upload_bytes;
   return rc;
@@ -732,6 +738,7 @@ int grd_upload(grd_ctx* ctx, uint64_t* bytes_copied) {
 
 int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
   if (!ctx) return GRD_E_INVALID;
+  TRY(grd_wait(ctx, nullptr));  // the loop graph of a queued run must finish before it is replaced
   if (algo < GRD_PR_DELTA || algo > GRD_SSSP_W) {
     ctx->err = "unknown algorithm id";
     return GRD_E_INVALID;
@@ -799,6 +806,7 @@ int grd_init(grd_ctx* ctx) {
     return GRD_E_INVALID;
   }
   CK(cudaSetDevice(ctx->device));
+  TRY(grd_wait(ctx, nullptr));
   CK(cudaMemsetAsync(ctx->st.counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, ctx->stream));
   CK(cudaMemsetAsync(ctx->st.lc, 0, sizeof(uint32_t) * NUM_LIST_COUNTERS, ctx->stream));
   const uint64_t n = std::max<uint64_t>(ctx->g.S, ctx->g.V);
@@ -919,13 +927,20 @@ int grd_update(grd_ctx* ctx, uint64_t* frontier_size) {
 int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
   TRY(check_ready(ctx));
   CK(cudaSetDevice(ctx->device));
+  TRY(grd_wait(ctx, nullptr));  // a previous asynchronous run first
   bool device_loop = false;
+  const bool async = (flags & GRD_RUN_ASYNC) != 0;
   if (ctx->algo != GRD_PR_PULL && !ctx->profiling && !(flags & GRD_RUN_HOST_LOOP) &&
       ctx->stats.rounds < ctx->params.max_rounds)
-    TRY(grd_graph_run(ctx, &device_loop));
+    TRY(grd_graph_run(ctx, &device_loop, async));
   ctx->stats.device_loop = device_loop ? 1 : 0;
   if (device_loop) {
-    // the whole loop ran as one graph launch
+    // the whole loop ran (or, async, is queued) as one graph launch
+    if (ctx->run_pending) {
+      ctx->strict_pending = (flags & GRD_RUN_STRICT) != 0;
+      if (stats) *stats = ctx->stats;
+      return GRD_OK;  // grd_wait completes the statistics
+    }
   } else if (ctx->algo == GRD_PR_PULL) {
     TRY(grd_pull_run(ctx));
   } else {
@@ -987,6 +1002,24 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
     ctx->err = "round cap reached with a non-empty frontier";
     return GRD_E_ROUND_CAP;
   }
+  return GRD_OK;
+}
+
+int grd_wait(grd_ctx* ctx, grd_stats* stats) {
+  if (!ctx) return GRD_E_INVALID;
+  if (ctx->run_pending) {
+    ctx->run_pending = false;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    TRY(grd_fold_counters(ctx));
+    TRY(grd_graph_run_finish(ctx));
+    if (ctx->strict_pending && !ctx->stats.converged) {
+      ctx->err = "round cap reached with a non-empty frontier";
+      if (stats) *stats = ctx->stats;
+      return GRD_E_ROUND_CAP;
+    }
+  }
+  if (stats) *stats = ctx->stats;
   return GRD_OK;
 }
 

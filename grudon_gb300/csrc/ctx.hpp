@@ -62,6 +62,8 @@ struct grd_ctx {
   size_t verify_cap = 0;
   bool has_policy = false;
   bool device_layout = false;  // layout built on the device (no host copy of its arrays)
+  bool run_pending = false;    // a GRD_RUN_ASYNC loop launch not yet waited for
+  bool strict_pending = false; // ... run with GRD_RUN_STRICT
 };
 
 // Error plumbing shared by the host translation units (expects a `ctx`).
@@ -105,6 +107,7 @@ int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks);
 int grd_upload_layout(grd_ctx* ctx);
 int grd_ensure_in_edges(grd_ctx* ctx);
 int grd_read_counters(grd_ctx* ctx);
+int grd_fold_counters(grd_ctx* ctx);
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused);
 int grd_enqueue_edge_map(grd_ctx* ctx);
 // Round modes: direction x sync format.  Values are the SWITCH branch indices
@@ -142,8 +145,11 @@ int grd_enqueue_round(grd_ctx* ctx, int mode);
 // the fixed rule).
 grd::PolicyArgs grd_policy_args(const grd_ctx* ctx);
 const grd_policy_model* grd_policy_model_dev(const grd_ctx* ctx);
-// Device-driven loop (graph_run.cu).
-int grd_graph_run(grd_ctx* ctx, bool* used);
+// Device-driven loop (graph_run.cu).  async: queue the launch and the
+// counter read-back only (ctx->run_pending); grd_graph_run_finish folds them
+// once the stream has drained.
+int grd_graph_run(grd_ctx* ctx, bool* used, bool async = false);
+int grd_graph_run_finish(grd_ctx* ctx);
 // One round in `mode` as one graph launch (built on first use).
 int grd_round_graph_launch(grd_ctx* ctx, int mode);
 void grd_graph_release(grd_ctx* ctx);

@@ -163,7 +163,7 @@ int grd_round_graph_launch(grd_ctx* ctx, int mode) {
 // Runs the rest of the algorithm as one graph launch.  Returns GRD_OK with
 // *used = false when the graph cannot be built here (the caller then runs the
 // host-driven loop); the reason is kept in ctx->graph_error.
-int grd_graph_run(grd_ctx* ctx, bool* used) {
+int grd_graph_run(grd_ctx* ctx, bool* used, bool async) {
   *used = false;
   if (ctx->graph_failed) return GRD_OK;
   if (!ctx->run_exec) {
@@ -199,7 +199,20 @@ int grd_graph_run(grd_ctx* ctx, bool* used) {
   CK(cudaMemcpyAsync(ctx->st.counters + C_NOOFF_ROUNDS, seed + 8, sizeof(unsigned long long), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(cudaGraphLaunch(ctx->run_exec, ctx->stream));
+  *used = true;
+  if (async) {
+    CK(cudaMemcpyAsync(ctx->h_counters, ctx->st.counters, sizeof(unsigned long long) * NUM_COUNTERS,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->run_pending = true;
+    return GRD_OK;
+  }
   TRY(grd_read_counters(ctx));
+  return grd_graph_run_finish(ctx);
+}
+
+// Statistics of a finished loop launch (its counters already on the host).
+int grd_graph_run_finish(grd_ctx* ctx) {
+  if (!ctx->run_exec) return GRD_OK;
   const unsigned long long* c = ctx->h_counters;
   ctx->stats.rounds = (uint32_t)c[C_ROUNDS];
   ctx->stats.push_rounds = (uint32_t)c[C_PUSH_ROUNDS];
@@ -209,6 +222,5 @@ int grd_graph_run(grd_ctx* ctx, bool* used) {
   ctx->stats.no_offload_rounds = (uint32_t)c[C_NOOFF_ROUNDS];
   ctx->stats.kernel_launches += c[C_LAUNCHES];
   ctx->stats.converged = c[C_FRONTIER] == 0;
-  *used = true;
   return GRD_OK;
 }

@@ -88,6 +88,10 @@ extern "C" {
 #define GRD_RUN_HOST_LOOP 2u /* flag: drive rounds from the host (one
                                 synchronisation per round) instead of the
                                 device-driven CUDA-graph loop */
+#define GRD_RUN_ASYNC 4u     /* flag: queue the device-driven loop and return
+                                at once; grd_wait completes the run and its
+                                statistics (runs that cannot use the device
+                                loop still return finished) */
 
 /* Host CSR as handed to the library: row_offsets has num_vertices+1 entries
  * (u64, like the reference's LC_CSR_Graph row ends), col_indices num_edges
@@ -248,6 +252,10 @@ int grd_aggregate_values_noalloc(grd_ctx* ctx, const uint32_t* gids,
 /* Full run: init() already called; loops rounds until the frontier is empty
  * or params.max_rounds.  flags: GRD_RUN_STRICT. */
 int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats);
+/* Completes a GRD_RUN_ASYNC run (no-op otherwise) and copies the stats.
+ * Every call that changes the ctx's algorithm, init state or layout waits
+ * first; the result reads are stream-ordered behind the run. */
+int grd_wait(grd_ctx* ctx, grd_stats* stats);
 int grd_get_stats(const grd_ctx* ctx, grd_stats* stats);
 /* Per-stage CUDA-event timing inside grd_run (off by default).  While it is
  * on, grd_run drives the rounds from the host and records one grd_round_rec

@@ -143,3 +143,42 @@ def test_device_verify(gpu):
         order = np.lexsort((np.arange(len(ranks)), -ranks.astype(np.float64)))[:20]
         assert r["top_ids"] == [int(i) for i in order]
         np.testing.assert_array_equal(np.array(r["top_values"], dtype=np.float32), ranks[order])
+
+
+@pytest.mark.gpu
+def test_async_runs_overlap_and_match(gpu):
+    """GRD_RUN_ASYNC: two contexts' loops queued back to back give the same
+    results and statistics as blocking runs; calls that change the ctx wait
+    for a queued run first."""
+    G1 = g.Graph.rmat(13, 8, symmetrize=True, weighted=True)
+    G2 = g.Graph.rmat(13, 16, weighted=True)
+    with g.Context(G1, G1.partition_edge_balanced(3), num_memory=3) as a, \
+            g.Context(G2, G2.partition_edge_balanced(3), num_memory=3) as b:
+        a.set_algo(g.GRD_CC)
+        b.set_algo(g.GRD_SSSP_W)
+        ref = []
+        for c in (a, b):
+            c.init()
+            st = c.run()
+            ref.append((c.read_props(), st))
+        for c in (a, b):
+            c.init()
+            c.run(wait=False)
+        got = [c.wait() for c in (a, b)]
+        for c, (props, st), st2 in zip((a, b), ref, got):
+            np.testing.assert_array_equal(c.read_props(), props)
+            assert st2["device_loop"] == 1
+            for k in ("rounds", "converged", "edges_scanned", "bytes_synced", "reference_bytes_moved",
+                      "push_rounds", "pull_rounds", "kernel_launches"):
+                assert st2[k] == st[k], k
+        # a queued run, then init and set_algo without wait(): both wait for it
+        a.init()
+        a.run(wait=False)
+        a.set_algo(g.GRD_SSSP_HOP)
+        a.init()
+        st = a.run()
+        ref = O.run(O.ORC_SSSP_HOP, G1.row_offsets, G1.col_indices, mirror=G1.partition_edge_balanced(3),
+                    num_memory=3)
+        np.testing.assert_array_equal(a.read_props(), ref["props"])
+        assert st["rounds"] == ref["stats"]["rounds"]
+        assert a.wait()["rounds"] == st["rounds"]
