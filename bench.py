@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--kernel-run-pr", action="store_true",
                     help="only run PageRank (Jacobi pull, RMAT-{pr-scale}) for warmup + steps iterations and print a "
                          "short summary: the target of per-kernel profilers")
+    ap.add_argument("--ingest-run", action="store_true",
+                    help="only build the partition layouts of the workload's graphs on the GPU "
+                         "(grd_ingest, warmup + steps times each), for profiling")
     ap.add_argument("--kernel-run", action="store_true",
                     help="only run the workload's steps with the rounds driven from the host (plain kernel "
                          "launches, no CUDA graphs) and print a short summary: the target of per-kernel profilers")
@@ -441,6 +444,15 @@ def main():
     seed, G_cc, G_ss = make_graphs(args.scale, threads)
     p_cc = G_cc.partition_edge_balanced(NUM_MEMORY)
     p_ss = G_ss.partition_edge_balanced(NUM_MEMORY)
+    if args.ingest_run:
+        for G, p in ((G_cc, p_cc), (G_ss, p_ss)):
+            with g.Context(G, p, num_memory=NUM_MEMORY, device=local, device_layout=True) as c:
+                for _ in range(args.warmup + args.steps):
+                    c.ingest(G, p)
+        if rank == 0:
+            print(json.dumps({"ingest_run": True, "scale": args.scale,
+                              "builds_per_graph": 1 + args.warmup + args.steps}), flush=True)
+        return
     ctx_cc = g.Context(G_cc, p_cc, num_memory=NUM_MEMORY, device=local)
     ctx_ss = g.Context(G_ss, p_ss, num_memory=NUM_MEMORY, device=local)
     model = load_policy_model()

@@ -893,26 +893,35 @@ static __global__ void __launch_bounds__(256) k_deg_down(DevGraph g, DevState st
 }
 
 // One warp per 256-edge chunk.  The warp stages a window of up to LBS_WIN
-// consecutive actives (their DP, row start and source value) in shared
-// memory, 32 at a time with coalesced loads, only as many as the chunk's
-// edges need (one group of 32 for a typical degree) — one window covers the
-// whole chunk unless more than LBS_WIN actives fall inside it.  The source of each
-// of the window's edge positions comes from a mark-and-scan in shared memory
-// (every active marks the position where its row starts, then a running max
-// over the 256 positions), so an edge costs one shared load to find its row
-// and lanes read consecutive edge slots.  All 8 edges of a lane are loaded
+// consecutive actives (their DP, row start minus DP, and source value) in
+// shared memory, 32 at a time with coalesced loads, only as many as the
+// chunk's edges need (one group of 32 for a typical degree) — one window
+// covers the whole chunk unless more than LBS_WIN actives fall inside it.
+// The row of each of the window's edge positions comes from a mark-and-scan:
+// every active with edges marks the position where its row starts, then a
+// running max over the 256 positions.  Marks carry a per-warp generation
+// number above the window index, so the mark array is never cleared: the
+// current window always marks position 0, and its marks outrank every older
+// one.  An edge then costs three shared loads (its row, the row's edge base,
+// the source value), and lane l takes positions l, l+32, ...: one load
+// instruction of the warp reads 32 consecutive edges, whose destinations
+// (sorted within a row) share sectors.  All 8 edges of a lane are loaded
 // (index, weight, current value) before any update is issued, keeping 8
 // independent memory chains in flight per lane.
 constexpr uint32_t LBS_WIN = 256;
+constexpr int LBS_JBITS = 9;  // window index bits of a mark
+static_assert(LBS_WIN <= (1u << LBS_JBITS), "window index fits its mark field");
 
 template <int A, bool kDense, bool kCompute = false>
 __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
   static_assert(!(kDense && kCompute), "NO_OFFLOAD rounds use the sparse form");
   constexpr int B = LBS_CHUNK / 32;
   constexpr int SW = LBS_WIN / 32;
-  __shared__ uint32_t s_dp[8][LBS_WIN];
-  __shared__ uint32_t s_rb[8][LBS_WIN];
-  __shared__ uint32_t s_sv[8][LBS_WIN];
+  constexpr uint32_t GEN_MAX = (1u << (32 - LBS_JBITS)) - 1u;
+  static_assert(LBS_CHUNK == 8 * 32, "each lane owns 8 consecutive edge positions");
+  __shared__ uint32_t s_dp[8][LBS_WIN];   // DP of window active j
+  __shared__ uint32_t s_bmd[8][LBS_WIN];  // its row start - DP: edge index = bmd + position
+  __shared__ uint32_t s_sv[8][LBS_WIN];   // its source value
   __shared__ uint32_t s_src[8][LBS_CHUNK];
   const uint32_t K = (uint32_t)__ldcg(&st.counters[C_ACTIVE]);
   const uint32_t m = (uint32_t)__ldcg(&st.counters[C_MEDGES]);
@@ -920,19 +929,23 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
   const uint32_t nchunks = (m + LBS_CHUNK - 1) / LBS_CHUNK;
   const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
   uint32_t* dp = s_dp[w];
-  uint32_t* rbs = s_rb[w];
+  uint32_t* bmd = s_bmd[w];
   uint32_t* svs = s_sv[w];
   uint32_t* srcs = s_src[w];
+  uint32_t gen = GEN_MAX;  // the first step clears the marks
   for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + w; c < nchunks; c += nwarps) {
     uint32_t e = c * LBS_CHUNK;
     const uint32_t e_end = min(m, e + LBS_CHUNK);
     uint32_t i0 = st.chunk_start[c];
     while (e < e_end) {
+      if (gen == GEN_MAX) {  // start (and, in principle, generation wrap): clear the marks
+#pragma unroll
+        for (int q = 0; q < B; ++q) srcs[B * lane + q] = 0;
+        gen = 0;
+      }
+      ++gen;
       // Load the window 32 actives at a time, only as far as the chunk
       // needs: `cover` is the DP of the first active not loaded.
-      static_assert(LBS_CHUNK == 8 * 32, "each lane owns 8 consecutive edge positions");
-#pragma unroll
-      for (int q = 0; q < 8; ++q) srcs[8 * lane + q] = 0;
       uint32_t nw = 0, cover;
       do {
         const uint32_t idx = i0 + nw * 32 + lane;
@@ -942,7 +955,7 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
         const uint32_t nx = i0 + nw * 32 + 32;
         const uint32_t tl = (lane == 31) ? (nx < K ? st.DP[nx] : m) : 0u;
         dp[nw * 32 + lane] = av;
-        rbs[nw * 32 + lane] = bv;
+        bmd[nw * 32 + lane] = bv - av;
         svs[nw * 32 + lane] = source_value<A>(vv);
         cover = __shfl_sync(FULL, tl, 31);
         ++nw;
@@ -952,22 +965,24 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
       // mark: the row of window active j starts at position dp[j] - e (the
       // first active's row may start before the window: position 0).  Only
       // rows with edges mark, so no two actives share a position.
+      const uint32_t tag = gen << LBS_JBITS;
 #pragma unroll
       for (int k = 0; k < SW; ++k) {
         const uint32_t j = k * 32 + lane;
         if ((uint32_t)k < nw) {
           const uint32_t aj = dp[j];
           const uint32_t next = j + 1 < nw * 32 ? dp[j + 1] : cover;
-          if (aj < wend && next > aj) srcs[(aj > e ? aj : e) - e] = j;
+          if (aj < wend && next > aj) srcs[(aj > e ? aj : e) - e] = tag | j;
         }
       }
       __syncwarp();
-      // scan: running max over the positions (lane-local 8, then the warp)
+      // scan: running max over the positions (lane-local 8, then the warp),
+      // written back as window indices
       {
-        uint32_t loc[8], run = 0;
+        uint32_t loc[B], run = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          run = max(run, srcs[8 * lane + q]);
+        for (int q = 0; q < B; ++q) {
+          run = max(run, srcs[B * lane + q]);
           loc[q] = run;
         }
         uint32_t inc = run;
@@ -979,7 +994,7 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
         uint32_t ex = __shfl_up_sync(FULL, inc, 1);
         if (lane == 0) ex = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) srcs[8 * lane + q] = max(ex, loc[q]);
+        for (int q = 0; q < B; ++q) srcs[B * lane + q] = max(ex, loc[q]);  // the lane's own positions
       }
       __syncwarp();
       uint32_t dst[B], cand[B], cur[B];
@@ -989,8 +1004,8 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
         dst[k] = 0xFFFFFFFFu;
         cand[k] = 0;
         if (eid < wend) {
-          const uint32_t j = srcs[k * 32 + lane];
-          const uint32_t ed = rbs[j] + (eid - dp[j]);
+          const uint32_t j = srcs[k * 32 + lane] & ((1u << LBS_JBITS) - 1u);
+          const uint32_t ed = bmd[j] + eid;
           dst[k] = __ldg(&g.col[ed]);
           cand[k] = svs[j];
           if (A == A_SSSP_W) cand[k] = relax_cand<A>(cand[k], __ldg(&g.wgt[ed]));

@@ -129,13 +129,11 @@ struct CsrIn {
 };
 
 // ---------------------------------------------------------------- phase A --
-// Mirror id, out-degree and row-start mark of every vertex; per-partition
-// owned-vertex and edge counts.
+// Mirror id, out-degree and row-start mark of every vertex.  (Partition
+// sizes come from the sorted partition ids, edge counts from the row
+// offsets: no shared counter for every thread to contend on.)
 __global__ void __launch_bounds__(LT) k_lay_vertex(CsrIn in, uint32_t* mir, uint32_t* outdeg, uint32_t* esrc,
-                                                   unsigned long long* part_cnt, uint32_t* err) {
-  __shared__ unsigned long long s_own[DEV_MAX_PARTS], s_edges[DEV_MAX_PARTS];
-  for (uint32_t i = threadIdx.x; i < DEV_MAX_PARTS; i += blockDim.x) s_own[i] = s_edges[i] = 0;
-  __syncthreads();
+                                                   uint32_t* err) {
   uint32_t bad = 0;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < in.V; v += gridDim.x * blockDim.x) {
     uint32_t p = in.mir_in ? in.mir_in[v] : v % in.M;
@@ -153,15 +151,8 @@ __global__ void __launch_bounds__(LT) k_lay_vertex(CsrIn in, uint32_t* mir, uint
       if (deg) esrc[r0] = v;  // the row's first edge: source of the run that follows
     }
     outdeg[v] = (uint32_t)deg;
-    atomicAdd(&s_own[p], 1ull);
-    if (deg) atomicAdd(&s_edges[p], (unsigned long long)deg);
   }
   if (bad) atomicOr(err, bad);
-  __syncthreads();
-  for (uint32_t p = threadIdx.x; p < in.M; p += blockDim.x) {
-    if (s_own[p]) atomicAdd(&part_cnt[p], s_own[p]);
-    if (s_edges[p]) atomicAdd(&part_cnt[DEV_MAX_PARTS + p], s_edges[p]);
-  }
 }
 
 // Proxy discovery (cross_node_mirrors, src/DistributedGraph.cpp:345-349): a
@@ -317,7 +308,8 @@ __global__ void __launch_bounds__(LT) k_lay_in_gather(const uint32_t* __restrict
   }
 }
 
-// in_off from the sorted destination keys: in_off[s] = first k with key >= s.
+// Bounds of sorted keys: out[s] = first k with key[k] >= s, for s = 0..S
+// (the in-edge offsets; the partition starts of the owned order).
 __global__ void __launch_bounds__(LT) k_lay_in_off(const uint32_t* __restrict__ key, uint64_t E, uint64_t S,
                                                    uint32_t* in_off) {
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k <= E; k += (uint64_t)gridDim.x * blockDim.x) {
@@ -405,12 +397,12 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
   // ---- phase A
   const uint64_t W = ((uint64_t)V + 63) / 64;
   uint32_t *mir = nullptr, *esrc = nullptr, *err = nullptr, *outdeg = nullptr, *pcnt = nullptr, *pre = nullptr;
-  uint32_t *pb = nullptr, *okeys = nullptr, *ovals = nullptr;
-  unsigned long long *bm = nullptr, *part_cnt = nullptr;
+  uint32_t *pb = nullptr, *okeys = nullptr, *ovals = nullptr, *pstart = nullptr;
+  unsigned long long* bm = nullptr;
   TRY(tmp.get(&mir, V));
   TRY(tmp.get(&esrc, E));
   TRY(tmp.get(&err, 1));
-  TRY(tmp.get(&part_cnt, 2 * DEV_MAX_PARTS));
+  TRY(tmp.get(&pstart, M + 1));
   TRY(tmp.get(&bm, W * M));
   TRY(tmp.get(&pcnt, W * M));
   TRY(tmp.get(&pre, W * M + 1));
@@ -423,10 +415,9 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
     outdeg = const_cast<uint32_t*>(ctx->g.outdeg);
   }
   CK(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
-  CK(cudaMemsetAsync(part_cnt, 0, sizeof(unsigned long long) * 2 * DEV_MAX_PARTS, s));
   CK(cudaMemsetAsync(bm, 0, sizeof(unsigned long long) * W * M, s));
   if (E) CK(cudaMemsetAsync(esrc, 0, sizeof(uint32_t) * E, s));
-  k_lay_vertex<<<grid_of(ctx, V), LT, 0, s>>>(in, mir, outdeg, esrc, part_cnt, err);
+  k_lay_vertex<<<grid_of(ctx, V), LT, 0, s>>>(in, mir, outdeg, esrc, err);
   CK_LAUNCH();
   TRY(scan<OpMax>(ctx, tmp, esrc, esrc, E, true, false));
   k_lay_proxy_bits<<<grid_of(ctx, E), LT, 0, s>>>(in, mir, esrc, bm, W, err);
@@ -439,11 +430,12 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
   CK_LAUNCH();
   uint32_t *sk = okeys, *sv = ovals;
   TRY(radix_sort(ctx, tmp, sk, sv, V, bits_for(M - 1)));  // owned gids, partition-major, ascending
+  k_lay_in_off<<<grid_of(ctx, (uint64_t)V + 1), LT, 0, s>>>(sk, V, M, pstart);
+  CK_LAUNCH();
   // sizes to the host
-  std::vector<unsigned long long> h_cnt(2 * DEV_MAX_PARTS);
-  std::vector<uint32_t> h_pb(M + 1);
+  std::vector<uint32_t> h_pb(M + 1), h_ps(M + 1);
   uint32_t h_err = 0;
-  CK(cudaMemcpyAsync(h_cnt.data(), part_cnt, sizeof(unsigned long long) * h_cnt.size(), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h_ps.data(), pstart, sizeof(uint32_t) * (M + 1), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(h_pb.data(), pb, sizeof(uint32_t) * (M + 1), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&h_err, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -453,16 +445,13 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
   }
   Layout& L = ctx->L;
   std::vector<uint32_t> n_owned(M), n_proxy(M);
-  std::vector<uint64_t> part_edges(M);
   for (uint32_t p = 0; p < M; ++p) {
-    n_owned[p] = (uint32_t)h_cnt[p];
-    part_edges[p] = h_cnt[DEV_MAX_PARTS + p];
+    n_owned[p] = h_ps[p + 1] - h_ps[p];
     n_proxy[p] = h_pb[p + 1] - h_pb[p];
   }
   if (first) {
     L.n_owned = n_owned;
     L.n_proxy = n_proxy;
-    L.part_edges = part_edges;
     L.slot_base.assign(M, 0);
     uint64_t S = 0;
     for (uint32_t p = 0; p < M; ++p) {
@@ -496,7 +485,7 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
     CK(cudaMemcpyAsync((void*)ctx->g.part_T, T.data(), sizeof(uint32_t) * M, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)ctx->g.part_owned, L.n_owned.data(), sizeof(uint32_t) * M, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));  // the pageable sources above are locals
-  } else if (n_owned != L.n_owned || n_proxy != L.n_proxy || part_edges != L.part_edges) {
+  } else if (n_owned != L.n_owned || n_proxy != L.n_proxy) {
     ctx->err = "grd_ingest: the graph's partition sizes differ from the ctx's";
     return GRD_E_INVALID;
   }
@@ -523,6 +512,23 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
   k_lay_slot_deg<<<grid_of(ctx, S), LT, 0, s>>>(slot_gid, ctx->st.own_slot, g.outdeg, S, sdeg);
   CK_LAUNCH();
   TRY(scan<OpAdd>(ctx, tmp, sdeg, row_off, S, false, true));
+  {  // edges per partition: its owned rows are contiguous in the row offsets
+    std::vector<uint32_t> ends(2 * M);
+    for (uint32_t p = 0; p < M; ++p) {
+      CK(cudaMemcpyAsync(&ends[2 * p], row_off + L.slot_base[p], sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(&ends[2 * p + 1], row_off + L.slot_base[p] + L.n_owned[p], sizeof(uint32_t),
+                         cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    std::vector<uint64_t> part_edges(M);
+    for (uint32_t p = 0; p < M; ++p) part_edges[p] = ends[2 * p + 1] - ends[2 * p];
+    if (first) {
+      L.part_edges = part_edges;
+    } else if (part_edges != L.part_edges) {
+      ctx->err = "grd_ingest: the graph's partition sizes differ from the ctx's";
+      return GRD_E_INVALID;
+    }
+  }
   k_lay_edges<<<grid_of(ctx, E), LT, 0, s>>>(in, mir, esrc, ctx->st.own_slot, row_off, bm, pre, W, info,
                                              const_cast<uint32_t*>(g.col), const_cast<uint32_t*>(g.wgt));
   CK_LAUNCH();
