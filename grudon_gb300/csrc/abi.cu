@@ -118,6 +118,27 @@ int grd_alloc_resident(grd_ctx* ctx) {
   return GRD_OK;
 }
 
+// Vertex arrays that follow from the slot map and the row offsets: every
+// owned slot s of gid v gives own_slot[v] = s and outdeg[v] = its row length.
+static __global__ void __launch_bounds__(256) k_derive_vertex_arrays(DevGraph g, uint32_t* own_slot,
+                                                                     uint32_t* outdeg) {
+  for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.S; s += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t p = g.tile_part[s / K_TILE_SLOTS];
+    if (s - g.part_base[p] >= g.part_owned[p]) continue;
+    const uint32_t v = g.slot_gid[s];
+    own_slot[v] = (uint32_t)s;
+    outdeg[v] = g.row_off[s + 1] - g.row_off[s];
+  }
+}
+
+// Weights sent as bytes (every weight below 256) widened to the resident
+// u32 array.
+static __global__ void __launch_bounds__(256) k_widen_weights(const uint8_t* __restrict__ w8, uint64_t n,
+                                                              uint32_t* w) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    w[i] = w8[i];
+}
+
 int grd_upload_layout(grd_ctx* ctx) {
   const Layout& L = ctx->L;
   DevGraph& g = ctx->g;
@@ -125,8 +146,13 @@ int grd_upload_layout(grd_ctx* ctx) {
   TRY(upload(ctx, (uint32_t*)g.slot_gid, L.slot_gid));
   TRY(upload(ctx, (uint32_t*)g.row_off, L.row_off));
   TRY(upload(ctx, (uint32_t*)g.col, L.col));
-  if (L.weighted) TRY(upload(ctx, (uint32_t*)g.wgt, L.wgt));
-  TRY(upload(ctx, (uint32_t*)g.outdeg, L.outdeg));
+  if (L.weighted && !ctx->wgt8_host.empty()) {
+    TRY(upload(ctx, ctx->wgt8_dev, ctx->wgt8_host));
+    k_widen_weights<<<(uint32_t)ctx->num_sms * 8, 256, 0, ctx->stream>>>(ctx->wgt8_dev, L.E, (uint32_t*)g.wgt);
+    CK_LAUNCH();
+  } else if (L.weighted) {
+    TRY(upload(ctx, (uint32_t*)g.wgt, L.wgt));
+  }
   if (!L.hubs.empty()) {
     static_assert(sizeof(HubChunk) == sizeof(HubChunkD), "hub chunk layout");
     CK(cudaMemcpyAsync((void*)g.hubs, L.hubs.data(), sizeof(HubChunk) * L.hubs.size(), cudaMemcpyHostToDevice,
@@ -139,7 +165,8 @@ int grd_upload_layout(grd_ctx* ctx) {
   for (uint32_t p = 0; p < L.M; ++p) T[p] = L.T(p);
   TRY(upload(ctx, (uint32_t*)g.part_T, T));
   TRY(upload(ctx, (uint32_t*)g.part_owned, L.n_owned));
-  TRY(upload(ctx, ctx->st.own_slot, ctx->own_slot_host));
+  k_derive_vertex_arrays<<<(uint32_t)ctx->num_sms * 8, 256, 0, ctx->stream>>>(g, ctx->st.own_slot, (uint32_t*)g.outdeg);
+  CK_LAUNCH();
   if (ctx->in_edges_alloc) {
     TRY(upload(ctx, (uint32_t*)g.in_off, L.in_off));
     TRY(upload(ctx, (uint32_t*)g.in_src, L.in_src));
@@ -1243,17 +1270,32 @@ int grd_ctx_init_stream(grd_ctx* ctx) {
 int grd_ctx_init_device(grd_ctx* ctx) {
   TRY(grd_ctx_init_stream(ctx));
   TRY(grd_alloc_resident(ctx));
-  // gid -> owned global slot (the first n_owned slots of each partition).
+  // Weights that all fit a byte travel as bytes (a quarter of the copy).
   const Layout& L = ctx->L;
-  ctx->own_slot_host.assign(L.V, 0);
-  for (uint32_t p = 0; p < L.M; ++p)
-    for (uint32_t k = 0; k < L.n_owned[p]; ++k) ctx->own_slot_host[L.slot_gid[L.slot_base[p] + k]] = L.slot_base[p] + k;
-  grd_pin_host(ctx, {&ctx->L.col, &ctx->L.wgt, &ctx->L.row_off, &ctx->L.slot_gid, &ctx->own_slot_host});
+  if (L.weighted && L.E > 0 &&
+      std::all_of(L.wgt.begin(), L.wgt.begin() + (ptrdiff_t)L.E, [](uint32_t w) { return w < 256u; })) {
+    ctx->wgt8_host.assign(L.wgt.begin(), L.wgt.begin() + (ptrdiff_t)L.E);
+    void* p = nullptr;
+    TRY(grd_dev_alloc_bytes(ctx, &p, L.E));
+    ctx->wgt8_dev = static_cast<uint8_t*>(p);
+  }
+  grd_pin_host(ctx, {&ctx->L.col, &ctx->L.wgt, &ctx->L.row_off, &ctx->L.slot_gid});
+  grd_pin_host_bytes(ctx, ctx->wgt8_host);
   return grd_upload_layout(ctx);
 }
 
 // Pins large host layout arrays so grd_upload copies run at full
 // host->device bandwidth; pageable copies still work if pinning fails.
+void grd_pin_host_bytes(grd_ctx* ctx, std::vector<uint8_t>& v) {
+  if (v.size() < (1u << 20)) return;
+  if (cudaHostRegister(v.data(), v.size(), cudaHostRegisterDefault) == cudaSuccess) {
+    ctx->host_registered.push_back(v.data());
+  } else {
+    (void)cudaGetLastError();
+    std::fprintf(stderr, "grudon: pinning %zu B of host weights failed; uploads use pageable copies\n", v.size());
+  }
+}
+
 void grd_pin_host(grd_ctx* ctx, std::initializer_list<std::vector<uint32_t>*> arrays) {
   for (auto* v : arrays) {
     if (v->size() * sizeof(uint32_t) < (1u << 20)) continue;

@@ -56,7 +56,8 @@ struct grd_ctx {
   // load-balanced push kernel
   cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<void*> host_registered;  // layout arrays pinned for H2D uploads
-  std::vector<uint32_t> own_slot_host;  // gid -> owned global slot (uploaded)
+  std::vector<uint8_t> wgt8_host;  // weights as bytes when all are < 256 (uploaded instead of L.wgt)
+  uint8_t* wgt8_dev = nullptr;     // their device staging copy
   grd_policy_model* policy_dev = nullptr;  // learned round policy (device copy)
   unsigned long long* verify_buf = nullptr;  // grd_verify per-block top ranks
   size_t verify_cap = 0;
@@ -99,6 +100,7 @@ int grd_device_layout_check(const grd_csr* graph, uint32_t M, std::string* why);
 int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* mirror_part, bool first);
 int grd_device_in_edges(grd_ctx* ctx);
 void grd_pin_host(grd_ctx* ctx, std::initializer_list<std::vector<uint32_t>*> arrays);
+void grd_pin_host_bytes(grd_ctx* ctx, std::vector<uint8_t>& v);
 int grd_dev_alloc_bytes(grd_ctx* ctx, void** p, size_t bytes);
 void grd_prof_mark(grd_ctx* ctx, int i);
 void grd_prof_collect(grd_ctx* ctx);

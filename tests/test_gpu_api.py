@@ -182,3 +182,30 @@ def test_async_runs_overlap_and_match(gpu):
         np.testing.assert_array_equal(a.read_props(), ref["props"])
         assert st["rounds"] == ref["stats"]["rounds"]
         assert a.wait()["rounds"] == st["rounds"]
+
+
+@pytest.mark.gpu
+def test_upload_sends_byte_weights_and_derives_vertex_arrays(gpu):
+    """Weights below 256 travel as bytes and are widened on the device;
+    out-degrees and owned slots are derived there.  Re-uploads keep every
+    result, and a graph with wide weights still uploads them as u32."""
+    G = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
+    rng = np.random.default_rng(5)
+    wide = g.Graph.from_csr(G.row_offsets, G.col_indices, rng.integers(1, 1_000_000, G.num_edges, dtype=np.uint32))
+    part = G.partition_edge_balanced(3)
+    sizes = []
+    for graph in (G, wide):
+        ref = O.run(O.ORC_SSSP_W, graph.row_offsets, graph.col_indices, graph.weights, mirror=part, num_memory=3)
+        with g.Context(graph, part, num_memory=3) as ctx, \
+                g.Context(graph, part, num_memory=3, device_layout=True) as dctx:
+            ctx.set_algo(g.GRD_SSSP_W)
+            for _ in range(2):
+                sizes.append(ctx.upload())
+                ctx.init()
+                ctx.run()
+                np.testing.assert_array_equal(ctx.read_props(), ref["props"])
+            for name in ("wgt", "outdeg", "own_slot"):
+                np.testing.assert_array_equal(ctx.read_layout(name), dctx.read_layout(name), err_msg=name)
+            np.testing.assert_array_equal(ctx.read_layout("outdeg"), np.diff(graph.row_offsets).astype(np.uint32))
+    assert sizes[0] == sizes[1] and sizes[2] == sizes[3]
+    assert sizes[2] - sizes[0] == 3 * G.num_edges
