@@ -571,24 +571,38 @@ def main():
     for c in (ctx_cc, ctx_ss):
         c.set_profiling(False)
 
-    # Host->device bandwidth of the layout upload alone (both graphs).
-    barrier()
-    t0 = time.perf_counter()
-    up_bytes = sum(c.upload() for c in (ctx_cc, ctx_ss))
-    barrier()
-    upload_gbs = up_bytes / (time.perf_counter() - t0) / 1e9
+    # Host->device bandwidth of the layout upload alone (both graphs, best of 3).
+    up_s = []
+    for _ in range(3):
+        barrier()
+        t0 = time.perf_counter()
+        up_bytes = sum(c.upload() for c in (ctx_cc, ctx_ss))
+        barrier()
+        up_s.append(time.perf_counter() - t0)
+    upload_gbs = up_bytes / min(up_s) / 1e9
 
     # End to end through the C ABI with host buffers.
     barrier()
     h2d = 0
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for c in (ctx_cc, ctx_ss):  # queued on each ctx's stream
-            h2d += c.upload()
-        for c in (ctx_cc, ctx_ss):  # SSSP's copy overlaps CC's run
-            c.init()
-            c.run()
-            c.read_props()
+    # Every step copies both graphs' layouts and reads both results back.  The
+    # copies are pipelined with the runs: CC's copy has the link to itself,
+    # SSSP's follows it and overlaps CC's run, and once CC's result is read
+    # the next step's CC copy overlaps SSSP's run.
+    up_done = torch.cuda.Event()
+    h2d += ctx_cc.upload()
+    for k in range(args.steps):
+        up_done.record(s_cc)
+        s_ss.wait_event(up_done)
+        h2d += ctx_ss.upload()
+        ctx_cc.init()
+        ctx_cc.run()
+        ctx_cc.read_props()
+        if k + 1 < args.steps:
+            h2d += ctx_cc.upload()
+        ctx_ss.init()
+        ctx_ss.run()
+        ctx_ss.read_props()
     barrier()
     e2e_thr, _, _ = job_throughput(args.steps * E, time.perf_counter() - t0, dev)
     e2e = {"value": e2e_thr / 1e9, "unit": "GTEPS",

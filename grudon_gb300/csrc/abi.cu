@@ -153,18 +153,18 @@ int grd_upload_layout(grd_ctx* ctx) {
   } else if (L.weighted) {
     TRY(upload(ctx, (uint32_t*)g.wgt, L.wgt));
   }
-  if (!L.hubs.empty()) {
-    static_assert(sizeof(HubChunk) == sizeof(HubChunkD), "hub chunk layout");
-    CK(cudaMemcpyAsync((void*)g.hubs, L.hubs.data(), sizeof(HubChunk) * L.hubs.size(), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    ctx->upload_bytes += sizeof(HubChunk) * L.hubs.size();
-  }
-  TRY(upload(ctx, (uint32_t*)g.tile_part, L.tile_part));
-  TRY(upload(ctx, (uint32_t*)g.part_base, L.slot_base));
-  std::vector<uint32_t> T(L.M);
-  for (uint32_t p = 0; p < L.M; ++p) T[p] = L.T(p);
-  TRY(upload(ctx, (uint32_t*)g.part_T, T));
-  TRY(upload(ctx, (uint32_t*)g.part_owned, L.n_owned));
+  // the small tables, from their pinned copy (a pageable copy would block
+  // the caller until the stream's earlier copies are done)
+  static_assert(sizeof(HubChunk) == sizeof(HubChunkD), "hub chunk layout");
+  const unsigned char* sm = ctx->h_small;
+  const size_t nh = sizeof(HubChunk) * L.hubs.size(), nt = sizeof(uint32_t) * L.tile_part.size(),
+               nm = sizeof(uint32_t) * L.M;
+  if (nh) CK(cudaMemcpyAsync((void*)g.hubs, sm, nh, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync((void*)g.tile_part, sm + nh, nt, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync((void*)g.part_base, sm + nh + nt, nm, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync((void*)g.part_T, sm + nh + nt + nm, nm, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync((void*)g.part_owned, sm + nh + nt + 2 * nm, nm, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->upload_bytes += nh + nt + 3 * nm;
   k_derive_vertex_arrays<<<(uint32_t)ctx->num_sms * 8, 256, 0, ctx->stream>>>(g, ctx->st.own_slot, (uint32_t*)g.outdeg);
   CK_LAUNCH();
   if (ctx->in_edges_alloc) {
@@ -746,6 +746,7 @@ void grd_ctx_destroy(grd_ctx* ctx) {
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+  if (ctx->h_small) cudaFreeHost(ctx->h_small);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   (void)cudaGetLastError();
   delete ctx;
@@ -1281,6 +1282,18 @@ int grd_ctx_init_device(grd_ctx* ctx) {
   }
   grd_pin_host(ctx, {&ctx->L.col, &ctx->L.wgt, &ctx->L.row_off, &ctx->L.slot_gid});
   grd_pin_host_bytes(ctx, ctx->wgt8_host);
+  {  // pinned copy of the small tables: hubs, tile partitions, partition bases, sizes, owned counts
+    const size_t nh = sizeof(HubChunk) * L.hubs.size(), nt = sizeof(uint32_t) * L.tile_part.size(),
+                 nm = sizeof(uint32_t) * L.M;
+    CK(cudaMallocHost((void**)&ctx->h_small, nh + nt + 3 * nm));
+    unsigned char* sm = ctx->h_small;
+    if (nh) std::memcpy(sm, L.hubs.data(), nh);
+    std::memcpy(sm + nh, L.tile_part.data(), nt);
+    std::memcpy(sm + nh + nt, L.slot_base.data(), nm);
+    uint32_t* T = reinterpret_cast<uint32_t*>(sm + nh + nt + nm);
+    for (uint32_t p = 0; p < L.M; ++p) T[p] = L.T(p);
+    std::memcpy(sm + nh + nt + 2 * nm, L.n_owned.data(), nm);
+  }
   return grd_upload_layout(ctx);
 }
 

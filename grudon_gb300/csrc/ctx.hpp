@@ -58,6 +58,7 @@ struct grd_ctx {
   std::vector<void*> host_registered;  // layout arrays pinned for H2D uploads
   std::vector<uint8_t> wgt8_host;  // weights as bytes when all are < 256 (uploaded instead of L.wgt)
   uint8_t* wgt8_dev = nullptr;     // their device staging copy
+  unsigned char* h_small = nullptr;  // pinned small tables of the upload (hubs, tiles, partitions)
   grd_policy_model* policy_dev = nullptr;  // learned round policy (device copy)
   unsigned long long* verify_buf = nullptr;  // grd_verify per-block top ranks
   size_t verify_cap = 0;

@@ -27,6 +27,25 @@ using namespace grd;
 
 namespace {
 
+// Carries the host-side round statistics into the device counters.  A
+// kernel, not a copy: a host-to-device copy would queue behind any large
+// upload another stream has on the copy engine.
+struct LoopSeed {
+  unsigned long long rounds, push_rounds, pull_rounds, actives_total, push_actives, no_offload_rounds;
+};
+
+__global__ void k_seed_loop(DevState st, LoopSeed s) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  st.counters[C_ROUNDS] = s.rounds;
+  st.counters[C_PUSH_ROUNDS] = s.push_rounds;
+  st.counters[C_PULL_ROUNDS] = s.pull_rounds;
+  st.counters[C_ACTIVE_TOTAL] = s.actives_total;
+  st.counters[C_MODE] = 0;
+  st.counters[C_LAUNCHES] = 0;
+  st.counters[C_PUSH_ACTIVES] = s.push_actives;
+  st.counters[C_NOOFF_ROUNDS] = s.no_offload_rounds;
+}
+
 __global__ void k_round_end(DevState st, cudaGraphConditionalHandle wh, uint32_t max_rounds) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   const unsigned long long r = st.counters[C_ROUNDS] + 1;
@@ -183,21 +202,10 @@ int grd_graph_run(grd_ctx* ctx, bool* used, bool async) {
       return GRD_OK;
     }
   }
-  // Carry the host-side round statistics into the device counters.
-  // counters C_ROUNDS .. C_PUSH_ACTIVES, in order
-  unsigned long long* seed = ctx->h_seed;
-  seed[0] = ctx->stats.rounds;
-  seed[1] = ctx->stats.push_rounds;
-  seed[2] = ctx->stats.pull_rounds;
-  seed[3] = ctx->stats.actives_total;
-  seed[4] = 0;  // C_MODE
-  seed[5] = 0;  // C_LAUNCHES
-  seed[6] = ctx->stats.push_actives;
-  seed[8] = ctx->stats.no_offload_rounds;
-  CK(cudaMemcpyAsync(ctx->st.counters + C_ROUNDS, seed, sizeof(unsigned long long) * 7, cudaMemcpyHostToDevice,
-                     ctx->stream));
-  CK(cudaMemcpyAsync(ctx->st.counters + C_NOOFF_ROUNDS, seed + 8, sizeof(unsigned long long), cudaMemcpyHostToDevice,
-                     ctx->stream));
+  const LoopSeed seed{ctx->stats.rounds,        ctx->stats.push_rounds,  ctx->stats.pull_rounds,
+                      ctx->stats.actives_total, ctx->stats.push_actives, ctx->stats.no_offload_rounds};
+  k_seed_loop<<<1, 32, 0, ctx->stream>>>(ctx->st, seed);
+  CK_LAUNCH();
   CK(cudaGraphLaunch(ctx->run_exec, ctx->stream));
   *used = true;
   if (async) {
