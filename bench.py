@@ -562,12 +562,14 @@ def main():
                                   st["pull_rounds"] * (Eg * (8 + wb) + S * 8 + S / 8))
             prof["push_rounds"] += st["push_rounds"]
             prof["pull_rounds"] += st["pull_rounds"]
-            # the load-balanced push kernel alone: DP/RB/SV of each active,
-            # then per edge its column index (+ weight) and the destination peek
+            # the load-balanced push kernel alone, by the push round's
+            # algorithmic bytes: DP/RB/SV of each active (12), then per edge
+            # its column index (4), weight (4, weighted) and the destination's
+            # read-modify-write (8)
             prof["lbs_ms"] += st["lbs_ms"]
             prof["lbs_launches"] += st["lbs_launches"]
             prof["lbs_edges"] += st["lbs_edges"]
-            prof["lbs_bytes"] += st["lbs_actives"] * 12 + st["lbs_edges"] * (8 + wb)
+            prof["lbs_bytes"] += st["lbs_actives"] * 12 + st["lbs_edges"] * (12 + wb)
     for c in (ctx_cc, ctx_ss):
         c.set_profiling(False)
 
