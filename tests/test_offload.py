@@ -200,3 +200,50 @@ def test_gpu_no_offload_multi_source_batch(gpu):
     for p, r, e in out[1:]:
         np.testing.assert_array_equal(p, out[0][0])
         assert (r, e) == out[0][1:]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algo", [g.GRD_CC, g.GRD_SSSP_W])
+def test_gpu_no_offload_sees_values_aggregated_between_rounds(gpu, algo):
+    """grd_aggregate_values before a run lists gids for the next update;
+    NO_OFFLOAD rounds (which append to the same list) keep them."""
+    G = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
+    gids = np.array([5, 77, 5, 1000], dtype=np.uint32)
+    vals = np.array([0, 3, 2, 1], dtype=np.uint32)
+    outs = []
+    with g.Context(G, G.partition_edge_balanced(3), num_memory=3) as ctx:
+        for off in (g.GRD_OFFLOAD_NDP, g.GRD_OFFLOAD_ENGINE, g.GRD_OFFLOAD_NONE):
+            for host_loop in (True, False):
+                ctx.set_algo(algo, offload=off, frontier_format=g.GRD_FMT_LIST)
+                ctx.init()
+                rc = ctx._lib.grd_aggregate_values(ctx._ctx, gids.ctypes.data_as(g._ffi.u32p),
+                                                   vals.ctypes.data_as(g._ffi.u32p), len(gids))
+                assert rc == 0
+                st = ctx.run(host_loop=host_loop)
+                outs.append((ctx.read_props(), ctx.read_updates(), st["rounds"]))
+    for p, u, r in outs[1:]:
+        np.testing.assert_array_equal(p, outs[0][0])
+        np.testing.assert_array_equal(u, outs[0][1])
+        assert r == outs[0][2]
+
+
+@pytest.mark.gpu
+def test_gpu_no_offload_cli(gpu, tmp_path):
+    """The flag-compatible driver accepts --offload and prints the same
+    checksum as the default schedule."""
+    import subprocess
+    from pathlib import Path
+    cli = Path(g.__file__).resolve().parent / "_build" / "grudon"
+    if not cli.exists():
+        pytest.skip("driver not built")
+    G = g.Graph.rmat(11, 8, symmetrize=True)
+    path = tmp_path / "g.gr"
+    G.write_gr(str(path))
+    outs = []
+    for extra in ([], ["--offload", "engine"], ["--offload", "none"]):
+        r = subprocess.run([str(cli), "-g", str(path), "-c", "1", "-m", "2", "-a", "cc", *extra],
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        outs.append([l for l in r.stdout.splitlines() if l.startswith(("CHECKSUM", "STAT"))
+                     and "TotalBytesMoved" not in l])
+    assert outs[1] == outs[0] and outs[2] == outs[0]
