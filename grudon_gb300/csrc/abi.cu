@@ -220,6 +220,10 @@ int dispatch(int algo, F&& f) {
 
 int check_ready(grd_ctx* ctx) {
   if (!ctx) return GRD_E_INVALID;
+  if (!ctx->layout_valid) {
+    ctx->err = "the layout was left incomplete by a failed grd_ingest: ingest a matching graph first";
+    return GRD_E_INVALID;
+  }
   if (ctx->algo < 0) {
     ctx->err = "no algorithm selected (grd_set_algo)";
     return GRD_E_INVALID;
@@ -829,6 +833,10 @@ int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
 
 int grd_init(grd_ctx* ctx) {
   if (!ctx) return GRD_E_INVALID;
+  if (!ctx->layout_valid) {
+    ctx->err = "the layout was left incomplete by a failed grd_ingest: ingest a matching graph first";
+    return GRD_E_INVALID;
+  }
   if (ctx->algo < 0) {
     ctx->err = "no algorithm selected (grd_set_algo)";
     return GRD_E_INVALID;

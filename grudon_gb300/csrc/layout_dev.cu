@@ -372,6 +372,10 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
     ctx->err = "grd_ingest: the graph's size differs from the ctx's";
     return GRD_E_INVALID;
   }
+  // A re-ingest overwrites the resident arrays as it goes; until it has
+  // finished, the ctx refuses to run (a graph that turns out not to match
+  // the ctx's partition, proxy or hub counts leaves it that way).
+  ctx->layout_valid = false;
   cudaStream_t s = ctx->stream;
   Scratch tmp(ctx);
   // inputs
@@ -555,6 +559,7 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
   ctx->upload_bytes = h2d;
   if (ctx->in_edges_alloc) TRY(grd_device_in_edges(ctx));  // a re-ingest rebuilds the pull view too
   CK(cudaStreamSynchronize(s));
+  ctx->layout_valid = true;
   return GRD_OK;
 }
 

@@ -188,3 +188,28 @@ def test_device_layout_rejects_bad_input(gpu):
         assert rc != 0 and "monotone" in why
     rc, why = _create_raw(ro, ci, w, None, 2)
     assert rc == 0, why
+
+
+def test_failed_reingest_leaves_ctx_refusing_until_a_good_one(gpu):
+    """A CSR of the same size but other partition counts fails part-way
+    through grd_ingest; the ctx then refuses to run until a matching graph is
+    ingested again."""
+    G = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
+    part = G.partition_edge_balanced(3)
+    V = G.num_vertices
+    other = g.Graph.from_csr(G.row_offsets, (G.col_indices.astype(np.int64) * 7 + 1) % V, G.weights)
+    ref = O.run(O.ORC_SSSP_W, G.row_offsets, G.col_indices, G.weights, mirror=part, num_memory=3)
+    with g.Context(G, part, num_memory=3, device_layout=True) as ctx:
+        ctx.set_algo(g.GRD_SSSP_W)
+        try:
+            ctx.ingest(other, part)
+            mismatched = False
+        except g.GrdError:
+            mismatched = True
+        if mismatched:
+            with pytest.raises(g.GrdError):
+                ctx.init()
+        ctx.ingest(G, part)
+        ctx.init()
+        ctx.run()
+        np.testing.assert_array_equal(ctx.read_props(), ref["props"])
