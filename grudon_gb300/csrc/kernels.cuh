@@ -634,8 +634,10 @@ struct OpBwdPack {
   }
 };
 
-// Compute-side aggregate of one received value (plugin aggregate()):
-// PageRank addUpdate, CC/SSSP minUpdate, marking the vertex_updates dirty bit.
+// Compute-side aggregate of one received value (plugin aggregate()) in a
+// bitvector round: PageRank addUpdate, CC/SSSP minUpdate.  No dirty bit: the
+// bitvector round's update (k_update) tests every vertex, and its test is
+// false for every vertex whose entry this round left unchanged.
 template <int A>
 __device__ __forceinline__ void aggregate_one(const DevState& st, uint32_t gid, uint32_t v, uint32_t cur) {
   if (A == A_PR_DELTA || A == A_PR_PULL) {
@@ -643,10 +645,8 @@ __device__ __forceinline__ void aggregate_one(const DevState& st, uint32_t gid, 
     // once per partition, so this read-modify-write is race free and the
     // per-vertex summation order is partition 0, 1, ..., M-1.
     st.upd[gid] = __float_as_uint(__fadd_rn(__uint_as_float(cur), __uint_as_float(v)));
-    red_or(st.UD + (gid >> 5), 1u << (gid & 31));
   } else if (v < cur) {
-    const uint32_t old = atomicMin(&st.upd[gid], v);
-    if (v < old) red_or(st.UD + (gid >> 5), 1u << (gid & 31));
+    red_min(st.upd + gid, v);
   }
 }
 
@@ -1715,17 +1715,21 @@ __global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevSt
   if (tid == 0) st.lc[L_UL] = 0;
 }
 
-// Update over the whole dirty bitmap (bitvector rounds): rebuilds the
-// frontier bitmap (frontier.reset() first, src/GraphAlgorithm.cpp:646) and
-// list, clears the dirty bits (clear_uv, :661) and records the frontier's
-// shape.  Block-uniform loop.
+// Update of a bitvector round: rebuilds the frontier bitmap
+// (frontier.reset() first, src/GraphAlgorithm.cpp:646) and list, clears the
+// dirty bits (clear_uv, :661) and records the frontier's shape.  The
+// reference tests its dirty vertices; this tests every vertex, which selects
+// the same ones: after each update, update_frontier's test (CC/SSSP
+// prop > upd, PageRank upd > tol) is false for every vertex, and only an
+// aggregate (this round's, or grd_aggregate_values) can make it true again.
+// Block-uniform loop.
 template <int A>
 __global__ void __launch_bounds__(256) k_update(DevGraph g, DevState st, double tol, double damping) {
   uint32_t fcount = 0, fedges = 0, fmax = 0, visited = 0;
   for (uint32_t base = blockIdx.x * blockDim.x; base < g.V; base += gridDim.x * blockDim.x) {
     const uint32_t v = base + threadIdx.x;
     bool nf = false;
-    if (v < g.V && test_bit(st.UD, v)) {
+    if (v < g.V) {
       nf = update_one<A>(g, st, v, tol, damping, visited);
       if (nf) {
         const uint32_t d = g.outdeg[v];
