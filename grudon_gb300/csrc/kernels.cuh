@@ -596,15 +596,16 @@ struct OpFwdUnpack {
     st.AL[jg] = slot;
   }
 };
-// Fused forward pack + unpack (one pass; the wire buffer is still written).
+// Fused forward pack + unpack (one pass): the value goes straight from the
+// compute side to the memory-side slot; the packed wire buffer, which only
+// carries values between the separate pack and unpack stages, is skipped.
 struct OpFwdXfer {
   __device__ __forceinline__ Payload gather(const DevGraph& g, const DevState& st, uint32_t, uint32_t slot,
                                             uint32_t) const {
     return Payload{st.prop[__ldg(&g.slot_gid[slot])], 0, 0};
   }
   __device__ __forceinline__ void scatter(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
-                                          uint32_t j, uint32_t jg, const Payload& v) const {
-    st.FV[g.part_base[p] + j] = v.v;
+                                          uint32_t, uint32_t jg, const Payload& v) const {
     st.mprop[slot] = v.v;
     st.AL[jg] = slot;
   }
@@ -667,7 +668,7 @@ struct OpAggregate {
     aggregate_one<A>(st, v.gid, v.v, v.cur);
   }
 };
-// Fused backward pack + aggregate.
+// Fused backward pack + aggregate (no wire buffer, as OpFwdXfer).
 template <int A>
 struct OpBwdXfer {
   __device__ __forceinline__ Payload gather(const DevGraph& g, const DevState& st, uint32_t, uint32_t slot,
@@ -675,9 +676,8 @@ struct OpBwdXfer {
     const uint32_t gid = __ldg(&g.slot_gid[slot]);
     return Payload{st.mupd[slot], gid, aggregate_peek<A>(st, gid)};
   }
-  __device__ __forceinline__ void scatter(const DevGraph& g, const DevState& st, uint32_t p, uint32_t slot,
-                                          uint32_t j, uint32_t, const Payload& v) const {
-    st.BV[g.part_base[p] + j] = v.v;
+  __device__ __forceinline__ void scatter(const DevGraph&, const DevState& st, uint32_t, uint32_t slot, uint32_t,
+                                          uint32_t, const Payload& v) const {
     retire_update<A>(st, slot, v.v);
     aggregate_one<A>(st, v.gid, v.v, v.cur);
   }
@@ -1421,7 +1421,6 @@ __global__ void __launch_bounds__(256) k_bwd_list(DevGraph g, DevState st) {
       const uint32_t v = st.mupd[s];
       gid = __ldg(&g.slot_gid[s]);
       retire_update<A>(st, s, v);
-      st.BV[j] = v;
       atomicAnd(&st.MD[s >> 5], ~(1u << (s & 31)));
       if (A == A_PR_DELTA) {
         atomicAdd(reinterpret_cast<float*>(st.upd) + gid, __uint_as_float(v));
@@ -1676,7 +1675,6 @@ __global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevSt
       const uint32_t v = st.mupd[s];
       gid = __ldg(&g.slot_gid[s]);
       retire_update<A>(st, s, v);
-      st.BV[j] = v;
       atomicAnd(&st.MD[s >> 5], ~(1u << (s & 31)));
       if (A == A_PR_DELTA) {
         atomicAdd(reinterpret_cast<float*>(st.upd) + gid, __uint_as_float(v));
