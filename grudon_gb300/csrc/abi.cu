@@ -98,9 +98,6 @@ int grd_alloc_resident(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, &st.BV, S));
   TRY(dev_alloc(ctx, &st.AL, S));
   TRY(dev_alloc(ctx, &st.tile_cnt, T));
-  TRY(dev_alloc(ctx, &st.tile_off, T));
-  TRY(dev_alloc(ctx, &st.tile_goff, T));
-  TRY(dev_alloc(ctx, &st.part_cnt, M));
   TRY(dev_alloc(ctx, &st.DP, S + 1));
   TRY(dev_alloc(ctx, &st.RB, S));
   TRY(dev_alloc(ctx, &st.SV, S));
@@ -326,15 +323,14 @@ static int host_loop_mode(grd_ctx* ctx, int* mode) {
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
   const uint32_t T = ctx->g.num_tiles;
   k_fwd_bits<<<T, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-  k_scan_tiles<<<1, 1024, 0, ctx->stream>>>(ctx->g, ctx->st, 1);
   if (fused) {
-    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdXfer{});
+    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdXfer{}, 2);
   } else {
-    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdPack{});
-    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdUnpack{});
+    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdPack{}, 2);
+    k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdUnpack{}, 0);
   }
   CK_LAUNCH();
-  ctx->stats.kernel_launches += fused ? 3 : 4;
+  ctx->stats.kernel_launches += fused ? 2 : 3;
   return GRD_OK;
 }
 
@@ -351,7 +347,10 @@ uint32_t grd_round_launches(const grd_ctx* ctx, int mode) {
   if (mode == RM_NO_OFFLOAD) return 3 /*fwd list, retire, update list*/ + grd_edge_map_launches(ctx, mode);
   const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
   const uint32_t groups = ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1;
-  const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (3 /*fwd*/ + 2 + groups /*bwd*/ + 1 /*update*/);
+  // bitvector: fwd bits + compaction; the backward tile counts (pull only:
+  // the push map's dirty diff writes them) + one compaction per group; update
+  const uint32_t bwd = (mode == RM_PULL_BITVEC ? 1u : 0u) + groups;
+  const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (2 + bwd + 1);
   return sync + grd_edge_map_launches(ctx, mode);
 }
 
@@ -372,6 +371,7 @@ int grd_enqueue_edge_map(grd_ctx* ctx) {
 }
 
 int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
+  ctx->tile_counts_ready = mode == RM_PUSH_BITVEC;  // k_diff_dirty writes them
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
     const uint32_t pull_hub_grid = std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8));
@@ -408,7 +408,7 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
       k_push_lbs<A, true><<<resident_grid(ctx, k_push_lbs<A, true>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       grd_prof_mark(ctx, 6);
       if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-      k_diff_dirty<A><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      k_diff_dirty<A><<<ctx->g.num_tiles, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     } else if (mode == RM_NO_OFFLOAD) {  // compute-side push into vertex_updates
       k_push_lbs<A, false, true><<<resident_grid(ctx, k_push_lbs<A, false, true>), 256, 0, ctx->stream>>>(ctx->g,
                                                                                                           ctx->st);
@@ -432,10 +432,14 @@ int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate) {
     constexpr int A = decltype(a)::value;
     constexpr bool kPR = (A == A_PR_DELTA);
     if (do_pack) {
-      k_tile_count<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.tile_cnt, ctx->st.FB);
-      k_scan_tiles<<<1, 1024, 0, ctx->stream>>>(ctx->g, ctx->st, 0);
-      if (!fused) k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, nullptr, 0u, ctx->g, ctx->st, OpBwdPack<A>{});
-      ctx->stats.kernel_launches += fused ? 2 : 3;
+      if (!ctx->tile_counts_ready) {  // the push map's dirty diff already counted them
+        k_tile_count<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.tile_cnt, ctx->st.FB);
+        ctx->stats.kernel_launches += 1;
+      }
+      if (!fused) {
+        k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, nullptr, 0u, ctx->g, ctx->st, OpBwdPack<A>{}, 1);
+        ctx->stats.kernel_launches += 1;
+      }
     }
     if (do_aggregate) {
       // PageRank: one launch per partition in ascending order fixes the
@@ -445,10 +449,11 @@ int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate) {
         uint32_t t0 = kPR ? L.slot_base[p] / TILE_SLOTS : 0;
         uint32_t t1 = kPR ? ((p + 1 < L.M) ? L.slot_base[p + 1] / TILE_SLOTS : T) : T;
         if (fused)
-          k_compact<<<t1 - t0, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.MD, t0, ctx->g, ctx->st, OpBwdXfer<A>{});
+          k_compact<<<t1 - t0, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.MD, t0, ctx->g, ctx->st, OpBwdXfer<A>{},
+                                                      1);
         else
           k_compact<<<t1 - t0, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.MD, t0, ctx->g, ctx->st,
-                                                      OpAggregate<A>{});
+                                                      OpAggregate<A>{}, 0);
       }
       ctx->stats.kernel_launches += groups;
     }

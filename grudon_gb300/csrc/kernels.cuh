@@ -34,7 +34,7 @@ enum Counter : int {
   C_EDGES = 2,     // cumulative edges scanned
   C_BYTES = 3,     // cumulative wire bytes (true size)
   C_REFBYTES = 4,  // cumulative bytes by the reference's accounting
-  C_TOTAL = 5,     // total set bits of the last compaction scan
+  // 5: unused
   C_ERR = 6,       // first device-side error code (0 = none)
   C_PULL_EDGES = 7,
   C_MEDGES = 8,    // edges of the load-balanced push this round (non-hub rows)
@@ -96,10 +96,7 @@ struct DevState {
   uint32_t* MD;
   uint32_t* BV;
   uint32_t* AL;
-  uint32_t* tile_cnt;
-  uint32_t* tile_off;
-  uint32_t* tile_goff;
-  uint32_t* part_cnt;
+  uint32_t* tile_cnt;     // set bits per compaction tile of the bitvector being compacted
   uint32_t* DP;           // [S+1] exclusive degree prefix over the active list
   uint32_t* RB;           // [S] row start of each active (active-list order)
   uint32_t* SV;           // [S] property of each active (active-list order)
@@ -373,6 +370,7 @@ static __global__ void __launch_bounds__(256) k_fwd_bits(DevGraph g, DevState st
   const uint32_t t = blockIdx.x;
   if (t == 0 && threadIdx.x == 0) {
     reset_round_counters(st);
+    st.counters[C_ACTIVE] = 0;  // the compaction adds each tile's actives
     st.lc[L_FL] = 0;
     st.lc[L_UL] = 0;  // the bitvector update consumes every dirty bit
   }
@@ -421,59 +419,6 @@ static __global__ void __launch_bounds__(256) k_tile_count(const uint32_t* __res
   if (threadIdx.x == 0) tile_cnt[t] = c;
 }
 
-// Exclusive scan of tile counts, restarting per partition (packed value index
-// j of the j-th set bit) and global (index into the active list).  Also
-// accumulates the wire-size statistics of one sync direction.
-static __global__ void __launch_bounds__(1024) k_scan_tiles(DevGraph g, DevState st, int set_active) {
-  __shared__ uint32_t s_w[32];
-  __shared__ uint32_t s_carry;
-  const uint32_t tid = threadIdx.x, lane = lane_id(), w = tid >> 5;
-  uint32_t gcarry = 0;
-  unsigned long long bytes = 0, refbytes = 0;
-  for (uint32_t p = 0; p < g.M; ++p) {
-    const uint32_t t0 = g.part_base[p] / K_TILE_SLOTS;
-    const uint32_t t1 = (p + 1 < g.M) ? g.part_base[p + 1] / K_TILE_SLOTS : g.num_tiles;
-    if (tid == 0) s_carry = 0;
-    __syncthreads();
-    for (uint32_t c0 = t0; c0 < t1; c0 += blockDim.x) {
-      const uint32_t t = c0 + tid;
-      const uint32_t v = t < t1 ? st.tile_cnt[t] : 0;
-      uint32_t incl = warp_incl_scan(v);
-      if (lane == 31) s_w[w] = incl;
-      __syncthreads();
-      if (w == 0) {
-        uint32_t x = s_w[lane];
-        s_w[lane] = warp_incl_scan(x) - x;
-      }
-      __syncthreads();
-      incl += s_w[w];
-      const uint32_t carry = s_carry;
-      if (t < t1) {
-        st.tile_off[t] = carry + incl - v;
-        st.tile_goff[t] = gcarry + carry + incl - v;
-      }
-      __syncthreads();
-      if (tid == blockDim.x - 1) s_carry = carry + incl;
-      __syncthreads();
-    }
-    const uint32_t kp = s_carry;
-    if (tid == 0) {
-      st.part_cnt[p] = kp;
-      const unsigned long long words64 = ((unsigned long long)g.part_T[p] + 63ull) / 64ull;
-      bytes += words64 * 8ull + (unsigned long long)kp * 4ull;
-      refbytes += words64 * 64ull + (unsigned long long)kp * 4ull;
-    }
-    gcarry += kp;
-    __syncthreads();
-  }
-  if (tid == 0) {
-    st.counters[C_TOTAL] = gcarry;
-    if (set_active) st.counters[C_ACTIVE] = gcarry;
-    st.counters[C_BYTES] += bytes;
-    st.counters[C_REFBYTES] += refbytes;
-  }
-}
-
 // ------------------------------------------------------------- compaction --
 // Fire-and-forget reductions (no returned value, so no round trip).
 __device__ __forceinline__ void red_or(uint32_t* a, uint32_t v) {
@@ -489,6 +434,12 @@ __device__ __forceinline__ void red_add_f32(float* a, float v) {
 // Visits every set bit of `bits` over the tiles [tile_begin, tile_begin +
 // gridDim.x) in ascending slot order with j = the bit's rank inside its
 // partition (packed value index) and jg = its rank over all partitions.
+// Each block first sums the set-bit counts of the tiles before its own
+// (st.tile_cnt, from the kernel that produced the bitvector): a few hundred
+// L2 reads per block instead of a separate one-block scan launch.
+// `count` adds this sync pass's wire bytes to the statistics (1), and also
+// the actives of a forward pass to C_ACTIVE (2); 0 for the second half of a
+// split pass.
 // Phase A: each of the 8 warps loads its K_TILE_WORDS/8 words (coalesced),
 // scans their popcounts and writes the slot of every set bit to a warp-private
 // shared buffer in rank order (shuffles and shared stores only).  Phase B:
@@ -502,7 +453,7 @@ struct Payload {
 template <class Op>
 __global__ void __launch_bounds__(256)
     k_compact(const uint32_t* __restrict__ bits, uint32_t* clear_bits, uint32_t tile_begin, DevGraph g,
-              DevState st, Op op) {
+              DevState st, Op op, int count) {
   constexpr int KW = K_TILE_WORDS / 256;  // 32-word groups per warp
   constexpr int CAP = 32 * 32 * KW;       // slots owned by one warp
   constexpr int U = 4;
@@ -511,6 +462,17 @@ __global__ void __launch_bounds__(256)
   const uint32_t t = tile_begin + blockIdx.x;
   const uint32_t p = g.tile_part[t];
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+  uint32_t pre_p = 0, pre_g = 0;  // set bits before this tile: in its partition, in all
+  {
+    const uint32_t t0 = g.part_base[p] / K_TILE_SLOTS;
+    for (uint32_t i = threadIdx.x; i < t; i += blockDim.x) {
+      const uint32_t c = __ldcg(&st.tile_cnt[i]);
+      pre_g += c;
+      if (i >= t0) pre_p += c;
+    }
+    pre_p = block_sum(pre_p);
+    pre_g = block_sum(pre_g);
+  }
   const size_t wbase = (size_t)t * K_TILE_WORDS + warp * (32 * KW);
   uint32_t x[KW];
   uint32_t c = 0;
@@ -524,8 +486,18 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   uint32_t wb = 0;
   for (uint32_t i = 0; i < warp; ++i) wb += s_wsum[i];
-  const uint32_t run = st.tile_off[t] + wb;
-  const uint32_t grun = st.tile_goff[t] + wb;
+  const uint32_t run = pre_p + wb;
+  const uint32_t grun = pre_g + wb;
+  if (count && threadIdx.x == 0) {
+    uint32_t ct = 0;
+    for (int i = 0; i < 8; ++i) ct += s_wsum[i];
+    // every partition's bitvector once per pass, plus 4 B per packed value
+    unsigned long long b = 4ull * ct, rb = 4ull * ct;
+    if (t == 0) b += g.bv_bytes, rb += g.bv_refbytes;
+    if (b) atomicAdd(&st.counters[C_BYTES], b);
+    if (rb) atomicAdd(&st.counters[C_REFBYTES], rb);
+    if (count == 2 && ct) atomicAdd(&st.counters[C_ACTIVE], (unsigned long long)ct);
+  }
   const uint32_t lt = (1u << lane) - 1u;
   uint32_t* buf = s_slot[warp];
   uint32_t n = 0;
@@ -1118,20 +1090,38 @@ __global__ void __launch_bounds__(256) k_hub_push(DevGraph g, DevState st) {
 // the snapshot taken at its last send (CC/SSSP), or when it received any
 // PageRank contribution (the entry is zeroed after every send and every
 // contribution is positive).  Rebuilds every word of MD.
+// One block per compaction tile: it also writes the tile's dirty count (for
+// the backward compaction) and clears the tile's forward bitvector words,
+// which nothing reads once the edge-map has run.
 template <int A>
 __global__ void __launch_bounds__(256) k_diff_dirty(DevGraph g, DevState st) {
-  for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.S; s += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t a = st.mupd[s];
-    bool dirty;
-    if (A == A_PR_DELTA) {
-      dirty = a != 0u;
-    } else {
-      const uint32_t b = st.snap[s];
-      dirty = a < b;
+  constexpr int U = 8;  // slots in flight per thread
+  static_assert(K_TILE_SLOTS % (256 * U) == 0, "whole steps per tile");
+  const uint32_t t = blockIdx.x;
+  const uint64_t s0 = (uint64_t)t * K_TILE_SLOTS;
+  uint32_t c = 0;
+  for (uint32_t i0 = 0; i0 < K_TILE_SLOTS; i0 += 256 * U) {
+    uint32_t a[U], b[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t s = s0 + i0 + u * 256 + threadIdx.x;
+      a[u] = __ldcg(&st.mupd[s]);
+      b[u] = A == A_PR_DELTA ? 0u : __ldcg(&st.snap[s]);
     }
-    const uint32_t m = __ballot_sync(FULL, dirty);
-    if (lane_id() == 0) st.MD[s >> 5] = m;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t s = s0 + i0 + u * 256 + threadIdx.x;
+      const bool dirty = A == A_PR_DELTA ? a[u] != 0u : a[u] < b[u];
+      const uint32_t m = __ballot_sync(FULL, dirty);
+      if (lane_id() == 0) {
+        st.MD[s >> 5] = m;
+        st.FB[s >> 5] = 0;
+        c += __popc(m);
+      }
+    }
   }
+  c = block_sum(c);
+  if (threadIdx.x == 0) st.tile_cnt[t] = c;
 }
 
 // -------------------------------------------------------------- pull map --

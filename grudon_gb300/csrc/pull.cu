@@ -36,7 +36,7 @@ struct OpPullXfer {
   }
   __device__ __forceinline__ void scatter(const DevGraph& g, const DevState& st, uint32_t p, uint32_t, uint32_t j,
                                           uint32_t, const Payload& v) const {
-    if (pack) st.BV[g.part_base[p] + j] = v.v;
+    if (pack && !merge) st.BV[g.part_base[p] + j] = v.v;  // the wire buffer feeds a separate merge only
     if (merge) {
       float s = __uint_as_float(v.cur), c = __uint_as_float(v.cmp);
       kahan_add(s, c, __uint_as_float(v.v));
@@ -115,14 +115,14 @@ int enqueue_pull_bwd(grd_ctx* ctx, bool pack, bool merge) {
   const Layout& L = ctx->L;
   if (pack) {
     k_tile_count<<<T, 256, 0, ctx->stream>>>(ctx->st.MD, ctx->st.tile_cnt);
-    k_scan_tiles<<<1, 1024, 0, ctx->stream>>>(ctx->g, ctx->st, 0);
-    ctx->stats.kernel_launches += 2;
+    ctx->stats.kernel_launches += 1;
   }
   for (uint32_t p = 0; p < L.M; ++p) {
     const uint32_t t0 = L.slot_base[p] / TILE_SLOTS;
     const uint32_t t1 = (p + 1 < L.M) ? L.slot_base[p + 1] / TILE_SLOTS : T;
     OpPullXfer op{ctx->pull.comp, pack, merge};
-    k_compact<<<t1 - t0, 256, 0, ctx->stream>>>(ctx->st.MD, merge ? ctx->st.MD : nullptr, t0, ctx->g, ctx->st, op);
+    k_compact<<<t1 - t0, 256, 0, ctx->stream>>>(ctx->st.MD, merge ? ctx->st.MD : nullptr, t0, ctx->g, ctx->st, op,
+                                                pack ? 1 : 0);
     ctx->stats.kernel_launches += 1;
   }
   CK_LAUNCH();
