@@ -366,7 +366,42 @@ def cpu_baseline(G_cc, G_ss, p_cc, p_ss, steps: int = 1) -> dict:
             "seconds": t_total,
             "sample": f"{steps} full step(s): CC + weighted SSSP to convergence on the same RMAT-{SCALE} graphs, "
                       f"1C+{NUM_MEMORY}M, oracle restatement of the reference round protocol (reference "
-                      "unbuildable: Galois/MPI absent), {threads} host threads"}
+                      f"unbuildable: Galois/MPI absent), {threads} host threads"}
+
+
+def bench_reference_cpu_case(g, local) -> dict:
+    """The reference's own CPU-runnable case: plain (delta-push) PageRank,
+    damping 0.85, 20 iterations, seeded RMAT-16 ef16, 1 compute + 1 memory
+    partition.  The whole run on the GPU (one device-loop launch, init
+    excluded) beside the oracle restatement on all host threads (run()
+    only), medians."""
+    import numpy as np
+    import torch
+    from oracle import ffi as O
+    G = g.Graph.rmat(16, EF, seed=g.rmat_seed(16, EF))
+    with g.Context(G, None, num_memory=1, device=local) as ctx:
+        ctx.set_algo(g.GRD_PR_DELTA, max_rounds=20)
+        ts = []
+        for k in range(13):
+            ctx.init()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = ctx.run()
+            if k >= 3:
+                ts.append(time.perf_counter() - t0)
+        ranks = ctx.read_ranks()
+    L = O.Layout(G.row_offsets, G.col_indices, num_memory=1)
+    threads = os.cpu_count() or 1
+    cs = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        ref = L.run(O.ORC_PR_DELTA, max_rounds=20, threads=threads)
+        cs.append(time.perf_counter() - t0)
+    gpu_ms, cpu_ms = 1e3 * statistics.median(ts), 1e3 * statistics.median(cs)
+    return {"workload": "PageRank delta push, damping 0.85, 20 iterations, RMAT-16 ef16, 1C+1M",
+            "num_edges": G.num_edges, "rounds": st["rounds"], "gpu_ms": gpu_ms, "cpu_ms": cpu_ms,
+            "cpu_threads": threads, "speedup": cpu_ms / gpu_ms,
+            "max_abs_rank_diff": float(np.abs(ranks - ref["ranks"]).max())}
 
 
 def run_reference(args):
@@ -691,6 +726,7 @@ def main():
         }
         if ws == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(G_cc, G_ss, p_cc, p_ss)
+            line["reference_cpu_case"] = bench_reference_cpu_case(g, local)
             if pr is not None:
                 pr_fp64_check(pr, line["cpu_baseline"])
         if pr is not None:

@@ -279,3 +279,34 @@ def test_pr_pull_converges_and_stage_api(gpu):
             r += 1
         assert r + 1 == st["rounds"]
         np.testing.assert_array_equal(ctx.read_ranks(), full)
+
+
+def test_reference_cpu_case_pagerank_rmat16(gpu, tmp_path):
+    """The reference's own CPU-runnable case: plain PageRank (delta push,
+    damping 0.85) for 20 iterations on seeded RMAT-16 ef16, written as
+    .mtx, 1 compute + 1 memory partition.  Through the .mtx reader, the
+    plugin driver and the C ABI against the oracle."""
+    import subprocess
+    from pathlib import Path
+    G0 = g.Graph.rmat(16, 16, seed=g.rmat_seed(16, 16))
+    path = tmp_path / "rmat16.mtx"
+    G0.write_mtx(str(path))
+    G = g.Graph.read_mtx(str(path))
+    np.testing.assert_array_equal(G.row_offsets, G0.row_offsets)
+    np.testing.assert_array_equal(G.col_indices, G0.col_indices)
+    ref = O.run(O.ORC_PR_DELTA, G.row_offsets, G.col_indices, max_rounds=20)
+    assert ref["stats"]["rounds"] == 20
+    with g.Context(G, None, num_memory=1) as ctx:
+        ctx.set_algo(g.GRD_PR_DELTA, max_rounds=20)
+        ctx.init()
+        st = ctx.run()
+        assert st["rounds"] == 20
+        np.testing.assert_allclose(ctx.read_ranks(), ref["ranks"], rtol=1e-4, atol=2e-5)
+    cli = Path(g.__file__).resolve().parent / "_build" / "grudon"
+    if cli.exists():
+        r = subprocess.run([str(cli), "-g", str(path), "-c", "1", "-m", "1", "-a", "pr", "--max-rounds", "20"],
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        assert "STAT PageRank Iterations 20" in r.stdout, r.stdout
+        total = float(next(l for l in r.stdout.splitlines() if l.startswith("CHECKSUM")).split()[1])
+        assert abs(total - float(ref["ranks"].astype(np.float64).sum())) < 1e-3 * max(1.0, total)
