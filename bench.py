@@ -237,14 +237,22 @@ def bench_ingest(g, args, G_cc, G_ss, p_cc, p_ss, local, barrier, dev) -> dict:
             c.run()
         barrier()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            for c, G, p in zip(dctx, (G_cc, G_ss), (p_cc, p_ss)):
-                c.ingest(G, p)  # SSSP's upload and build overlap CC's run
-                c.init()
-                c.run(wait=False)
-            for c in dctx:
-                c.wait()
-                c.read_props()
+        (cc, ss), graphs = dctx, ((G_cc, p_cc), (G_ss, p_ss))
+        # every step ingests both CSRs and reads both results back; each
+        # ingest overlaps the other graph's queued run
+        cc.ingest(*graphs[0])
+        for k in range(args.steps):
+            cc.init()
+            cc.run(wait=False)
+            ss.ingest(*graphs[1])
+            cc.wait()
+            cc.read_props()
+            ss.init()
+            ss.run(wait=False)
+            if k + 1 < args.steps:
+                cc.ingest(*graphs[0])
+            ss.wait()
+            ss.read_props()
         barrier()
         thr, _, _ = job_throughput(args.steps * E, time.perf_counter() - t0, dev)
     finally:
@@ -253,7 +261,8 @@ def bench_ingest(g, args, G_cc, G_ss, p_cc, p_ss, local, barrier, dev) -> dict:
     return {"host_layout_ms": host_ms, "device_layout_ms": best, "speedup": host_ms / best,
             "device_h2d_bytes": nbytes, "host_threads": os.cpu_count(),
             "e2e_from_host_csr": {"value": thr / 1e9, "unit": "GTEPS",
-                                  "note": "per step: CSR upload + device layout build + both runs + results read"}}
+                                  "note": "per step: CSR upload + device layout build + both runs + results read, "
+                                          "each graph's ingest overlapping the other's run"}}
 
 
 def pr_fp64_check(pr: dict, cpu: dict) -> None:
