@@ -213,3 +213,24 @@ def test_failed_reingest_leaves_ctx_refusing_until_a_good_one(gpu):
         ctx.init()
         ctx.run()
         np.testing.assert_array_equal(ctx.read_props(), ref["props"])
+
+
+@pytest.mark.parametrize("V,edges,M", [(1, [], 1), (7, [], 2), (5, [(0, 1), (1, 0), (3, 4)], 3),
+                                       (70, [(i, (i * 7 + 3) % 70) for i in range(70)], 64)])
+def test_device_layout_tiny_graphs(gpu, V, edges, M):
+    """No edges, one vertex, more partitions than owned vertices in some."""
+    src = [a for a, _ in edges]
+    dst = [b for _, b in edges]
+    G = g.Graph.from_edges(V, src, dst, [1 + (a * 3 + b) % 9 for a, b in edges])
+    with g.Context(G, None, num_memory=M) as h, g.Context(G, None, num_memory=M, device_layout=True) as d:
+        for p in range(M):
+            assert h.layout_info(p) == d.layout_info(p)
+        assert_same_layout(h, d, ARRAYS)
+        for c in (h, d):
+            c.set_algo(g.GRD_SSSP_W)
+            c.init()
+            c.run()
+        np.testing.assert_array_equal(h.read_props(), d.read_props())
+        for c in (h, d):
+            c.set_algo(g.GRD_PR_PULL, max_rounds=3)
+        assert_same_layout(h, d, IN_ARRAYS)
