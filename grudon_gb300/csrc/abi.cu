@@ -103,7 +103,6 @@ int grd_alloc_resident(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, &st.SV, S));
   TRY(dev_alloc(ctx, &st.chunk_start, E / LBS_CHUNK + 2));
   TRY(dev_alloc(ctx, &st.blk_sum, lbs_blocks(ctx)));
-  TRY(dev_alloc(ctx, &st.blk_off, lbs_blocks(ctx)));
   TRY(dev_alloc(ctx, &st.counters, NUM_COUNTERS));
   TRY(dev_alloc(ctx, &st.FL, V));
   TRY(dev_alloc(ctx, &st.DL, S));
@@ -338,20 +337,22 @@ int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
   if (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)
     return 1 + (ctx->pull.num_in_meds ? 1 : 0) + (ctx->pull.num_in_hubs ? 1 : 0);
-  return 4 + (ctx->g.num_hubs ? 1 : 0) + (mode == RM_PUSH_BITVEC ? 1 : 0);  // push, NO_OFFLOAD too
+  return 3 + (ctx->g.num_hubs ? 1 : 0) + (mode == RM_PUSH_BITVEC ? 1 : 0);  // push, NO_OFFLOAD too
 }
 
 // Kernels of a whole round in each mode (edge-map + syncs + update).
 uint32_t grd_round_launches(const grd_ctx* ctx, int mode) {
   if (mode == RM_PUSH_TINY || mode == RM_NOOFF_TINY) return 1;
-  if (mode == RM_NO_OFFLOAD) return 3 /*fwd list, retire, update list*/ + grd_edge_map_launches(ctx, mode);
+  if (mode == RM_NO_OFFLOAD)  // fwd list fused with the first degree pass, retire, update list
+    return 2 + grd_edge_map_launches(ctx, mode);
   const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
   const uint32_t groups = ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1;
   // bitvector: fwd bits + compaction; the backward tile counts (pull only:
   // the push map's dirty diff writes them) + one compaction per group; update
   const uint32_t bwd = (mode == RM_PULL_BITVEC ? 1u : 0u) + groups;
   const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (2 + bwd + 1);
-  return sync + grd_edge_map_launches(ctx, mode);
+  // push + list: the forward list sync and the first degree pass are one kernel
+  return sync + grd_edge_map_launches(ctx, mode) - (mode == RM_PUSH_LIST ? 1u : 0u);
 }
 
 // Stage API edge-map (bitvector sync around it): push with dense dirty
@@ -370,7 +371,7 @@ int grd_enqueue_edge_map(grd_ctx* ctx) {
   return GRD_OK;
 }
 
-int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
+int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, bool degrees_reduced) {
   ctx->tile_counts_ready = mode == RM_PUSH_BITVEC;  // k_diff_dirty writes them
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
@@ -399,8 +400,7 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode) {
       return GRD_OK;
     }
     const uint32_t B = lbs_blocks(ctx);
-    k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-    k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(ctx->st, B);
+    if (!degrees_reduced) k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
     grd_prof_mark(ctx, 5);
@@ -482,6 +482,13 @@ int grd_enqueue_fwd_list(grd_ctx* ctx) {
   return GRD_OK;
 }
 
+// Push rounds in list form: forward list sync + first degree pass.
+static int enqueue_fwd_list_deg(grd_ctx* ctx) {
+  k_fwd_list_deg<<<lbs_blocks(ctx), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+  CK_LAUNCH();
+  return GRD_OK;
+}
+
 int grd_enqueue_bwd_update_list(grd_ctx* ctx) {
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
@@ -529,9 +536,9 @@ int grd_enqueue_round(grd_ctx* ctx, int mode) {
   }
   if (mode == RM_NO_OFFLOAD) {
     const uint64_t launches = ctx->stats.kernel_launches;
-    TRY(grd_enqueue_fwd_list(ctx));
+    TRY(enqueue_fwd_list_deg(ctx));
     grd_prof_mark(ctx, 1);
-    TRY(grd_enqueue_edge_map_mode(ctx, mode));
+    TRY(grd_enqueue_edge_map_mode(ctx, mode, true));
     grd_prof_mark(ctx, 2);
     TRY(enqueue_retire_update_list(ctx));
     ctx->stats.kernel_launches = launches + grd_round_launches(ctx, mode);
@@ -539,13 +546,16 @@ int grd_enqueue_round(grd_ctx* ctx, int mode) {
   }
   const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
   const uint64_t launches = ctx->stats.kernel_launches;
-  if (list) {
+  const bool push_list = mode == RM_PUSH_LIST;
+  if (push_list) {
+    TRY(enqueue_fwd_list_deg(ctx));  // timed as the forward sync
+  } else if (list) {
     TRY(grd_enqueue_fwd_list(ctx));
   } else {
     TRY(grd_enqueue_fwd(ctx, true));
   }
   grd_prof_mark(ctx, 1);
-  TRY(grd_enqueue_edge_map_mode(ctx, mode));
+  TRY(grd_enqueue_edge_map_mode(ctx, mode, push_list));
   grd_prof_mark(ctx, 2);
   if (list) {
     TRY(grd_enqueue_bwd_update_list(ctx));

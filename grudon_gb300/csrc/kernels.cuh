@@ -102,7 +102,6 @@ struct DevState {
   uint32_t* SV;           // [S] property of each active (active-list order)
   uint32_t* chunk_start;  // [E/256+2] first active of each 256-edge chunk
   uint32_t* blk_sum;      // [LBS blocks]
-  uint32_t* blk_off;      // [LBS blocks]
   // Sparse-list sync (list-format rounds): the frontier as a gid list, the
   // memory-side dirty slots and the compute-side updated gids as lists.
   uint32_t* FL;           // [V] frontier gids (valid after every update)
@@ -759,10 +758,10 @@ __device__ __forceinline__ void relax_compute(const DevState& st, const uint32_t
 }
 
 // ---- load-balanced push (gen_updates over the compacted active list) ------
-// The edge-map runs in three steps so that every warp gets the same number of
+// The edge-map runs in two steps so that every warp gets the same number of
 // edges whatever the degree skew: (1) per-block sums of the (hub-capped)
-// degrees of the active list, (2) one block scans those sums, (3) each block
-// writes the exclusive degree prefix DP[i] of its actives and, for every
+// degrees of the active list, (2) each block adds up the sums before its own
+// and writes the exclusive degree prefix DP[i] of its actives and, for every
 // 256-edge chunk boundary that falls inside a row, the chunk's first active
 // (chunk_start).  k_push_lbs then hands one 256-edge chunk to a warp.
 // Rows longer than K_HUB_DEGREE count as 0 here and run in k_hub_push.
@@ -791,46 +790,51 @@ static __global__ void __launch_bounds__(256) k_deg_reduce(DevGraph g, DevState 
   if (threadIdx.x == 0) st.blk_sum[blockIdx.x] = sum;
 }
 
-// One block: exclusive scan of the nb block sums; DP[K] = total edges m.
-static __global__ void __launch_bounds__(1024) k_scan_blocks(DevState st, uint32_t nb) {
-  __shared__ uint32_t s_w[32];
-  __shared__ uint32_t s_carry;
-  const uint32_t tid = threadIdx.x, lane = lane_id(), w = tid >> 5;
-  if (tid == 0) s_carry = 0;
-  __syncthreads();
-  for (uint32_t c0 = 0; c0 < nb; c0 += blockDim.x) {
-    const uint32_t i = c0 + tid;
-    const uint32_t v = i < nb ? st.blk_sum[i] : 0;
-    uint32_t incl = warp_incl_scan(v);
-    if (lane == 31) s_w[w] = incl;
-    __syncthreads();
-    if (w == 0) {
-      const uint32_t x = s_w[lane];
-      s_w[lane] = warp_incl_scan(x) - x;
-    }
-    __syncthreads();
-    incl += s_w[w];
-    const uint32_t carry = s_carry;
-    if (i < nb) st.blk_off[i] = carry + incl - v;
-    __syncthreads();
-    if (tid == blockDim.x - 1) s_carry = carry + incl;
-    __syncthreads();
+// Push rounds in list form: the forward sync from the frontier list
+// (k_fwd_list) and the first degree pass (k_deg_reduce) in one kernel over
+// the same segments of the list (its length is known from the last update).
+static __global__ void __launch_bounds__(256) k_fwd_list_deg(DevGraph g, DevState st) {
+  const uint32_t K = __ldcg(&st.lc[L_FL]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st.counters[C_ACTIVE] = K;
+    st.counters[C_BYTES] += g.bv_bytes + 4ull * K;
+    st.counters[C_REFBYTES] += g.bv_refbytes + 4ull * K;
+    reset_round_counters(st);
+    st.lc[L_DL] = 0;
   }
-  if (tid == 0) {
-    const uint64_t K = __ldcg(&st.counters[C_ACTIVE]);
-    st.DP[K] = s_carry;
-    st.counters[C_MEDGES] = s_carry;
-    st.counters[C_EDGES] += s_carry;
+  uint32_t b0, b1;
+  lbs_segment(K, b0, b1);
+  uint32_t sum = 0;
+  for (uint32_t j = b0 + threadIdx.x; j < b1; j += blockDim.x) {
+    const uint32_t gid = st.FL[j];
+    const uint32_t s = st.own_slot[gid];
+    st.AL[j] = s;
+    st.mprop[s] = st.prop[gid];
+    atomicOr(&st.FB[s >> 5], 1u << (s & 31));
+    sum += capped_degree(g, s);
   }
+  sum = block_sum(sum);
+  if (threadIdx.x == 0) st.blk_sum[blockIdx.x] = sum;
 }
 
+// Each block first sums the degree totals of the blocks before it (a few
+// hundred L2 reads: no separate scan launch); the last block records the
+// round's edge total m (C_MEDGES, and DP[K]).
 static __global__ void __launch_bounds__(256) k_deg_down(DevGraph g, DevState st) {
   __shared__ uint32_t s_w[8];
   const uint64_t K = __ldcg(&st.counters[C_ACTIVE]);
   uint32_t b0, b1;
   lbs_segment(K, b0, b1);
   const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
-  uint32_t run = st.blk_off[blockIdx.x];
+  uint32_t run = 0;
+  for (uint32_t i = threadIdx.x; i < blockIdx.x; i += blockDim.x) run += __ldcg(&st.blk_sum[i]);
+  run = block_sum(run);
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    const uint32_t m = run + __ldcg(&st.blk_sum[blockIdx.x]);
+    st.DP[K] = m;
+    st.counters[C_MEDGES] = m;
+    st.counters[C_EDGES] += m;
+  }
   for (uint32_t base = b0; base < b1; base += blockDim.x) {
     const uint32_t i = base + threadIdx.x;
     uint32_t d = 0;
