@@ -1717,25 +1717,32 @@ __global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevSt
 // Block-uniform loop.
 template <int A>
 __global__ void __launch_bounds__(256) k_update(DevGraph g, DevState st, double tol, double damping) {
+  constexpr int U = 4;  // vertices per thread per step; one list append per block and step
   uint32_t fcount = 0, fedges = 0, fmax = 0, visited = 0;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < g.V; base += gridDim.x * blockDim.x) {
-    const uint32_t v = base + threadIdx.x;
-    bool nf = false;
-    if (v < g.V) {
-      nf = update_one<A>(g, st, v, tol, damping, visited);
-      if (nf) {
-        const uint32_t d = g.outdeg[v];
-        ++fcount;
-        fedges += d;
-        fmax = max(fmax, d);
+  for (uint32_t base = blockIdx.x * blockDim.x * U; base < g.V; base += gridDim.x * blockDim.x * U) {
+    bool nf[U];
+    uint32_t vs[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t v = base + u * blockDim.x + threadIdx.x;  // a warp takes 32 consecutive vertices
+      vs[u] = v;
+      nf[u] = false;
+      if (v < g.V) {
+        nf[u] = update_one<A>(g, st, v, tol, damping, visited);
+        if (nf[u]) {
+          const uint32_t d = g.outdeg[v];
+          ++fcount;
+          fedges += d;
+          fmax = max(fmax, d);
+        }
+      }
+      const uint32_t m = __ballot_sync(FULL, nf[u]);
+      if (lane_id() == 0 && v < g.V) {  // v is the first gid of this word
+        st.F[v >> 5] = m;
+        st.UD[v >> 5] = 0;
       }
     }
-    const uint32_t m = __ballot_sync(FULL, nf);
-    if (lane_id() == 0 && v < g.V) {  // v is the first gid of this word
-      st.F[v >> 5] = m;
-      st.UD[v >> 5] = 0;
-    }
-    block_append(st.FL, st.lc + L_FL, nf, v);
+    block_append_n<U>(st.FL, st.lc + L_FL, nf, vs);
   }
   flush_frontier_shape(st, fcount, fedges, fmax, visited);
 }
