@@ -520,12 +520,20 @@ int grd_enqueue_round(grd_ctx* ctx, int mode) {
     grd_prof_mark(ctx, 1);
     TRY(dispatch(ctx->algo, [&](auto a) -> int {
       constexpr int A = decltype(a)::value;
-      if (mode == RM_NOOFF_TINY)
-        k_round_tiny<A, true><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
-                                                                     ctx->params.damping);
-      else
-        k_round_tiny<A><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
-                                                               ctx->params.damping);
+      const double tol = ctx->params.tolerance, d = ctx->params.damping;
+      if (ctx->capturing_loop) {  // the device-driven loop: small rounds continue in the kernel
+        const PolicyArgs pa = grd_policy_args(ctx);
+        const grd_policy_model* m = grd_policy_model_dev(ctx);
+        const uint32_t cap = ctx->params.max_rounds;
+        if (mode == RM_NOOFF_TINY)
+          k_round_tiny_loop<A, true><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, tol, d, pa, m, cap);
+        else
+          k_round_tiny_loop<A, false><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, tol, d, pa, m, cap);
+      } else if (mode == RM_NOOFF_TINY) {
+        k_round_tiny<A, true><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, tol, d);
+      } else {
+        k_round_tiny<A><<<1, K_TINY_THREADS, 0, ctx->stream>>>(ctx->g, ctx->st, tol, d);
+      }
       CK_LAUNCH();
       return GRD_OK;
     }));

@@ -65,6 +65,7 @@ struct grd_ctx {
   bool has_policy = false;
   bool device_layout = false;  // layout built on the device (no host copy of its arrays)
   bool tile_counts_ready = false;  // the last edge-map wrote the backward tile counts
+  bool capturing_loop = false;     // the device-driven loop graph's branches are being captured
   bool layout_valid = true;    // false while (or after a failed) grd_ingest rewrites the layout
   bool run_pending = false;    // a GRD_RUN_ASYNC loop launch not yet waited for
   bool strict_pending = false; // ... run with GRD_RUN_STRICT

@@ -131,7 +131,9 @@ int build(grd_ctx* ctx) {
     const bool nooff = m == RM_NO_OFFLOAD || m == RM_NOOFF_TINY;
     if (nooff ? offload == GRD_OFFLOAD_NDP : offload == GRD_OFFLOAD_NONE) continue;
     TRY(capture_into(ctx, branches[m]));
+    ctx->capturing_loop = true;
     rc = grd_enqueue_round(ctx, m);
+    ctx->capturing_loop = false;
     const int e = end_capture(ctx, branches[m]);
     if (rc != GRD_OK) return rc;
     if (e != GRD_OK) return e;

@@ -1548,8 +1548,10 @@ constexpr uint32_t K_TINY_ACTIVE = 2048;
 constexpr uint32_t K_TINY_EDGES = 16384;
 constexpr int K_TINY_THREADS = 1024;
 
-template <int A, bool kCompute = false>
-__global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevState st, double tol, double damping) {
+// One whole round by one CTA of K_TINY_THREADS (k_round_tiny, and the
+// in-kernel round loop of the device-driven loop).
+template <int A, bool kCompute>
+__device__ __forceinline__ void tiny_round(const DevGraph& g, const DevState& st, double tol, double damping) {
   __shared__ uint32_t s_dp[K_TINY_ACTIVE + 1];
   __shared__ uint32_t s_rb[K_TINY_ACTIVE];
   __shared__ uint32_t s_sv[K_TINY_ACTIVE];
@@ -1705,6 +1707,11 @@ __global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevSt
   flush_frontier_shape(st, fcount, fedges, fmax, visited);
   __syncthreads();
   if (tid == 0) st.lc[L_UL] = 0;
+}
+
+template <int A, bool kCompute = false>
+__global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny(DevGraph g, DevState st, double tol, double damping) {
+  tiny_round<A, kCompute>(g, st, tol, damping);
 }
 
 // Update of a bitvector round: rebuilds the frontier bitmap

@@ -203,6 +203,54 @@ __device__ __forceinline__ int policy_choose(const DevGraph& g, const DevState& 
   return s_out[best] + P_MARGIN < s_out[fm] ? best : fm;
 }
 
+// In the device-driven loop, a one-CTA round is followed in the same kernel
+// by the next one while the policy would choose one again: after each round
+// thread 0 decides as k_policy would (offload rule, then the fixed rule or
+// the tiny guard that precedes the model's inference, then the branch) and,
+// to go on, records the device-loop statistics of the finished round and of
+// the next one as k_round_end and k_policy would.  A high-diameter graph's
+// long tail of small rounds then costs one launch instead of three per round.
+template <bool kCompute>
+__device__ __forceinline__ bool tiny_continue(const DevGraph& g, const DevState& st, const PolicyArgs& a,
+                                              const grd_policy_model* model, uint32_t max_rounds) {
+  if (st.counters[C_ERR]) return false;
+  const unsigned long long f = st.counters[C_FRONTIER], fe = st.counters[C_FEDGES];
+  const unsigned long long r = st.counters[C_ROUNDS] + 1;  // rounds finished, this one included
+  if (f == 0 || r >= max_rounds) return false;
+  int mode;
+  if (policy_no_offload(a.offload, f, g.V))
+    mode = GRD_ROUND_NO_OFFLOAD;
+  else if (model == nullptr)
+    mode = policy_fixed(g, a, f, fe);
+  else if (policy_tiny(f, fe, policy_allowed(a.direction, a.format, a.has_in != 0)))
+    mode = GRD_ROUND_PUSH_LIST;
+  else
+    return false;  // the model's inference decides: back to the loop graph
+  if (policy_branch(mode, f, fe) != (kCompute ? P_BRANCH_NOOFF_TINY : P_BRANCH_TINY)) return false;
+  st.counters[C_ROUNDS] = r;  // k_round_end of the finished round
+  st.counters[C_ACTIVE_TOTAL] += st.counters[C_ACTIVE];
+  st.counters[C_PUSH_ACTIVES] += st.counters[C_ACTIVE];
+  st.counters[C_PUSH_ROUNDS] += 1;  // k_policy of the next (no launch)
+  if (kCompute) st.counters[C_NOOFF_ROUNDS] += 1;
+  st.counters[C_MODE] = (unsigned long long)mode;
+  return true;
+}
+
+template <int A, bool kCompute>
+__global__ void __launch_bounds__(K_TINY_THREADS) k_round_tiny_loop(DevGraph g, DevState st, double tol,
+                                                                    double damping, PolicyArgs a,
+                                                                    const grd_policy_model* model,
+                                                                    uint32_t max_rounds) {
+  __shared__ int s_go;
+  for (;;) {
+    tiny_round<A, kCompute>(g, st, tol, damping);
+    __syncthreads();
+    if (threadIdx.x == 0) s_go = tiny_continue<kCompute>(g, st, a, model, max_rounds) ? 1 : 0;
+    __syncthreads();
+    if (!s_go) break;
+  }
+}
+
 // The round's policy kernel (one block of P_HID threads).  In the device
 // loop (kGraph) it also counts the round's statistics and selects the SWITCH
 // branch; in the host loop it only leaves the mode in C_MODE.
