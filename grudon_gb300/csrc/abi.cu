@@ -586,8 +586,19 @@ int grd_read_counters(grd_ctx* ctx) {
   return grd_fold_counters(ctx);
 }
 
+// The counters copied by grd_init, once a host-side decision needs them.
+int grd_sync_init_counters(grd_ctx* ctx) {
+  if (!ctx->counters_stale) return GRD_OK;
+  CK(cudaStreamSynchronize(ctx->stream));
+  const grd_stats keep = ctx->stats;  // only the frontier shape is wanted
+  const int rc = grd_fold_counters(ctx);
+  ctx->stats = keep;
+  return rc;
+}
+
 // Folds the host copy of the counters into the stats.
 int grd_fold_counters(grd_ctx* ctx) {
+  ctx->counters_stale = false;
   ctx->stats.edges_scanned = ctx->h_counters[C_EDGES] + ctx->pull.edges;
   ctx->stats.bytes_synced = ctx->h_counters[C_BYTES];
   ctx->stats.reference_bytes_moved = ctx->h_counters[C_REFBYTES];
@@ -873,7 +884,13 @@ int grd_init(grd_ctx* ctx) {
   int rc = grd_enqueue_init(ctx, blocks);
   if (rc != GRD_OK) return rc;
   CK_LAUNCH();
-  TRY(grd_read_counters(ctx));  // initial |frontier| for the first round's mode
+  // The initial frontier shape matters only to host-side decisions (the
+  // host-driven loop, the per-stage calls): its copy is queued here and read
+  // when one of those needs it, so a device-driven run starts without a host
+  // round trip.
+  CK(cudaMemcpyAsync(ctx->h_counters, ctx->st.counters, sizeof(unsigned long long) * NUM_COUNTERS,
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  ctx->counters_stale = true;
   ctx->stats = grd_stats{};
   ctx->stats.kernel_launches = 1;
   ctx->pull.edges = 0;
@@ -930,6 +947,7 @@ int grd_init_sources(grd_ctx* ctx, const uint32_t* sources, size_t n) {
   CK(cudaMemcpyAsync(ctx->st.counters + C_FRONTIER, ctx->h_seed, sizeof(unsigned long long), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->counters_stale = false;
   ctx->last_frontier = m;
   CK(cudaMemcpyAsync(ctx->h_counters, ctx->st.counters, sizeof(unsigned long long) * NUM_COUNTERS,
                      cudaMemcpyDeviceToHost, ctx->stream));
@@ -941,30 +959,35 @@ int grd_init_sources(grd_ctx* ctx, const uint32_t* sources, size_t n) {
 
 int grd_sync_fwd(grd_ctx* ctx) {
   TRY(check_ready(ctx));
+  TRY(grd_sync_init_counters(ctx));
   if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, 0);
   return grd_enqueue_fwd(ctx, false);
 }
 
 int grd_edge_map(grd_ctx* ctx) {
   TRY(check_ready(ctx));
+  TRY(grd_sync_init_counters(ctx));
   if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, 1);
   return grd_enqueue_edge_map(ctx);
 }
 
 int grd_sync_bwd(grd_ctx* ctx) {
   TRY(check_ready(ctx));
+  TRY(grd_sync_init_counters(ctx));
   if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, 2);
   return grd_enqueue_bwd(ctx, false, true, false);
 }
 
 int grd_aggregate(grd_ctx* ctx) {
   TRY(check_ready(ctx));
+  TRY(grd_sync_init_counters(ctx));
   if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, 3);
   return grd_enqueue_bwd(ctx, false, false, true);
 }
 
 int grd_update(grd_ctx* ctx, uint64_t* frontier_size) {
   TRY(check_ready(ctx));
+  TRY(grd_sync_init_counters(ctx));
   uint64_t f;
   ctx->stats.rounds++;
   if (ctx->algo == GRD_PR_PULL) {
@@ -993,6 +1016,7 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
       ctx->stats.rounds < ctx->params.max_rounds)
     TRY(grd_graph_run(ctx, &device_loop, async));
   ctx->stats.device_loop = device_loop ? 1 : 0;
+  if (!device_loop) TRY(grd_sync_init_counters(ctx));  // host-side decisions need the frontier shape
   if (device_loop) {
     // the whole loop ran (or, async, is queued) as one graph launch
     if (ctx->run_pending) {

@@ -66,6 +66,7 @@ struct grd_ctx {
   bool device_layout = false;  // layout built on the device (no host copy of its arrays)
   bool tile_counts_ready = false;  // the last edge-map wrote the backward tile counts
   bool capturing_loop = false;     // the device-driven loop graph's branches are being captured
+  bool counters_stale = false;     // h_counters holds grd_init's queued copy, not yet read
   bool layout_valid = true;    // false while (or after a failed) grd_ingest rewrites the layout
   bool run_pending = false;    // a GRD_RUN_ASYNC loop launch not yet waited for
   bool strict_pending = false; // ... run with GRD_RUN_STRICT
@@ -114,6 +115,7 @@ int grd_upload_layout(grd_ctx* ctx);
 int grd_ensure_in_edges(grd_ctx* ctx);
 int grd_read_counters(grd_ctx* ctx);
 int grd_fold_counters(grd_ctx* ctx);
+int grd_sync_init_counters(grd_ctx* ctx);
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused);
 int grd_enqueue_edge_map(grd_ctx* ctx);
 // Round modes: direction x sync format.  Values are the SWITCH branch indices

@@ -188,6 +188,7 @@ int grd_graph_run(grd_ctx* ctx, bool* used, bool async) {
   *used = false;
   if (ctx->graph_failed) return GRD_OK;
   if (!ctx->run_exec) {
+    CK(cudaStreamSynchronize(ctx->stream));  // capture starts on an idle stream
     const int rc = build(ctx);
     if (rc != GRD_OK) {
       ctx->graph_failed = true;
