@@ -287,57 +287,65 @@ __device__ __forceinline__ void warp_append_n(uint32_t* list, uint32_t* counter,
 // of a block runs the same iterations (block-aggregated list appends).
 template <int A>
 __global__ void __launch_bounds__(256) k_init(DevGraph g, DevState st, uint32_t source, double damping) {
+  constexpr int U = 4;  // elements per thread per step; one list append per block and step
   const uint64_t n = g.S > g.V ? g.S : g.V;
   uint32_t fcount = 0, fedges = 0, fmax = 0, unvis = 0;
-  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x; b < n; b += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t i = b + threadIdx.x;
-    uint32_t fbit = 0;
-    if (i < g.V) {
-      const uint32_t v = (uint32_t)i;
-      const uint32_t deg = g.outdeg[v];
-      if (A == A_CC) {
-        st.prop[v] = v;
-        st.upd[v] = 0xFFFFFFFFu;
-        fbit = 1;
-      } else if (A == A_SSSP_HOP || A == A_SSSP_W) {
-        const uint32_t x = (v == source) ? 0u : 0xFFFFFFFFu;
-        st.prop[v] = x;
-        st.upd[v] = x;
-        fbit = (v == source);
-        if (!fbit) unvis += deg;
-      } else {  // PageRank (delta and pull share the initial state)
-        if (deg != 0) {
-          st.prop[v] = __float_as_uint((float)(damping * (1.0 - damping) / (double)deg));
-          st.ranks[v] = (float)(1.0 - damping);
+  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x * U; b < n; b += (uint64_t)gridDim.x * blockDim.x * U) {
+    bool fb[U];
+    uint32_t ids[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t i = b + (uint64_t)u * blockDim.x + threadIdx.x;  // a warp takes 32 consecutive ids
+      ids[u] = (uint32_t)i;
+      uint32_t fbit = 0;
+      if (i < g.V) {
+        const uint32_t v = (uint32_t)i;
+        const uint32_t deg = g.outdeg[v];
+        if (A == A_CC) {
+          st.prop[v] = v;
+          st.upd[v] = 0xFFFFFFFFu;
           fbit = 1;
-        } else {
-          st.prop[v] = 0;
-          st.ranks[v] = 0.0f;
+        } else if (A == A_SSSP_HOP || A == A_SSSP_W) {
+          const uint32_t x = (v == source) ? 0u : 0xFFFFFFFFu;
+          st.prop[v] = x;
+          st.upd[v] = x;
+          fbit = (v == source);
+          if (!fbit) unvis += deg;
+        } else {  // PageRank (delta and pull share the initial state)
+          if (deg != 0) {
+            st.prop[v] = __float_as_uint((float)(damping * (1.0 - damping) / (double)deg));
+            st.ranks[v] = (float)(1.0 - damping);
+            fbit = 1;
+          } else {
+            st.prop[v] = 0;
+            st.ranks[v] = 0.0f;
+          }
+          st.upd[v] = 0;
         }
-        st.upd[v] = 0;
+        if (fbit) {
+          fedges += deg;
+          fmax = max(fmax, deg);
+        }
       }
-      if (fbit) {
-        fedges += deg;
-        fmax = max(fmax, deg);
+      fb[u] = fbit != 0;
+      const uint32_t m = __ballot_sync(FULL, fbit);
+      if (lane_id() == 0 && i < g.V) {  // i is the first gid of its word
+        st.F[i >> 5] = m;
+        st.UD[i >> 5] = 0;
+        fcount += __popc(m);
+      }
+      if (i < g.S) {
+        const uint32_t x = (A == A_PR_DELTA || A == A_PR_PULL) ? 0u : 0xFFFFFFFFu;
+        st.mprop[i] = x;
+        st.mupd[i] = x;
+        st.snap[i] = x;
+        if ((i & 31) == 0) {
+          st.FB[i >> 5] = 0;
+          st.MD[i >> 5] = 0;
+        }
       }
     }
-    const uint32_t m = __ballot_sync(FULL, fbit);
-    block_append(st.FL, st.lc + L_FL, fbit != 0, (uint32_t)i);
-    if (lane_id() == 0 && i < g.V) {  // i is the first gid of its word
-      st.F[i >> 5] = m;
-      st.UD[i >> 5] = 0;
-      fcount += __popc(m);
-    }
-    if (i < g.S) {
-      const uint32_t x = (A == A_PR_DELTA || A == A_PR_PULL) ? 0u : 0xFFFFFFFFu;
-      st.mprop[i] = x;
-      st.mupd[i] = x;
-      st.snap[i] = x;
-      if ((i & 31) == 0) {
-        st.FB[i >> 5] = 0;
-        st.MD[i >> 5] = 0;
-      }
-    }
+    block_append_n<U>(st.FL, st.lc + L_FL, fb, ids);
   }
   // one counter update per block
   fcount = block_sum(fcount);
