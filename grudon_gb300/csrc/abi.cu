@@ -1109,7 +1109,8 @@ int grd_wait(grd_ctx* ctx, grd_stats* stats) {
 int grd_set_policy(grd_ctx* ctx, const grd_policy_model* model) {
   if (!ctx) return GRD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
-  grd_graph_release(ctx);  // the loop graph holds the model pointer (or none)
+  TRY(grd_wait(ctx, nullptr));  // a queued run still uses the loop graph
+  grd_graph_release(ctx);       // the loop graph holds the model pointer (or none)
   if (!model) {
     ctx->has_policy = false;
     return GRD_OK;
