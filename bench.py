@@ -706,7 +706,7 @@ def main():
                 "alg_bytes_per_launch": prof["lbs_bytes"] / nl, "avg_launch_ms": prof["lbs_ms"] / nl,
                 "launches": prof["lbs_launches"],
                 "edge_map_stage": {"achieved": stage_ach, "frac": stage_ach / hbm_peak,
-                                   "kernels": "k_deg_*, k_push_lbs, k_hub_push, k_diff_dirty (push) or k_pull* (pull)",
+                                   "kernels": "k_deg_* (list rounds), k_push_lbs, k_hub_push, k_diff_dirty (push) or k_pull* (pull)",
                                    "share_of_rounds": prof["edge_map_ms"] / prof["rounds_ms"]
                                    if prof["rounds_ms"] else None},
                 "push_rounds_per_step": prof["push_rounds"] / args.steps,

@@ -98,6 +98,8 @@ int grd_alloc_resident(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, &st.BV, S));
   TRY(dev_alloc(ctx, &st.AL, S));
   TRY(dev_alloc(ctx, &st.tile_cnt, T));
+  TRY(dev_alloc(ctx, &st.tile_deg, T));
+  TRY(dev_alloc(ctx, &st.warp_deg, 8 * (size_t)T));
   TRY(dev_alloc(ctx, &st.DP, S + 1));
   TRY(dev_alloc(ctx, &st.RB, S));
   TRY(dev_alloc(ctx, &st.SV, S));
@@ -321,7 +323,7 @@ static int host_loop_mode(grd_ctx* ctx, int* mode) {
 
 int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
   const uint32_t T = ctx->g.num_tiles;
-  k_fwd_bits<<<T, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+  k_fwd_bits<false><<<T, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
   if (fused) {
     k_compact<<<T, 256, 0, ctx->stream>>>(ctx->st.FB, nullptr, 0u, ctx->g, ctx->st, OpFwdXfer{}, 2);
   } else {
@@ -330,6 +332,16 @@ int grd_enqueue_fwd(grd_ctx* ctx, bool fused) {
   }
   CK_LAUNCH();
   ctx->stats.kernel_launches += fused ? 2 : 3;
+  return GRD_OK;
+}
+
+// Push rounds in bitvector form: the forward sync also places the degree
+// prefix of the active list (both degree passes of the edge-map).
+static int enqueue_fwd_push(grd_ctx* ctx) {
+  const uint32_t T = ctx->g.num_tiles;
+  k_fwd_bits<true><<<T, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+  k_fwd_xfer_deg<<<T, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+  CK_LAUNCH();
   return GRD_OK;
 }
 
@@ -351,8 +363,8 @@ uint32_t grd_round_launches(const grd_ctx* ctx, int mode) {
   // the push map's dirty diff writes them) + one compaction per group; update
   const uint32_t bwd = (mode == RM_PULL_BITVEC ? 1u : 0u) + groups;
   const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (2 + bwd + 1);
-  // push + list: the forward list sync and the first degree pass are one kernel
-  return sync + grd_edge_map_launches(ctx, mode) - (mode == RM_PUSH_LIST ? 1u : 0u);
+  // push: the forward sync runs the degree passes (bitvector: both, list: the first)
+  return sync + grd_edge_map_launches(ctx, mode) - (mode == RM_PUSH_LIST ? 1u : mode == RM_PUSH_BITVEC ? 2u : 0u);
 }
 
 // Stage API edge-map (bitvector sync around it): push with dense dirty
@@ -371,7 +383,7 @@ int grd_enqueue_edge_map(grd_ctx* ctx) {
   return GRD_OK;
 }
 
-int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, bool degrees_reduced) {
+int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done) {
   ctx->tile_counts_ready = mode == RM_PUSH_BITVEC;  // k_diff_dirty writes them
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
@@ -400,8 +412,8 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, bool degrees_reduced) {
       return GRD_OK;
     }
     const uint32_t B = lbs_blocks(ctx);
-    if (!degrees_reduced) k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-    k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    if (degree_passes_done < 1) k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    if (degree_passes_done < 2) k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
     grd_prof_mark(ctx, 5);
     if (mode == RM_PUSH_BITVEC) {
@@ -546,7 +558,7 @@ int grd_enqueue_round(grd_ctx* ctx, int mode) {
     const uint64_t launches = ctx->stats.kernel_launches;
     TRY(enqueue_fwd_list_deg(ctx));
     grd_prof_mark(ctx, 1);
-    TRY(grd_enqueue_edge_map_mode(ctx, mode, true));
+    TRY(grd_enqueue_edge_map_mode(ctx, mode, 1));
     grd_prof_mark(ctx, 2);
     TRY(enqueue_retire_update_list(ctx));
     ctx->stats.kernel_launches = launches + grd_round_launches(ctx, mode);
@@ -559,11 +571,13 @@ int grd_enqueue_round(grd_ctx* ctx, int mode) {
     TRY(enqueue_fwd_list_deg(ctx));  // timed as the forward sync
   } else if (list) {
     TRY(grd_enqueue_fwd_list(ctx));
+  } else if (mode == RM_PUSH_BITVEC) {
+    TRY(enqueue_fwd_push(ctx));
   } else {
     TRY(grd_enqueue_fwd(ctx, true));
   }
   grd_prof_mark(ctx, 1);
-  TRY(grd_enqueue_edge_map_mode(ctx, mode, push_list));
+  TRY(grd_enqueue_edge_map_mode(ctx, mode, push_list ? 1 : mode == RM_PUSH_BITVEC ? 2 : 0));
   grd_prof_mark(ctx, 2);
   if (list) {
     TRY(grd_enqueue_bwd_update_list(ctx));

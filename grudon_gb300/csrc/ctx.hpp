@@ -143,8 +143,9 @@ __host__ __device__ inline int rm_branch(int mode, unsigned long long frontier, 
 }
 __host__ __device__ inline bool rm_is_pull(int m) { return m == RM_PULL_BITVEC || m == RM_PULL_LIST; }
 int grd_choose_round_mode(const grd_ctx* ctx);
-// degrees_reduced: the first degree pass already ran (k_fwd_list_deg).
-int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, bool degrees_reduced = false);
+// degree_passes_done: 1 = the first degree pass already ran (k_fwd_list_deg),
+// 2 = both (k_fwd_xfer_deg).
+int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done = 0);
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode);
 uint32_t grd_round_launches(const grd_ctx* ctx, int mode);
 int grd_enqueue_fwd_list(grd_ctx* ctx);

@@ -97,6 +97,8 @@ struct DevState {
   uint32_t* BV;
   uint32_t* AL;
   uint32_t* tile_cnt;     // set bits per compaction tile of the bitvector being compacted
+  uint32_t* tile_deg;     // [T] capped out-degrees of each tile's actives (push, bitvector form)
+  uint32_t* warp_deg;     // [8T] the same per 1024-slot warp range
   uint32_t* DP;           // [S+1] exclusive degree prefix over the active list
   uint32_t* RB;           // [S] row start of each active (active-list order)
   uint32_t* SV;           // [S] property of each active (active-list order)
@@ -373,7 +375,23 @@ __device__ __forceinline__ void reset_round_counters(const DevState& st) {
   st.counters[C_FMAXDEG] = 0;
 }
 
-static __global__ void __launch_bounds__(256) k_fwd_bits(DevGraph g, DevState st) {
+//
+// Warp w of the block builds the words of slots [w*1024, w*1024+1024) of its
+// tile, the same split as the compaction's warps.  kDeg (push rounds in
+// bitvector form): each warp also sums the hub-capped out-degrees of its
+// actives (warp_deg) and the block those of the tile (tile_deg), so that the
+// compaction can place every active's degree prefix directly.
+constexpr uint32_t K_WARP_SLOTS = K_TILE_SLOTS / 8;  // slots per warp of a 256-thread tile block
+
+// Out-degree of an owned slot as the load-balanced push counts it: rows longer
+// than K_HUB_DEGREE count as 0 (they run in k_hub_push).
+__device__ __forceinline__ uint32_t capped_degree(const DevGraph& g, uint32_t s) {
+  const uint32_t d = __ldg(&g.row_off[s + 1]) - __ldg(&g.row_off[s]);
+  return d > K_HUB_DEGREE ? 0u : d;
+}
+
+template <bool kDeg>
+__global__ void __launch_bounds__(256) k_fwd_bits(DevGraph g, DevState st) {
   const uint32_t t = blockIdx.x;
   if (t == 0 && threadIdx.x == 0) {
     reset_round_counters(st);
@@ -383,31 +401,43 @@ static __global__ void __launch_bounds__(256) k_fwd_bits(DevGraph g, DevState st
   }
   const uint32_t p = g.tile_part[t];
   const uint32_t base = g.part_base[p], nown = g.part_owned[p];
-  const uint32_t t0 = t * K_TILE_SLOTS;
+  const uint32_t w = threadIdx.x >> 5, lane = lane_id();
+  const uint32_t w0 = t * K_TILE_SLOTS + w * K_WARP_SLOTS;
   constexpr int U = 4;  // independent gathers in flight per thread
-  uint32_t cnt = 0;
-  for (uint32_t i = threadIdx.x; i < K_TILE_SLOTS; i += blockDim.x * U) {
-    uint32_t gid[U], fw[U];
+  uint32_t cnt = 0, deg = 0;
+  for (uint32_t i = lane; i < K_WARP_SLOTS; i += 32 * U) {
+    uint32_t gid[U], fw[U], bit[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const uint32_t s = t0 + i + u * blockDim.x;
+      const uint32_t s = w0 + i + u * 32;
       gid[u] = (s - base < nown) ? __ldg(&g.slot_gid[s]) : 0xFFFFFFFFu;
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) fw[u] = gid[u] != 0xFFFFFFFFu ? st.F[gid[u] >> 5] : 0u;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const uint32_t s = t0 + i + u * blockDim.x;
-      const uint32_t bit = gid[u] != 0xFFFFFFFFu ? (fw[u] >> (gid[u] & 31)) & 1u : 0u;
-      const uint32_t m = __ballot_sync(FULL, bit);
-      if (lane_id() == 0) {
+      const uint32_t s = w0 + i + u * 32;
+      bit[u] = gid[u] != 0xFFFFFFFFu ? (fw[u] >> (gid[u] & 31)) & 1u : 0u;
+      const uint32_t m = __ballot_sync(FULL, bit[u]);
+      if (lane == 0) {
         st.FB[s >> 5] = m;
         cnt += __popc(m);
       }
     }
+    if (kDeg) {
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (bit[u]) deg += capped_degree(g, w0 + i + u * 32);
+    }
   }
   cnt = block_sum(cnt);
   if (threadIdx.x == 0) st.tile_cnt[t] = cnt;
+  if (kDeg) {  // deg is still this lane's own sum: block_sum adds over all lanes
+    const uint32_t wdeg = warp_sum(deg);
+    if (lane == 0) st.warp_deg[t * 8 + w] = wdeg;
+    deg = block_sum(deg);
+    if (threadIdx.x == 0) st.tile_deg[t] = deg;
+  }
 }
 
 // Per-tile set-bit count of a bitvector (backward sync).  `zero`, when
@@ -457,6 +487,33 @@ struct Payload {
   uint32_t v, gid, cur, cmp;
 };
 
+// Phase A's second half: the warp's words x[k] (word index wbase + 32k +
+// lane) become the slots of their set bits in `buf`, in ascending order;
+// returns how many.
+template <int KW>
+__device__ __forceinline__ uint32_t collect_set_bits(const uint32_t (&x)[KW], size_t wbase, uint32_t* buf) {
+  const uint32_t lane = lane_id(), lt = (1u << lane) - 1u;
+  uint32_t n = 0;
+#pragma unroll
+  for (int k = 0; k < KW; ++k) {
+    const uint32_t xc = __popc(x[k]);
+    const uint32_t incl = warp_incl_scan(xc);
+    const uint32_t excl = incl - xc;
+    const uint32_t ctot = __shfl_sync(FULL, incl, 31);
+    if (ctot) {
+      for (int j = 0; j < 32; ++j) {
+        const uint32_t wj = __shfl_sync(FULL, x[k], j);
+        if (wj == 0) continue;
+        const uint32_t ej = __shfl_sync(FULL, excl, j);
+        if ((wj >> lane) & 1u) buf[n + ej + __popc(wj & lt)] = (uint32_t)(wbase + k * 32 + j) * 32 + lane;
+      }
+    }
+    n += ctot;
+  }
+  __syncwarp();
+  return n;
+}
+
 template <class Op>
 __global__ void __launch_bounds__(256)
     k_compact(const uint32_t* __restrict__ bits, uint32_t* clear_bits, uint32_t tile_begin, DevGraph g,
@@ -505,26 +562,8 @@ __global__ void __launch_bounds__(256)
     if (rb) atomicAdd(&st.counters[C_REFBYTES], rb);
     if (count == 2 && ct) atomicAdd(&st.counters[C_ACTIVE], (unsigned long long)ct);
   }
-  const uint32_t lt = (1u << lane) - 1u;
   uint32_t* buf = s_slot[warp];
-  uint32_t n = 0;
-#pragma unroll
-  for (int k = 0; k < KW; ++k) {
-    const uint32_t xc = __popc(x[k]);
-    const uint32_t incl = warp_incl_scan(xc);
-    const uint32_t excl = incl - xc;
-    const uint32_t ctot = __shfl_sync(FULL, incl, 31);
-    if (ctot) {
-      for (int j = 0; j < 32; ++j) {
-        const uint32_t wj = __shfl_sync(FULL, x[k], j);
-        if (wj == 0) continue;
-        const uint32_t ej = __shfl_sync(FULL, excl, j);
-        if ((wj >> lane) & 1u) buf[n + ej + __popc(wj & lt)] = (uint32_t)(wbase + k * 32 + j) * 32 + lane;
-      }
-    }
-    n += ctot;
-  }
-  __syncwarp();
+  const uint32_t n = collect_set_bits(x, wbase, buf);
   for (uint32_t q0 = 0; q0 < n; q0 += 32 * U) {
     uint32_t sl[U];
     Payload pv[U];
@@ -775,11 +814,6 @@ __device__ __forceinline__ void relax_compute(const DevState& st, const uint32_t
 // Rows longer than K_HUB_DEGREE count as 0 here and run in k_hub_push.
 constexpr uint32_t LBS_CHUNK = 256;
 
-__device__ __forceinline__ uint32_t capped_degree(const DevGraph& g, uint32_t s) {
-  const uint32_t d = __ldg(&g.row_off[s + 1]) - __ldg(&g.row_off[s]);
-  return d > K_HUB_DEGREE ? 0u : d;
-}
-
 // Fixed grid: block b owns actives [b*seg, min(K,(b+1)*seg)), seg = ceil(K/B).
 __device__ __forceinline__ void lbs_segment(uint64_t K, uint32_t& b0, uint32_t& b1) {
   const uint64_t seg = (K + gridDim.x - 1) / gridDim.x;
@@ -873,6 +907,103 @@ static __global__ void __launch_bounds__(256) k_deg_down(DevGraph g, DevState st
     }
     run += tot;
     __syncthreads();
+  }
+}
+
+// Forward transfer of a push round in bitvector form fused with both degree
+// passes (k_deg_reduce, k_deg_down).  The active list is the compaction
+// order, so the block of tile t knows where its actives start (tile_cnt of
+// the tiles before it) and where their edges start (tile_deg), and warp w
+// adds the warp_deg of the warps before it: every active's exclusive degree
+// prefix DP, row start RB, source value SV and the chunks that start in its
+// row are written here, with no scan launch and no second read of the list.
+// The last tile's block records the round's edge total (DP[K], C_MEDGES).
+static __global__ void __launch_bounds__(256) k_fwd_xfer_deg(DevGraph g, DevState st) {
+  constexpr int KW = K_TILE_WORDS / 256;
+  constexpr int CAP = 32 * 32 * KW;
+  constexpr int U = 4;
+  static_assert(CAP == K_WARP_SLOTS, "the compaction's warps own k_fwd_bits's warp ranges");
+  __shared__ uint32_t s_wsum[8], s_wdeg[8];
+  __shared__ uint32_t s_slot[8][CAP];
+  const uint32_t t = blockIdx.x;
+  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+  uint32_t pre_g = 0, pre_d = 0;  // actives and their capped edges before this tile
+  for (uint32_t i = threadIdx.x; i < t; i += blockDim.x) {
+    pre_g += __ldcg(&st.tile_cnt[i]);
+    pre_d += __ldcg(&st.tile_deg[i]);
+  }
+  pre_g = block_sum(pre_g);
+  pre_d = block_sum(pre_d);
+  const size_t wbase = (size_t)t * K_TILE_WORDS + warp * (32 * KW);
+  uint32_t x[KW];
+  uint32_t c = 0;
+#pragma unroll
+  for (int k = 0; k < KW; ++k) {
+    x[k] = __ldcg(&st.FB[wbase + k * 32 + lane]);
+    c += __popc(x[k]);
+  }
+  c = warp_sum(c);
+  if (lane == 0) {
+    s_wsum[warp] = c;
+    s_wdeg[warp] = __ldcg(&st.warp_deg[t * 8 + warp]);
+  }
+  __syncthreads();
+  uint32_t wb = 0, wd = 0, ct = 0, dt = 0;
+  for (uint32_t i = 0; i < 8; ++i) {
+    const uint32_t a = s_wsum[i], d = s_wdeg[i];
+    if (i < warp) wb += a, wd += d;
+    ct += a;
+    dt += d;
+  }
+  if (threadIdx.x == 0) {
+    // bitvectors once per pass, plus 4 B per packed value (k_compact's count 2)
+    unsigned long long b = 4ull * ct, rb = 4ull * ct;
+    if (t == 0) b += g.bv_bytes, rb += g.bv_refbytes;
+    if (b) atomicAdd(&st.counters[C_BYTES], b);
+    if (rb) atomicAdd(&st.counters[C_REFBYTES], rb);
+    if (ct) atomicAdd(&st.counters[C_ACTIVE], (unsigned long long)ct);
+    if (t == gridDim.x - 1) {
+      const uint32_t m = pre_d + dt;
+      st.DP[pre_g + ct] = m;
+      st.counters[C_MEDGES] = m;
+      st.counters[C_EDGES] += m;
+    }
+  }
+  uint32_t* buf = s_slot[warp];
+  const uint32_t n = collect_set_bits(x, wbase, buf);
+  const uint32_t grun = pre_g + wb;
+  uint32_t drun = pre_d + wd;  // capped edges of this warp's actives before the group
+  for (uint32_t q0 = 0; q0 < n; q0 += 32 * U) {
+    uint32_t sl[U], gid[U], r0[U], d[U], v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t q = q0 + u * 32 + lane;
+      sl[u] = q < n ? buf[q] : 0u;
+      gid[u] = q < n ? __ldg(&g.slot_gid[sl[u]]) : 0u;
+      r0[u] = q < n ? __ldg(&g.row_off[sl[u]]) : 0u;
+      d[u] = q < n ? __ldg(&g.row_off[sl[u] + 1]) - r0[u] : 0u;
+      if (d[u] > K_HUB_DEGREE) d[u] = 0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) v[u] = (q0 + u * 32 + lane) < n ? st.prop[gid[u]] : 0u;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t q = q0 + u * 32 + lane;
+      const uint32_t incl = warp_incl_scan(d[u]);
+      const uint32_t ex = drun + incl - d[u];
+      drun += __shfl_sync(FULL, incl, 31);
+      if (q < n) {
+        const uint32_t i = grun + q;
+        st.mprop[sl[u]] = v[u];
+        st.DP[i] = ex;
+        st.RB[i] = r0[u];
+        st.SV[i] = v[u];
+        if (d[u]) {
+          const uint32_t c0 = (ex + LBS_CHUNK - 1) / LBS_CHUNK, c1 = (ex + d[u] + LBS_CHUNK - 1) / LBS_CHUNK;
+          for (uint32_t cc = c0; cc < c1; ++cc) st.chunk_start[cc] = i;
+        }
+      }
+    }
   }
 }
 
