@@ -345,6 +345,12 @@ static int enqueue_fwd_push(grd_ctx* ctx) {
   return GRD_OK;
 }
 
+// Push + bitvector rounds of the min algorithms aggregate in the dirty diff
+// (k_diff_aggregate); PageRank keeps its ordered per-partition aggregate.
+static bool diff_aggregates(const grd_ctx* ctx) {
+  return ctx->algo == GRD_CC || ctx->algo == GRD_SSSP_HOP || ctx->algo == GRD_SSSP_W;
+}
+
 // Kernels of the edge-map of one round in each mode.
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
   if (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)
@@ -360,8 +366,10 @@ uint32_t grd_round_launches(const grd_ctx* ctx, int mode) {
   const bool list = mode == RM_PUSH_LIST || mode == RM_PULL_LIST;
   const uint32_t groups = ctx->algo == GRD_PR_DELTA ? ctx->L.M : 1;
   // bitvector: fwd bits + compaction; the backward tile counts (pull only:
-  // the push map's dirty diff writes them) + one compaction per group; update
-  const uint32_t bwd = (mode == RM_PULL_BITVEC ? 1u : 0u) + groups;
+  // the push map's dirty diff writes them) + one compaction per group (none
+  // when the dirty diff aggregates); update
+  const uint32_t bwd = mode == RM_PUSH_BITVEC && diff_aggregates(ctx) ? 0u
+                                                                      : (mode == RM_PULL_BITVEC ? 1u : 0u) + groups;
   const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (2 + bwd + 1);
   // push: the forward sync runs the degree passes (bitvector: both, list: the first)
   return sync + grd_edge_map_launches(ctx, mode) - (mode == RM_PUSH_LIST ? 1u : mode == RM_PUSH_BITVEC ? 2u : 0u);
@@ -383,8 +391,8 @@ int grd_enqueue_edge_map(grd_ctx* ctx) {
   return GRD_OK;
 }
 
-int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done) {
-  ctx->tile_counts_ready = mode == RM_PUSH_BITVEC;  // k_diff_dirty writes them
+int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bool aggregate) {
+  ctx->tile_counts_ready = mode == RM_PUSH_BITVEC && !aggregate;  // k_diff_dirty writes them
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
     const uint32_t pull_hub_grid = std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8));
@@ -420,6 +428,13 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done) {
       k_push_lbs<A, true><<<resident_grid(ctx, k_push_lbs<A, true>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       grd_prof_mark(ctx, 6);
       if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if constexpr (A != A_PR_DELTA && A != A_PR_PULL) {
+        if (aggregate) {
+          k_diff_aggregate<A><<<ctx->g.num_tiles, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+          CK_LAUNCH();
+          return GRD_OK;
+        }
+      }
       k_diff_dirty<A><<<ctx->g.num_tiles, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     } else if (mode == RM_NO_OFFLOAD) {  // compute-side push into vertex_updates
       k_push_lbs<A, false, true><<<resident_grid(ctx, k_push_lbs<A, false, true>), 256, 0, ctx->stream>>>(ctx->g,
@@ -577,13 +592,14 @@ int grd_enqueue_round(grd_ctx* ctx, int mode) {
     TRY(grd_enqueue_fwd(ctx, true));
   }
   grd_prof_mark(ctx, 1);
-  TRY(grd_enqueue_edge_map_mode(ctx, mode, push_list ? 1 : mode == RM_PUSH_BITVEC ? 2 : 0));
+  const bool aggregate = mode == RM_PUSH_BITVEC && diff_aggregates(ctx);
+  TRY(grd_enqueue_edge_map_mode(ctx, mode, push_list ? 1 : mode == RM_PUSH_BITVEC ? 2 : 0, aggregate));
   grd_prof_mark(ctx, 2);
   if (list) {
     TRY(grd_enqueue_bwd_update_list(ctx));
     grd_prof_mark(ctx, 3);
   } else {
-    TRY(grd_enqueue_bwd(ctx, true, true, true));
+    if (!aggregate) TRY(grd_enqueue_bwd(ctx, true, true, true));
     grd_prof_mark(ctx, 3);
     TRY(grd_enqueue_update(ctx));
   }

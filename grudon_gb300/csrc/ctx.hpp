@@ -144,8 +144,9 @@ __host__ __device__ inline int rm_branch(int mode, unsigned long long frontier, 
 __host__ __device__ inline bool rm_is_pull(int m) { return m == RM_PULL_BITVEC || m == RM_PULL_LIST; }
 int grd_choose_round_mode(const grd_ctx* ctx);
 // degree_passes_done: 1 = the first degree pass already ran (k_fwd_list_deg),
-// 2 = both (k_fwd_xfer_deg).
-int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done = 0);
+// 2 = both (k_fwd_xfer_deg).  aggregate (push + bitvector, min algorithms):
+// the dirty diff also runs the backward transfer and the aggregate.
+int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done = 0, bool aggregate = false);
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode);
 uint32_t grd_round_launches(const grd_ctx* ctx, int mode);
 int grd_enqueue_fwd_list(grd_ctx* ctx);

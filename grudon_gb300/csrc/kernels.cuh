@@ -1267,6 +1267,63 @@ __global__ void __launch_bounds__(256) k_diff_dirty(DevGraph g, DevState st) {
   if (threadIdx.x == 0) st.tile_cnt[t] = c;
 }
 
+// Push + bitvector rounds of the min algorithms: the dirty diff, the
+// backward transfer and the aggregate in one pass over the slots.  The
+// backward compaction only gives each dirty value its rank in the packed
+// message, which the fused path never writes; a dirty slot needs nothing but
+// its own gid.  So each thread retires its dirty slot (the snapshot becomes
+// the sent value, as OpBwdXfer) and folds the value into vertex_updates with
+// red.min.  The tile's words of MD (not needed: left clear, as the backward
+// compaction leaves them) and of the forward bitvector are cleared, and the
+// sync bytes counted as the backward compaction counts them.
+template <int A>
+__global__ void __launch_bounds__(256) k_diff_aggregate(DevGraph g, DevState st) {
+  static_assert(A != A_PR_DELTA && A != A_PR_PULL, "PageRank aggregates partition by partition");
+  constexpr int U = 4;  // slots in flight per thread (8: more registers, 3 blocks per SM, slower)
+  static_assert(K_TILE_SLOTS % (256 * U) == 0, "whole steps per tile");
+  const uint32_t t = blockIdx.x;
+  const uint64_t s0 = (uint64_t)t * K_TILE_SLOTS;
+  uint32_t c = 0;
+  for (uint32_t i0 = 0; i0 < K_TILE_SLOTS; i0 += 256 * U) {
+    uint32_t a[U], b[U], gid[U], cur[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t s = s0 + i0 + u * 256 + threadIdx.x;
+      a[u] = __ldcg(&st.mupd[s]);
+      b[u] = __ldcg(&st.snap[s]);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t s = s0 + i0 + u * 256 + threadIdx.x;
+      gid[u] = a[u] < b[u] ? __ldg(&g.slot_gid[s]) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) cur[u] = a[u] < b[u] ? __ldcg(&st.upd[gid[u]]) : 0u;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t s = s0 + i0 + u * 256 + threadIdx.x;
+      const bool dirty = a[u] < b[u];
+      if (dirty) {
+        st.snap[s] = a[u];
+        if (a[u] < cur[u]) red_min(st.upd + gid[u], a[u]);
+      }
+      const uint32_t m = __ballot_sync(FULL, dirty);
+      if (lane_id() == 0) {
+        st.FB[s >> 5] = 0;
+        st.MD[s >> 5] = 0;
+        c += __popc(m);
+      }
+    }
+  }
+  c = block_sum(c);
+  if (threadIdx.x == 0) {
+    unsigned long long bytes = 4ull * c, rbytes = 4ull * c;
+    if (t == 0) bytes += g.bv_bytes, rbytes += g.bv_refbytes;
+    if (bytes) atomicAdd(&st.counters[C_BYTES], bytes);
+    if (rbytes) atomicAdd(&st.counters[C_REFBYTES], rbytes);
+  }
+}
+
 // -------------------------------------------------------------- pull map --
 // Pull edge-map over each partition's in-edge lists (sources in ascending
 // slot order).  Min algorithms fold every in-edge: a source that is not in
