@@ -423,11 +423,38 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bo
     if (degree_passes_done < 1) k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     if (degree_passes_done < 2) k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
+    // Hub rows on the side stream, beside the load-balanced push; their
+    // blocks take the SMs as the push's blocks finish.  The two kernels only
+    // meet in atomics: reductions into mupd (min: the values do not depend
+    // on the order), dirty-bit claims and list appends, and the edge count.
+    // Profiling times each kernel alone: the hub rows then follow the push.
+    const bool hubs = ctx->g.num_hubs != 0;
+    const bool fork = hubs && !ctx->profiling;
+    cudaStream_t hs = fork ? ctx->side : ctx->stream;
+    if (fork) {
+      CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+      CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    }
     grd_prof_mark(ctx, 5);
     if (mode == RM_PUSH_BITVEC) {
       k_push_lbs<A, true><<<resident_grid(ctx, k_push_lbs<A, true>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       grd_prof_mark(ctx, 6);
-      if (ctx->g.num_hubs) k_hub_push<A, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (hubs) k_hub_push<A, true><<<hub_grid, 256, 0, hs>>>(ctx->g, ctx->st);
+    } else if (mode == RM_NO_OFFLOAD) {  // compute-side push into vertex_updates
+      k_push_lbs<A, false, true><<<resident_grid(ctx, k_push_lbs<A, false, true>), 256, 0, ctx->stream>>>(ctx->g,
+                                                                                                          ctx->st);
+      grd_prof_mark(ctx, 6);
+      if (hubs) k_hub_push<A, false, true><<<hub_grid, 256, 0, hs>>>(ctx->g, ctx->st);
+    } else {
+      k_push_lbs<A, false><<<resident_grid(ctx, k_push_lbs<A, false>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      grd_prof_mark(ctx, 6);
+      if (hubs) k_hub_push<A, false><<<hub_grid, 256, 0, hs>>>(ctx->g, ctx->st);
+    }
+    if (fork) {
+      CK(cudaEventRecord(ctx->ev_join, ctx->side));
+      CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+    }
+    if (mode == RM_PUSH_BITVEC) {
       if constexpr (A != A_PR_DELTA && A != A_PR_PULL) {
         if (aggregate) {
           k_diff_aggregate<A><<<ctx->g.num_tiles, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
@@ -436,15 +463,6 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bo
         }
       }
       k_diff_dirty<A><<<ctx->g.num_tiles, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-    } else if (mode == RM_NO_OFFLOAD) {  // compute-side push into vertex_updates
-      k_push_lbs<A, false, true><<<resident_grid(ctx, k_push_lbs<A, false, true>), 256, 0, ctx->stream>>>(ctx->g,
-                                                                                                          ctx->st);
-      grd_prof_mark(ctx, 6);
-      if (ctx->g.num_hubs) k_hub_push<A, false, true><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-    } else {
-      k_push_lbs<A, false><<<resident_grid(ctx, k_push_lbs<A, false>), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-      grd_prof_mark(ctx, 6);
-      if (ctx->g.num_hubs) k_hub_push<A, false><<<hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     }
     CK_LAUNCH();
     return GRD_OK;
@@ -815,6 +833,9 @@ void grd_ctx_destroy(grd_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
   if (ctx->h_small) cudaFreeHost(ctx->h_small);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   (void)cudaGetLastError();
   delete ctx;
@@ -1348,6 +1369,9 @@ int grd_ctx_init_stream(grd_ctx* ctx) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
   CK(cudaMallocHost((void**)&ctx->h_counters, sizeof(unsigned long long) * (NUM_COUNTERS + 16)));
   std::memset(ctx->h_counters, 0, sizeof(unsigned long long) * (NUM_COUNTERS + 16));
   ctx->h_seed = ctx->h_counters + NUM_COUNTERS;

@@ -25,6 +25,11 @@ struct PullState {
 struct grd_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // The push edge-map runs the hub rows (k_hub_push) on `side`, beside the
+  // load-balanced push: fork and join are events on the two streams, also
+  // inside a graph capture (two parallel kernel nodes).
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int num_sms = 0;
   grd::Layout L;
   grd::DevGraph g{};
