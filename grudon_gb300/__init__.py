@@ -383,23 +383,32 @@ class Context:
                                               C.byref(n)))
         return out.reshape(-1, 3) if name in ("hubs", "in_hubs", "in_meds") else out
 
-    def _read(self, fn, dtype, n):
-        out = np.empty(n, dtype=dtype)
+    def _read(self, fn, dtype, n, out=None):
+        """out: a caller's array to fill (for example a view of pinned host
+        memory, which the copy reaches at the link's full speed); a new array
+        otherwise."""
+        if out is None:
+            out = np.empty(n, dtype=dtype)
+        elif out.dtype != dtype or out.size < n or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out must be a contiguous {np.dtype(dtype).name} array of at least {n} elements")
         self._check(fn(self._ctx, out.ctypes.data_as(C.c_void_p), out.nbytes))
         return out
 
-    def read_props(self) -> np.ndarray:
+    def read_props(self, out=None) -> np.ndarray:
         dt = np.float32 if self.algo in (GRD_PR_DELTA, GRD_PR_PULL) else np.uint32
-        return self._read(self._lib.grd_read_props, dt, self.num_vertices)
+        return self._read(self._lib.grd_read_props, dt, self.num_vertices, out)
 
-    def read_ranks(self) -> np.ndarray:
-        out = np.empty(self.num_vertices, dtype=np.float32)
+    def read_ranks(self, out=None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.num_vertices, dtype=np.float32)
+        elif out.dtype != np.float32 or out.size < self.num_vertices or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out must be a contiguous float32 array of at least {self.num_vertices} elements")
         self._check(self._lib.grd_read_ranks(self._ctx, out.ctypes.data_as(C.c_void_p), out.size))
         return out
 
-    def read_updates(self) -> np.ndarray:
+    def read_updates(self, out=None) -> np.ndarray:
         dt = np.float32 if self.algo in (GRD_PR_DELTA, GRD_PR_PULL) else np.uint32
-        return self._read(self._lib.grd_read_updates, dt, self.num_vertices)
+        return self._read(self._lib.grd_read_updates, dt, self.num_vertices, out)
 
     def read_frontier(self) -> np.ndarray:
         words = (self.num_vertices + 31) // 32

@@ -209,3 +209,31 @@ def test_upload_sends_byte_weights_and_derives_vertex_arrays(gpu):
             np.testing.assert_array_equal(ctx.read_layout("outdeg"), np.diff(graph.row_offsets).astype(np.uint32))
     assert sizes[0] == sizes[1] and sizes[2] == sizes[3]
     assert sizes[2] - sizes[0] == 3 * G.num_edges
+
+
+@pytest.mark.gpu
+def test_read_into_caller_arrays(gpu):
+    """read_props / read_updates / read_ranks fill a caller's array (a
+    serving loop keeps pinned result buffers) and refuse one of the wrong
+    type or size."""
+    G = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
+    part = G.partition_edge_balanced(3)
+    ref = O.run(O.ORC_SSSP_W, G.row_offsets, G.col_indices, G.weights, mirror=part, num_memory=3)
+    V = G.num_vertices
+    with g.Context(G, part, num_memory=3) as ctx:
+        ctx.set_algo(g.GRD_SSSP_W)
+        out = np.zeros(V + 5, dtype=np.uint32)  # larger than needed
+        for _ in range(2):
+            ctx.init()
+            ctx.run()
+            assert ctx.read_props(out=out) is out
+            np.testing.assert_array_equal(out[:V], ref["props"])
+            np.testing.assert_array_equal(ctx.read_updates(out=np.empty(V, np.uint32)), ctx.read_updates())
+        with pytest.raises(ValueError):
+            ctx.read_props(out=np.zeros(V, dtype=np.int64))
+        with pytest.raises(ValueError):
+            ctx.read_props(out=np.zeros(V - 1, dtype=np.uint32))
+        with pytest.raises(ValueError):
+            ctx.read_props(out=np.zeros(2 * V, dtype=np.uint32)[::2])
+        ranks = np.empty(V, dtype=np.float32)
+        assert ctx.read_ranks(out=ranks) is ranks
