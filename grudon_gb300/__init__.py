@@ -394,9 +394,17 @@ class Context:
         self._check(fn(self._ctx, out.ctypes.data_as(C.c_void_p), out.nbytes))
         return out
 
-    def read_props(self, out=None) -> np.ndarray:
+    def read_props(self, out=None, wait: bool = True) -> np.ndarray:
+        """wait=False queues the copy into `out` on the ctx stream and returns
+        at once (grd_read_props_async): `out` holds the values after
+        synchronize(), or wait() for a run(wait=False) queued before it;
+        give pinned memory for a truly queued copy."""
         dt = np.float32 if self.algo in (GRD_PR_DELTA, GRD_PR_PULL) else np.uint32
-        return self._read(self._lib.grd_read_props, dt, self.num_vertices, out)
+        if wait:
+            return self._read(self._lib.grd_read_props, dt, self.num_vertices, out)
+        if out is None:
+            raise ValueError("read_props(wait=False) needs the caller's out array")
+        return self._read(self._lib.grd_read_props_async, dt, self.num_vertices, out)
 
     def read_ranks(self, out=None) -> np.ndarray:
         if out is None:

@@ -146,6 +146,7 @@ SIGNATURES = {
     "grd_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "grd_get_round_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "grd_read_props": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "grd_read_props_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_ranks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_updates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_frontier": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),

@@ -1251,6 +1251,18 @@ int grd_read_props(grd_ctx* ctx, void* host, size_t bytes) {
   return read_dev(ctx, host, ctx->st.prop, bytes, sizeof(uint32_t) * ctx->L.V);
 }
 
+int grd_read_props_async(grd_ctx* ctx, void* host, size_t bytes) {
+  if (!ctx || !host) return GRD_E_INVALID;
+  const size_t need = sizeof(uint32_t) * ctx->L.V;
+  if (bytes < need) {
+    ctx->err = "host buffer too small: need " + std::to_string(need) + " bytes";
+    return GRD_E_INVALID;
+  }
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpyAsync(host, ctx->st.prop, need, cudaMemcpyDeviceToHost, ctx->stream));
+  return GRD_OK;
+}
+
 int grd_read_ranks(grd_ctx* ctx, float* host, size_t count) {
   if (!ctx) return GRD_E_INVALID;
   return read_dev(ctx, host, ctx->st.ranks, count * sizeof(float), sizeof(float) * ctx->L.V);

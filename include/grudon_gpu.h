@@ -295,6 +295,14 @@ int grd_get_round_log(const grd_ctx* ctx, grd_round_rec* out, size_t cap,
 /* Compute-side vertex_properties, gid order (uint32 for CC/SSSP, float for PR
  * contributions). */
 int grd_read_props(grd_ctx* ctx, void* host, size_t bytes);
+/* The same copy queued on the ctx stream after the work queued so far, without
+ * waiting: `host` holds the values once grd_synchronize returns, or grd_wait
+ * for an asynchronous run queued before the copy (pinned memory; a pageable
+ * buffer makes the copy synchronous).  Lets a
+ * caller chain upload, run and read of several contexts with no host round
+ * trip in between.  No counterpart in the reference, whose results stay in
+ * host memory. */
+int grd_read_props_async(grd_ctx* ctx, void* host, size_t bytes);
 /* PageRank values (pr_vals for PR_DELTA, ranks for PR_PULL), float[V]. */
 int grd_read_ranks(grd_ctx* ctx, float* host, size_t count);
 /* Compute-side vertex_updates, gid order. */

@@ -237,3 +237,13 @@ def test_read_into_caller_arrays(gpu):
             ctx.read_props(out=np.zeros(2 * V, dtype=np.uint32)[::2])
         ranks = np.empty(V, dtype=np.float32)
         assert ctx.read_ranks(out=ranks) is ranks
+        # queued: run and read without waiting, then complete the run
+        import torch
+        pinned = torch.zeros(V, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+        ctx.init()
+        ctx.run(wait=False)
+        assert ctx.read_props(out=pinned, wait=False) is pinned
+        ctx.wait()
+        np.testing.assert_array_equal(pinned, ref["props"])
+        with pytest.raises(ValueError):
+            ctx.read_props(wait=False)
