@@ -422,7 +422,9 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bo
     const uint32_t B = lbs_blocks(ctx);
     if (degree_passes_done < 1) k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
     if (degree_passes_done < 2) k_deg_down<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-    const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 8));
+    // one block per hub item up to 32 per SM: beside the push, more and
+    // shorter blocks fill the SMs the push frees sooner (8 per SM: +1.3 % step)
+    const uint32_t hub_grid = std::min<uint32_t>(ctx->g.num_hubs, grid_for(ctx, 32));
     // Hub rows on the side stream, beside the load-balanced push; their
     // blocks take the SMs as the push's blocks finish.  The two kernels only
     // meet in atomics: reductions into mupd (min: the values do not depend
