@@ -827,6 +827,7 @@ void grd_ctx_destroy(grd_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
   }
+  if (ctx->side) cudaStreamSynchronize(ctx->side);  // joined into `stream` unless a call failed in between
   grd_ctx_release_extras(ctx);
   grd_graph_release(ctx);
   for (void* p : ctx->allocs) cudaFree(p);
