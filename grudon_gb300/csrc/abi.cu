@@ -141,6 +141,7 @@ int grd_upload_layout(grd_ctx* ctx) {
   const Layout& L = ctx->L;
   DevGraph& g = ctx->g;
   ctx->upload_bytes = 0;
+  ctx->layout_gen++;  // derived arrays (PR_PULL) are rebuilt from the new copy
   TRY(upload(ctx, (uint32_t*)g.slot_gid, L.slot_gid));
   TRY(upload(ctx, (uint32_t*)g.row_off, L.row_off));
   TRY(upload(ctx, (uint32_t*)g.col, L.col));
@@ -1066,9 +1067,12 @@ int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats) {
   TRY(grd_wait(ctx, nullptr));  // a previous asynchronous run first
   bool device_loop = false;
   const bool async = (flags & GRD_RUN_ASYNC) != 0;
-  if (ctx->algo != GRD_PR_PULL && !ctx->profiling && !(flags & GRD_RUN_HOST_LOOP) &&
-      ctx->stats.rounds < ctx->params.max_rounds)
-    TRY(grd_graph_run(ctx, &device_loop, async));
+  if (!ctx->profiling && !(flags & GRD_RUN_HOST_LOOP) && ctx->stats.rounds < ctx->params.max_rounds) {
+    if (ctx->algo == GRD_PR_PULL)
+      TRY(grd_pull_graph_run(ctx, &device_loop, async));
+    else
+      TRY(grd_graph_run(ctx, &device_loop, async));
+  }
   ctx->stats.device_loop = device_loop ? 1 : 0;
   if (!device_loop) TRY(grd_sync_init_counters(ctx));  // host-side decisions need the frontier shape
   if (device_loop) {

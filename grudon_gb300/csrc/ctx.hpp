@@ -11,10 +11,29 @@
 #include "layout.hpp"
 #include "policy.cuh"
 
+// PageRank Jacobi (GRD_PR_PULL) arrays derived from the resident layout
+// (pr_pull.cu): rebuilt whenever the layout changes.
+struct PrPullState {
+  uint64_t layout_gen = ~0ull;  // layout generation the arrays below describe
+  uint64_t E = 0, S_nz = 0, T = 0;  // in-edges, non-empty in-lists, 512-edge tiles
+  uint32_t H = 0;                // hot sources (staged in shared memory by the pull)
+  uint32_t hot_deg = 0;          // out-degree threshold of the hot set
+  uint64_t nondangling = 0;      // vertices with out-edges
+  uint64_t cap_E = 0, cap_S = 0, cap_V = 0, cap_T = 0;  // allocated sizes
+  uint32_t* src = nullptr;       // [E] in-edges, lists vertex-major: hot rank | 0x80000000, or the source slot
+  uint32_t* start_bits = nullptr;  // [E/32 + 2] bit e: edge e opens a non-empty in-list
+  uint32_t* tile_nz = nullptr;   // [T + 1] non-empty in-lists opened before tile t
+  uint4* piece = nullptr;        // [T] (head, tail sum, tail compensation, tail list)
+  uint32_t* piece_flags = nullptr;  // [T]
+  float* part = nullptr;         // [S_nz] partial sum of each non-empty in-list, vertex-major
+  uint32_t* vmap_off = nullptr;  // [V + 1] per vertex: its in-lists' range in part
+  uint32_t* hot_base = nullptr;  // [V/32 + 1] hot rank of each 32-vertex word's first hot vertex
+  float* hot_val = nullptr;      // [H] contributions of the hot sources
+  double* resid_part = nullptr;  // [update blocks] residual partial sums
+  uint32_t update_blocks = 0;
+};
+
 struct PullState {
-  uint32_t* comp = nullptr;       // [V] Kahan compensation of the aggregate
-  double* residual = nullptr;     // [1] FP64 L1 residual of the last iteration
-  double* h_residual = nullptr;   // pinned mirror
   grd::HubChunkD* in_hubs = nullptr;  // destination slots with long in-lists
   uint32_t num_in_hubs = 0;
   grd::HubChunkD* in_meds = nullptr;  // destination slots with medium in-lists
@@ -44,7 +63,9 @@ struct grd_ctx {
   unsigned long long* h_seed = nullptr;      // = h_counters + NUM_COUNTERS
   uint64_t upload_bytes = 0;
   bool in_edges_alloc = false;
+  uint64_t layout_gen = 0;     // bumped whenever a layout array is rewritten
   PullState pull;
+  PrPullState pr;
   uint64_t last_frontier = 0;  // |frontier| entering the next round
   uint64_t last_fedges = 0;    // its out-edges
   std::vector<grd_round_rec> round_log;  // profiled host-loop rounds
@@ -52,6 +73,8 @@ struct grd_ctx {
   cudaGraph_t run_graph = nullptr;     // device-driven round loop (graph_run.cu)
   cudaGraphExec_t run_exec = nullptr;
   cudaGraphExec_t round_exec[7] = {};  // one round per branch (profiled host loop)
+  cudaGraph_t pr_graph = nullptr;      // PR_PULL device-driven loop (pr_pull.cu)
+  cudaGraphExec_t pr_exec = nullptr;
   bool graph_failed = false;           // building it failed here: host loop
   std::string graph_error;
   uint32_t* agg_buf = nullptr; // staging of grd_aggregate_values (gids, values)
@@ -171,6 +194,15 @@ int grd_round_graph_launch(grd_ctx* ctx, int mode);
 void grd_graph_release(grd_ctx* ctx);
 int grd_enqueue_bwd(grd_ctx* ctx, bool fused, bool do_pack, bool do_aggregate);
 int grd_enqueue_update(grd_ctx* ctx);
-// PR_PULL: stage 0 fwd, 1 pull edge-map, 2 bwd pack, 3 aggregate, 4 update.
+// PR_PULL (pr_pull.cu): stage -1 init, 0 fwd, 1 pull edge-map, 2 bwd, 3
+// aggregate, 4 update; the host-driven loop; the device-driven loop (one
+// graph launch, *used = false when it cannot be built here).
 int grd_pull_stage(grd_ctx* ctx, int stage);
 int grd_pull_run(grd_ctx* ctx);
+int grd_pull_graph_run(grd_ctx* ctx, bool* used, bool async);
+void grd_pull_graph_release(grd_ctx* ctx);
+int grd_pull_run_finish(grd_ctx* ctx);
+// Exclusive add-scan of n u32 (out may alias in); with total_at_n, out[n]
+// also receives the total (layout_dev.cu).
+int grd_scan_add_u32(grd_ctx* ctx, const uint32_t* in, uint32_t* out, uint64_t n, bool total_at_n);
+int grd_scan_u32(grd_ctx* ctx, const uint32_t* in, uint32_t* out, uint64_t n, bool inclusive, bool total_at_n);

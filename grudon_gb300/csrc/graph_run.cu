@@ -146,6 +146,7 @@ int build(grd_ctx* ctx) {
 }  // namespace
 
 void grd_graph_release(grd_ctx* ctx) {
+  grd_pull_graph_release(ctx);
   if (ctx->run_exec) cudaGraphExecDestroy(ctx->run_exec);
   if (ctx->run_graph) cudaGraphDestroy(ctx->run_graph);
   ctx->run_exec = nullptr;
@@ -223,6 +224,7 @@ int grd_graph_run(grd_ctx* ctx, bool* used, bool async) {
 
 // Statistics of a finished loop launch (its counters already on the host).
 int grd_graph_run_finish(grd_ctx* ctx) {
+  if (ctx->algo == GRD_PR_PULL) return grd_pull_run_finish(ctx);
   if (!ctx->run_exec) return GRD_OK;
   const unsigned long long* c = ctx->h_counters;
   ctx->stats.rounds = (uint32_t)c[C_ROUNDS];

@@ -34,7 +34,7 @@ enum Counter : int {
   C_EDGES = 2,     // cumulative edges scanned
   C_BYTES = 3,     // cumulative wire bytes (true size)
   C_REFBYTES = 4,  // cumulative bytes by the reference's accounting
-  // 5: unused
+  C_RESID = 5,     // PR_PULL: L1 residual of the last iteration (FP64 bits)
   C_ERR = 6,       // first device-side error code (0 = none)
   C_PULL_EDGES = 7,
   C_MEDGES = 8,    // edges of the load-balanced push this round (non-hub rows)

@@ -349,6 +349,16 @@ std::string layout_error(uint32_t err) {
 }  // namespace
 
 // Checks the host-visible parts of a CSR for the device build.
+int grd_scan_add_u32(grd_ctx* ctx, const uint32_t* in, uint32_t* out, uint64_t n, bool total_at_n) {
+  Scratch tmp(ctx);
+  return scan<OpAdd>(ctx, tmp, in, out, n, false, total_at_n);
+}
+
+int grd_scan_u32(grd_ctx* ctx, const uint32_t* in, uint32_t* out, uint64_t n, bool inclusive, bool total_at_n) {
+  Scratch tmp(ctx);
+  return scan<OpAdd>(ctx, tmp, in, out, n, inclusive, total_at_n);
+}
+
 int grd_device_layout_check(const grd_csr* graph, uint32_t M, std::string* why) {
   if (!graph) return *why = "graph is NULL", GRD_E_INVALID;
   if (M == 0 || M > DEV_MAX_PARTS) return *why = "the device layout build takes 1..64 memory partitions", GRD_E_INVALID;
@@ -376,6 +386,7 @@ int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* 
   // finished, the ctx refuses to run (a graph that turns out not to match
   // the ctx's partition, proxy or hub counts leaves it that way).
   ctx->layout_valid = false;
+  ctx->layout_gen++;
   cudaStream_t s = ctx->stream;
   Scratch tmp(ctx);
   // inputs
@@ -620,5 +631,6 @@ int grd_device_in_edges(grd_ctx* ctx) {
   CK_LAUNCH();
   CK(cudaStreamSynchronize(s));
   ctx->in_edges_alloc = true;
+  ctx->layout_gen++;
   return GRD_OK;
 }
