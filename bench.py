@@ -1,22 +1,28 @@
 """Benchmark of the per-round graph operator on one GB300 (replicas for N>1).
 
-Workload (one step): connected components on the symmetrised graph and
-weighted SSSP (uint32 weights in [1,255], source 0) on the directed graph,
-both seeded RMAT scale 22 (4.19M vertices, edge factor 16, a/b/c/d =
-0.57/0.19/0.19/0.05, self-loops and duplicates removed), laid out as 1
-compute + 3 memory partitions (edge-balanced contiguous ranges) in HBM with
-bitvector-compacted sync.  Every step runs both algorithms to convergence
-from init().  The graphs are synthetic (no dataset is involved).
+Workload (one step, the PR/CC/SSSP RMAT-24 metric): on seeded RMAT scale 24
+(16.8M vertices, edge factor 16, a/b/c/d = 0.57/0.19/0.19/0.05, self-loops
+and duplicates removed), laid out as 1 compute + 3 memory partitions
+(edge-balanced contiguous ranges) in HBM with bitvector-compacted sync:
+  * connected components on the symmetrised graph, to convergence;
+  * weighted SSSP (uint32 weights in [1,255], source 0) on the directed
+    graph, to convergence;
+  * PageRank (Jacobi, damping 0.85, FP32 ranks with Kahan-compensated sums,
+    FP64 residual) on the directed graph until the L1 residual / V < 1e-7 or
+    100 iterations.
+The graphs are synthetic (no dataset is involved).
 
-value: Graph500-style GTEPS = (E_cc + E_sssp) / step time, inputs resident in
-HBM, CUDA events on the ctx streams.  e2e: the same through the C ABI with
-host buffers: every step uploads the partitioned CSR (pinned host memory),
-runs, and reads the results back.
+value: Graph500-style GTEPS = (E_cc + E_sssp + iterations * E_pr) / step time,
+inputs resident in HBM, CUDA events on the ctx streams.  e2e: the same
+through the C ABI with host buffers: every step uploads the three partitioned
+layouts from pinned host memory, runs, and reads the results back.
 
-`--impl reference` times the reference algorithm on the host cores: the
+`--impl reference` times the reference algorithm on the host cores.  The
 reference project cannot be built (its Galois/MPI dependencies are absent),
-so the arm runs the oracle's restatement of its round protocol with all host
-threads ("kind": "port").
+so the arm runs the oracle's restatement of its round protocol (CC, SSSP) and
+of the PageRank workload's Jacobi iteration with all host threads ("kind":
+"port"), on graphs made by the oracle's own generator: it loads no library of
+the product.
 """
 from __future__ import annotations
 
@@ -34,11 +40,13 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "GTEPS (PR/CC/SSSP, RMAT-24) & % HBM roofline; learned+batched vs plain GPU"
-SCALE, EF, NUM_MEMORY = 22, 16, 3
+SCALE, EF, NUM_MEMORY = 24, 16, 3
 RMAT_ABC = (0.57, 0.19, 0.19)
-# DRAM bytes (read + write) per edge of k_push_lbs in its ncu capture (CC
-# round 0 on RMAT-21, every vertex active): 249.9 MB for the 50.2 M edges of
-# non-hub rows.
+PR_MAX_ITERS, PR_TOL = 100, 1e-7
+# DRAM bytes (read + write) per in-edge of k_pr_pull in its ncu capture
+# (PageRank RMAT-22, 65.2 M in-edges): 291.9 MB per launch.
+DRAM_BYTES_PER_PULL_EDGE = 291.9e6 / 65.24e6
+# ... and of k_push_lbs (CC round 0 on RMAT-21): 249.9 MB for 50.2 M edges.
 DRAM_BYTES_PER_PUSH_EDGE = 249.9e6 / 50.2e6
 
 
@@ -50,25 +58,489 @@ def parse():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--scale", type=int, default=SCALE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-pagerank", action="store_true")
-    ap.add_argument("--pr-scale", type=int, default=24)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline, e2e and parity only (no batch, policy, offload, ingest or RMAT-22 legs)")
     ap.add_argument("--batch", action="store_true", help="run the batched workload (default at N=1)")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=512)
     ap.add_argument("--batch-sources", type=int, default=64)
     ap.add_argument("--policy", choices=["fixed", "learned"], default="fixed",
-                    help="round policy of the headline runs (the other one is timed beside it when the model "
-                         "file is present)")
-    ap.add_argument("--kernel-run-pr", action="store_true",
-                    help="only run PageRank (Jacobi pull, RMAT-{pr-scale}) for warmup + steps iterations and print a "
-                         "short summary: the target of per-kernel profilers")
-    ap.add_argument("--ingest-run", action="store_true",
-                    help="only build the partition layouts of the workload's graphs on the GPU "
-                         "(grd_ingest, warmup + steps times each), for profiling")
+                    help="round policy of the CC/SSSP runs of the headline (the other one is timed beside it when "
+                         "the model file is present)")
     ap.add_argument("--kernel-run", action="store_true",
                     help="only run the workload's steps with the rounds driven from the host (plain kernel "
                          "launches, no CUDA graphs) and print a short summary: the target of per-kernel profilers")
+    ap.add_argument("--kernel-run-pr", action="store_true",
+                    help="only run PageRank (RMAT-{scale}) for warmup + steps iterations from the host: the "
+                         "target of per-kernel profilers")
     return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def csr_checksum(ro, col, w=None) -> str:
+    """Order-sensitive 64-bit digest of a CSR (hex): both arms state which
+    graphs they ran in their config."""
+    import numpy as np
+    m = np.uint64(0x9E3779B97F4A7C15)
+    with np.errstate(over="ignore"):
+        acc = np.uint64(len(ro) - 1) * m
+        for arr in (ro, col, w):
+            if arr is None:
+                continue
+            a = np.ascontiguousarray(arr).astype(np.uint64, copy=False)
+            idx = np.arange(1, len(a) + 1, dtype=np.uint64)
+            acc = acc * np.uint64(31) + np.sum((a + np.uint64(1)) * (idx * m | np.uint64(1)), dtype=np.uint64)
+    return f"{int(acc):016x}"
+
+
+def workload_config(scale, seed, V, E_cc, E_dir, ck_cc, ck_dir, ws) -> dict:
+    return {
+        "workload": f"one step = CC (symmetrised) + weighted SSSP (w in [1,255], source 0) + PageRank (Jacobi, "
+                    f"FP32 Kahan sums, FP64 residual, until L1 residual/V < {PR_TOL:g} or {PR_MAX_ITERS} "
+                    f"iterations), RMAT-{scale} ef{EF} a/b/c/d .57/.19/.19/.05, 1 compute + {NUM_MEMORY} memory "
+                    f"partitions with bitvector-compacted sync",
+        "scale": scale, "edge_factor": EF, "seed": seed, "num_vertices": V,
+        "E_cc_symmetrised": E_cc, "E_directed": E_dir,
+        "csr_checksum": {"symmetrised": ck_cc, "directed_weighted": ck_dir},
+        "partitions": f"1C+{NUM_MEMORY}M edge-balanced contiguous",
+        "units": "GTEPS = (E_cc + E_sssp + pagerank_iterations * E_pr) / step time",
+        "l2": "inputs larger than L2 (CSR indices 1-2 GB > 129 MB), no flush",
+        "parallelism": f"replicas x{ws}",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 20 ms during the timed
+    region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak() -> tuple[float, str]:
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+        if "hbm_gbs" in peaks:
+            return float(peaks["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------- GPU arm --
+def load_policy_model():
+    """The shipped learned round-policy model, or None."""
+    from grudon_gb300 import policy as P
+    return P.load_model() if P.MODEL_FILE.exists() else None
+
+
+class Workload:
+    """The three contexts of one step: CC on the symmetrised graph, weighted
+    SSSP and PageRank on the directed graph (each its own partitioned layout
+    in HBM, each on its own stream)."""
+
+    def __init__(self, g, scale, threads, local):
+        a, b, c = RMAT_ABC
+        self.g = g
+        self.seed = g.rmat_seed(scale, EF)
+        self.G_cc = g.Graph.rmat(scale, EF, a, b, c, seed=self.seed, symmetrize=True, threads=threads)
+        self.G_d = g.Graph.rmat(scale, EF, a, b, c, seed=self.seed, weighted=True, threads=threads)
+        self.p_cc = self.G_cc.partition_edge_balanced(NUM_MEMORY)
+        self.p_d = self.G_d.partition_edge_balanced(NUM_MEMORY)
+        self.cc = g.Context(self.G_cc, self.p_cc, num_memory=NUM_MEMORY, device=local)
+        self.ss = g.Context(self.G_d, self.p_d, num_memory=NUM_MEMORY, device=local)
+        self.pr = g.Context(self.G_d, self.p_d, num_memory=NUM_MEMORY, device=local)
+        self.pr.set_algo(g.GRD_PR_PULL, max_rounds=PR_MAX_ITERS, tolerance=PR_TOL)
+        self.ctxs = (self.cc, self.ss, self.pr)
+        self.E_cc, self.E_d = self.G_cc.num_edges, self.G_d.num_edges
+        self.V = self.G_cc.num_vertices
+
+    def set_policy(self, policy, model=None, offload=None):
+        g = self.g
+        off = g.GRD_OFFLOAD_NDP if offload is None else offload
+        for c, a in ((self.cc, g.GRD_CC), (self.ss, g.GRD_SSSP_W)):
+            c.set_algo(a, policy=policy, offload=off)
+            c.set_policy(model if policy == g.GRD_POLICY_LEARNED else None)
+
+    def units(self, sts) -> float:
+        return self.E_cc + self.E_d + sts[2]["rounds"] * self.E_d
+
+    def close(self):
+        for c in self.ctxs:
+            c.close()
+
+
+def timed_steps(W, args, barrier, streams, which=(0, 1, 2)):
+    """W warm-up steps, then K timed steps: every step runs the contexts in
+    `which` to convergence from init(), each as one device-driven CUDA-graph
+    launch.  CUDA events on the ctx streams bracket the step and each run."""
+    import torch
+    ctxs = [W.ctxs[i] for i in which]
+    strm = [streams[i] for i in which]
+
+    def step():
+        out = []
+        for c in ctxs:
+            c.init()
+            out.append(c.run())
+        return out
+
+    for _ in range(args.warmup):
+        step()
+    per = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(len(ctxs) * args.steps)]
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    agg = {"units": 0.0, "edges": 0, "launches": 0, "rounds": [], "pr_iterations": [], "device_loop": True,
+           "push_rounds": 0, "pull_rounds": 0}
+    barrier()
+    ev0.record(strm[0])
+    k = 0
+    for _ in range(args.steps):
+        sts = []
+        for c, s in zip(ctxs, strm):
+            per[k][0].record(s)
+            c.init()
+            st = c.run()
+            per[k][1].record(s)
+            k += 1
+            sts.append(st)
+        for st in sts:
+            agg["edges"] += st["edges_scanned"]
+            agg["launches"] += st["kernel_launches"]
+            agg["device_loop"] = agg["device_loop"] and bool(st["device_loop"])
+            agg["push_rounds"] += st["push_rounds"]
+            agg["pull_rounds"] += st["pull_rounds"]
+        agg["rounds"].append([st["rounds"] for st in sts])
+        if which == (0, 1, 2):
+            agg["units"] += W.units(sts)
+            agg["pr_iterations"].append(sts[2]["rounds"])
+        else:
+            agg["units"] += sum((W.E_cc, W.E_d, W.E_d)[i] * (1 if i < 2 else st["rounds"])
+                                for i, st in zip(which, sts))
+    ev1.record(strm[-1])
+    barrier()
+    secs = ev0.elapsed_time(ev1) / 1e3
+    per_ms = [[0.0] * args.steps for _ in ctxs]
+    for j in range(len(ctxs) * args.steps):
+        per_ms[j % len(ctxs)][j // len(ctxs)] = per[j][0].elapsed_time(per[j][1])
+    agg["ctx_ms"] = [statistics.median(x) for x in per_ms]
+    return secs, agg
+
+
+def profile_pass(W):
+    """The same step with the rounds driven from the host and CUDA events
+    around every stage and around the two edge-map kernels (the
+    load-balanced push of CC/SSSP, the edge-balanced pull of PageRank)."""
+    out = {}
+    for c in W.ctxs:
+        c.set_profiling(True)
+    try:
+        for name, c in zip(("cc", "sssp", "pagerank"), W.ctxs):
+            c.init()
+            out[name] = c.run(host_loop=True)
+    finally:
+        for c in W.ctxs:
+            c.set_profiling(False)
+    return out
+
+
+def roofline_of(W, prof, pr_run_ms, peak, peak_src):
+    """k_pr_pull (the dominant kernel: the PageRank edge-map) by the pull
+    round's algorithmic bytes, the whole PageRank iteration by its
+    algorithmic bytes, and the load-balanced push of CC/SSSP."""
+    p = prof["pagerank"]
+    S = sum(sum(W.pr.layout_info(i)[:2]) for i in range(NUM_MEMORY))
+    V, E = W.V, W.E_d
+    # pull round over every slot: offsets, partial write, per in-edge its
+    # index and the source value gathered, the frontier bitmap
+    pull_bytes = (S + 1) * 4 + S * 4 + E * 8 + V / 8
+    nl = max(p["pull_launches"], 1)
+    pull_ms = p["pull_ms"] / nl
+    ach = pull_bytes / (pull_ms / 1e3) / 1e9 if pull_ms > 0 else 0.0
+    it = max(p["rounds"], 1)
+    iter_bytes = V * 16 + E * 8  # per iteration: offset, contribution read, rank and contribution writes; index + gather per edge
+    iter_ms = pr_run_ms / it
+    iter_ach = iter_bytes / (iter_ms / 1e3) / 1e9
+    push = {}
+    lbs_ms = sum(prof[k]["lbs_ms"] for k in ("cc", "sssp"))
+    lbs_n = max(sum(prof[k]["lbs_launches"] for k in ("cc", "sssp")), 1)
+    lbs_bytes = sum(prof[k]["lbs_actives"] * 12 + prof[k]["lbs_edges"] * (12 + (4 if k == "sssp" else 0))
+                    for k in ("cc", "sssp"))
+    lbs_edges = sum(prof[k]["lbs_edges"] for k in ("cc", "sssp"))
+    if lbs_ms > 0:
+        a = lbs_bytes / (lbs_ms / 1e3) / 1e9
+        push = {"kernel": "k_push_lbs (load-balanced push edge-map of CC/SSSP)", "achieved": a, "frac": a / peak,
+                "alg_bytes_per_launch": lbs_bytes / lbs_n, "avg_launch_ms": lbs_ms / lbs_n, "launches": lbs_n,
+                "traffic": DRAM_BYTES_PER_PUSH_EDGE * lbs_edges / lbs_n}
+    return {
+        "bound": "hbm", "kernel": "k_pr_pull (edge-balanced PageRank pull edge-map)",
+        "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_source": peak_src,
+        # DRAM bytes per in-edge of the kernel's ncu capture times this graph's in-edges
+        "traffic": DRAM_BYTES_PER_PULL_EDGE * E,
+        "alg_bytes_per_launch": pull_bytes, "avg_launch_ms": pull_ms, "launches": p["pull_launches"],
+        "pagerank_iteration": {"alg_bytes": iter_bytes, "ms": iter_ms, "achieved": iter_ach,
+                               "frac": iter_ach / peak,
+                               "kernels": "k_pr_pull, k_pr_fix, k_pr_update, k_pr_round_end"},
+        "push_edge_map": push,
+        "stage_ms": {k: prof[k]["stage_ms"] for k in prof},
+    }
+
+
+def e2e_pass(W, args, barrier, streams, dev):
+    """End to end through the C ABI with host buffers: every step copies the
+    three layouts from pinned host memory and reads the three results back
+    into pinned host arrays.  Copies are pipelined with the runs: while one
+    context runs, the next one's layout is on the link; runs and reads are
+    queued (run(wait=False), read(wait=False)) and ordered by stream events so
+    that the three runs never share the GPU."""
+    import numpy as np
+    import torch
+    from grudon_gb300.replicas import job_throughput
+    V = W.V
+    res = [torch.empty(V, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+           torch.empty(V, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+           torch.empty(V, dtype=torch.float32, pin_memory=True).numpy()]
+
+    def read(i, c, wait):
+        return c.read_ranks(out=res[i], wait=wait) if i == 2 else c.read_props(out=res[i], wait=wait)
+
+    up_done = [torch.cuda.Event() for _ in range(3)]
+    run_done = [torch.cuda.Event() for _ in range(3)]
+    n = len(W.ctxs)
+    barrier()
+    t0 = time.perf_counter()
+    h2d = W.ctxs[0].upload()
+    for k in range(args.steps):
+        for i, c in enumerate(W.ctxs):
+            j = (i + 1) % n
+            if j or k + 1 < args.steps:  # the next layout goes on the link once this one is there
+                up_done[i].record(streams[i])
+                streams[j].wait_event(up_done[i])
+                h2d += W.ctxs[j].upload()
+            c.wait()
+            if k or i:
+                streams[i].wait_event(run_done[(i - 1) % n])
+            c.init()
+            c.run(wait=False)
+            read(i, c, False)
+            run_done[i].record(streams[i])
+    sts = [c.wait() for c in W.ctxs]
+    barrier()
+    secs = time.perf_counter() - t0
+    units = args.steps * W.units(sts)  # every step runs the same graphs from init()
+    thr, _, _ = job_throughput(units, secs, dev)
+    for i, c in enumerate(W.ctxs):  # the queued reads delivered the final results
+        got = res[i].copy()
+        if not np.array_equal(got, c.read_ranks() if i == 2 else c.read_props()):
+            raise RuntimeError("queued result reads differ from a blocking read")
+    return {"value": thr / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d // args.steps,
+            "d2h_bytes_per_step": 4 * 3 * V}
+
+
+def parity_and_cpu(W, gpu_out, pr_iters, threads):
+    """Outside the timed region: the oracle's restated round protocol (CC,
+    weighted SSSP) and the restated FP32-Kahan Jacobi PageRank on the same
+    graphs, all host threads, timed as the CPU baseline (one full step); the
+    GPU results against them (CC/SSSP bit-exact, rounds equal), the
+    reference's verify() invariants on the device, and the PageRank ranks
+    against FP64 Jacobi for the same iteration count (max relative error
+    <= 1e-5)."""
+    import numpy as np
+    from oracle import ffi as O
+    G_cc, G_d = W.G_cc, W.G_d
+    L_cc = O.Layout(G_cc.row_offsets, G_cc.col_indices, mirror=W.p_cc, num_memory=NUM_MEMORY)
+    L_ss = O.Layout(G_d.row_offsets, G_d.col_indices, G_d.weights, mirror=W.p_d, num_memory=NUM_MEMORY)
+    t0 = time.perf_counter()
+    r_cc = L_cc.run(O.ORC_CC, threads=threads)
+    t_cc = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r_ss = L_ss.run(O.ORC_SSSP_W, threads=threads)
+    t_ss = time.perf_counter() - t0
+    P = O.PrJacobi(G_d.row_offsets, G_d.col_indices, threads=threads)
+    P.init()
+    t0 = time.perf_counter()
+    it, _ = P.iterate(pr_iters)
+    t_pr = time.perf_counter() - t0
+    cpu_ranks = P.ranks()
+    ref64, it64, _ = O.pr_jacobi_fp64_mt(G_d.row_offsets, G_d.col_indices, iters=pr_iters, threads=threads)
+
+    def rel(got):
+        got = got.astype(np.float64)
+        both0 = (got == 0) & (ref64 == 0)
+        return float(np.where(both0, 0.0, np.abs(got - ref64) / np.maximum(np.abs(ref64), 1e-300)).max())
+
+    cc_ok = bool(np.array_equal(gpu_out["cc"], r_cc["props"]))
+    ss_ok = bool(np.array_equal(gpu_out["sssp"], r_ss["props"]))
+    pr_err = rel(gpu_out["pagerank"])
+    parity = {
+        "cc": "bit-exact" if cc_ok else "MISMATCH", "cc_rounds_equal": gpu_out["rounds"][0] == r_cc["stats"]["rounds"],
+        "sssp": "bit-exact" if ss_ok else "MISMATCH",
+        "sssp_rounds_equal": gpu_out["rounds"][1] == r_ss["stats"]["rounds"],
+        "verify_errors": gpu_out["verify"],
+        "pagerank": {"max_rel_err_vs_fp64": pr_err, "bound": 1e-5, "iterations": pr_iters,
+                     "cpu_fp32_kahan_max_rel_err_vs_fp64": rel(cpu_ranks)},
+        "graphs": f"the benchmark's RMAT-{W.G_cc.num_vertices.bit_length() - 1} graphs",
+    }
+    parity["ok"] = bool(cc_ok and ss_ok and parity["cc_rounds_equal"] and parity["sssp_rounds_equal"] and
+                        not any(gpu_out["verify"].values()) and pr_err <= 1e-5)
+    units = W.E_cc + W.E_d + pr_iters * W.E_d
+    cpu = {"value": units / (t_cc + t_ss + t_pr) / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
+           "seconds": t_cc + t_ss + t_pr, "seconds_cc_sssp_pagerank": [t_cc, t_ss, t_pr],
+           "sample": f"one full step on the same graphs: CC + weighted SSSP to convergence (the oracle's "
+                     f"restatement of the reference round protocol, 1C+{NUM_MEMORY}M) and {pr_iters} PageRank "
+                     f"Jacobi iterations (FP32 Kahan, FP64 residual), {threads} host threads; the reference "
+                     f"itself is unbuildable (Galois/MPI absent)"}
+    return parity, cpu
+
+
+def bench_rmat22(g, args, local, barrier, threads):
+    """Config 2 of the workload definition, kept beside the headline: plain
+    CC + weighted SSSP on RMAT-22, 1C+3M, device-driven loops."""
+    import torch
+    a, b, c = RMAT_ABC
+    seed = g.rmat_seed(22, EF)
+    G_cc = g.Graph.rmat(22, EF, a, b, c, seed=seed, symmetrize=True, threads=threads)
+    G_d = g.Graph.rmat(22, EF, a, b, c, seed=seed, weighted=True, threads=threads)
+    cc = g.Context(G_cc, G_cc.partition_edge_balanced(NUM_MEMORY), num_memory=NUM_MEMORY, device=local)
+    ss = g.Context(G_d, G_d.partition_edge_balanced(NUM_MEMORY), num_memory=NUM_MEMORY, device=local)
+    cc.set_algo(g.GRD_CC)
+    ss.set_algo(g.GRD_SSSP_W)
+    try:
+        for _ in range(3):
+            for x in (cc, ss):
+                x.init()
+                x.run()
+        s0, s1 = torch.cuda.ExternalStream(cc.stream()), torch.cuda.ExternalStream(ss.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n = 10
+        barrier()
+        e0.record(s0)
+        for _ in range(n):
+            for x in (cc, ss):
+                x.init()
+                x.run()
+        e1.record(s1)
+        barrier()
+        ms = e0.elapsed_time(e1) / n
+    finally:
+        cc.close()
+        ss.close()
+    return {"workload": "CC (symmetrised) + weighted SSSP to convergence, RMAT-22 ef16, 1C+3M",
+            "value": (G_cc.num_edges + G_d.num_edges) / (ms / 1e3) / 1e9, "unit": "GTEPS", "ms_per_step": ms,
+            "E_cc_symmetrised": G_cc.num_edges, "E_sssp": G_d.num_edges}
+
+
+def bench_policy_offload(g, W, args, barrier, streams):
+    """CC + SSSP of the headline under the other schedules, timed on the same
+    contexts: the shipped learned round policy, and the reference's NDPEngine
+    offload rule; each must leave every result bit-identical."""
+    model = load_policy_model()
+    out = {}
+    W.set_policy(g.GRD_POLICY_FIXED)
+    base_s, base = timed_steps(W, args, barrier, streams, which=(0, 1))
+    base_props = [(c.init(), c.run(), c.read_props())[2] for c in (W.cc, W.ss)]
+    out["fixed"] = {"value": base["units"] / base_s / 1e9, "ms_per_step": base_s * 1e3 / args.steps,
+                    "rounds": base["rounds"][0], "push_rounds_per_step": base["push_rounds"] / args.steps,
+                    "pull_rounds_per_step": base["pull_rounds"] / args.steps}
+    if model is not None:
+        W.set_policy(g.GRD_POLICY_LEARNED, model)
+        s, a = timed_steps(W, args, barrier, streams, which=(0, 1))
+        props = [(c.init(), c.run(), c.read_props())[2] for c in (W.cc, W.ss)]
+        out["learned"] = {"value": a["units"] / s / 1e9, "ms_per_step": s * 1e3 / args.steps,
+                          "rounds": a["rounds"][0], "push_rounds_per_step": a["push_rounds"] / args.steps,
+                          "pull_rounds_per_step": a["pull_rounds"] / args.steps,
+                          "results_bit_identical": all(bool((x == y).all()) for x, y in zip(base_props, props))}
+        out["learned_speedup_vs_fixed"] = out["learned"]["value"] / out["fixed"]["value"]
+    W.set_policy(g.GRD_POLICY_FIXED, offload=g.GRD_OFFLOAD_ENGINE)
+    s, a = timed_steps(W, args, barrier, streams, which=(0, 1))
+    sts = [(c.init(), c.run())[1] for c in (W.cc, W.ss)]
+    props = [c.read_props() for c in (W.cc, W.ss)]
+    W.set_policy(g.GRD_POLICY_FIXED)
+    offload = {"ndp": out["fixed"]["value"], "engine": a["units"] / s / 1e9,
+               "engine_speedup_vs_ndp": (a["units"] / s / 1e9) / out["fixed"]["value"],
+               "no_offload_rounds_per_step": [st["no_offload_rounds"] for st in sts],
+               "results_bit_identical": all(bool((x == y).all()) for x, y in zip(base_props, props))}
+    return {"cc_sssp": out, "model": "grudon_gb300/policy_model.json" if model is not None else None}, offload
+
+
+def bench_ingest(g, W, args, local, barrier, dev) -> dict:
+    """The partition layout of the three contexts built on the host
+    (layout.cpp, all host threads) and on the GPU (grd_ingest: the CSR
+    uploaded from host memory, then proxies, translation slots, the relabelled
+    CSR and, for PageRank, the in-edge view built by kernels)."""
+    graphs = ((W.G_cc, W.p_cc), (W.G_d, W.p_d), (W.G_d, W.p_d))
+    t0 = time.perf_counter()
+    for G, p in graphs[:2]:
+        g.layout_preview(G, p, NUM_MEMORY, 0)
+    host_ms = (time.perf_counter() - t0) * 1e3
+    dctx = [g.Context(G, p, num_memory=NUM_MEMORY, device=local, device_layout=True) for G, p in graphs]
+    try:
+        dctx[2].set_algo(g.GRD_PR_PULL, max_rounds=PR_MAX_ITERS, tolerance=PR_TOL)  # builds its in-edge view
+        best = None
+        for _ in range(3):
+            barrier()
+            t0 = time.perf_counter()
+            nbytes = sum(c.ingest(G, p) for c, (G, p) in zip(dctx, graphs))
+            barrier()
+            dt = (time.perf_counter() - t0) * 1e3
+            best = dt if best is None else min(best, dt)
+    finally:
+        for c in dctx:
+            c.close()
+    return {"host_layout_ms_cc_sssp": host_ms, "device_layout_ms_all_three": best, "device_h2d_bytes": nbytes,
+            "host_threads": os.cpu_count(),
+            "note": "device: CSR upload from pageable host memory + layout build of the three contexts (PageRank's "
+                    "in-edge view included); host: layout.cpp for the CC and SSSP graphs"}
 
 
 def bench_batch(g, args, local) -> dict:
@@ -162,223 +634,6 @@ def bench_batch(g, args, local) -> dict:
                     "pull); timings exclude layout build"}
 
 
-def bench_pagerank(g, args, local, hbm_peak, barrier, ws) -> dict:
-    """PageRank, RMAT-24 (ef16), 1C+3M: Jacobi with FP32 Kahan sums and an FP64
-    residual, until L1 residual / V < 1e-7 or 100 iterations."""
-    threads = max(1, (os.cpu_count() or 1) // ws)
-    a, b, c = RMAT_ABC
-    G = g.Graph.rmat(args.pr_scale, EF, a, b, c, seed=g.rmat_seed(args.pr_scale, EF), threads=threads)
-    part = G.partition_edge_balanced(NUM_MEMORY)
-    ctx = g.Context(G, part, num_memory=NUM_MEMORY, device=local)
-    ctx.set_algo(g.GRD_PR_PULL, max_rounds=100, tolerance=1e-7)
-    ctx.init()
-    ctx.run()  # warm-up
-    ctx.set_profiling(True)
-    reps = 2
-    stats = []
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        ctx.init()
-        stats.append(ctx.run())
-    barrier()
-    dt = (time.perf_counter() - t0) / reps
-    st = stats[-1]
-    it = st["rounds"]
-    pull_ms = sum(s["stage_ms"][1] for s in stats) / reps
-    rounds_ms = sum(s["stage_ms"][4] for s in stats) / reps
-    S = sum(ctx.layout_info(p)[0] + ctx.layout_info(p)[1] for p in range(NUM_MEMORY))
-    # pull edge-map bytes per iteration: in_off + partial writes + dirty bits
-    # over the slots, index + contribution gather per in-edge
-    alg = it * (S * 8 + S / 8 + G.num_edges * 8)
-    ach = alg / (pull_ms / 1e3) / 1e9 if pull_ms else 0.0
-    ranks = ctx.read_ranks()
-    ctx.close()
-    return {
-        "workload": f"PageRank Jacobi (FP32 Kahan, FP64 residual), RMAT-{args.pr_scale} ef{EF}, 1C+{NUM_MEMORY}M, "
-                    "stop at L1 residual/V < 1e-7 or 100 iterations",
-        "num_vertices": G.num_vertices, "num_edges": G.num_edges, "iterations": it,
-        "converged": st["converged"], "last_residual_per_vertex": st["last_residual"],
-        "seconds_per_run": dt, "gteps": G.num_edges * it / dt / 1e9,
-        "ms_per_iteration": rounds_ms / max(it, 1),
-        "roofline": {"bound": "hbm", "kernel": "pull edge-map (k_pull_pr + k_pull_hub)", "achieved": ach,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None},
-        "_graph": G, "_ranks": ranks,
-    }
-
-
-def bench_ingest(g, args, G_cc, G_ss, p_cc, p_ss, local, barrier, dev) -> dict:
-    """Partition layout of both graphs built on the host (layout.cpp, all
-    host threads) and on the GPU (grd_ingest: the CSR uploaded from host
-    memory, then proxies, translation slots and the relabelled CSR built by
-    kernels); then the headline steps end to end from the host CSR: ingest,
-    run both algorithms, read the results."""
-    from grudon_gb300.replicas import job_throughput
-    t0 = time.perf_counter()
-    for G, p in ((G_cc, p_cc), (G_ss, p_ss)):
-        g.layout_preview(G, p, NUM_MEMORY, 0)
-    host_ms = (time.perf_counter() - t0) * 1e3
-    dctx = [g.Context(G, p, num_memory=NUM_MEMORY, device=local, device_layout=True)
-            for G, p in ((G_cc, p_cc), (G_ss, p_ss))]
-    try:
-        best = None
-        for _ in range(3):
-            barrier()
-            t0 = time.perf_counter()
-            nbytes = sum(c.ingest(G, p) for c, G, p in zip(dctx, (G_cc, G_ss), (p_cc, p_ss)))
-            barrier()
-            dt = (time.perf_counter() - t0) * 1e3
-            best = dt if best is None else min(best, dt)
-        for c, a in zip(dctx, (g.GRD_CC, g.GRD_SSSP_W)):
-            c.set_algo(a)
-        E = G_cc.num_edges + G_ss.num_edges
-        for c in dctx:  # warm the loop graphs
-            c.init()
-            c.run()
-        barrier()
-        t0 = time.perf_counter()
-        (cc, ss), graphs = dctx, ((G_cc, p_cc), (G_ss, p_ss))
-        # every step ingests both CSRs and reads both results back; each
-        # ingest overlaps the other graph's queued run
-        cc.ingest(*graphs[0])
-        for k in range(args.steps):
-            cc.init()
-            cc.run(wait=False)
-            ss.ingest(*graphs[1])
-            cc.wait()
-            cc.read_props()
-            ss.init()
-            ss.run(wait=False)
-            if k + 1 < args.steps:
-                cc.ingest(*graphs[0])
-            ss.wait()
-            ss.read_props()
-        barrier()
-        thr, _, _ = job_throughput(args.steps * E, time.perf_counter() - t0, dev)
-    finally:
-        for c in dctx:
-            c.close()
-    return {"host_layout_ms": host_ms, "device_layout_ms": best, "speedup": host_ms / best,
-            "device_h2d_bytes": nbytes, "host_threads": os.cpu_count(),
-            "e2e_from_host_csr": {"value": thr / 1e9, "unit": "GTEPS",
-                                  "note": "per step: CSR upload + device layout build + both runs + results read, "
-                                          "each graph's ingest overlapping the other's run"}}
-
-
-def pr_fp64_check(pr: dict, cpu: dict) -> None:
-    """FP64 Jacobi on the host for the same iteration count (CPU-baseline
-    leg): reports its time and the GPU's max relative error against it."""
-    import numpy as np
-    from oracle import ffi as O
-    G = pr["_graph"]
-    t0 = time.perf_counter()
-    ref, it, _ = O.pr_jacobi_fp64_mt(G.row_offsets, G.col_indices, iters=pr["iterations"])
-    secs = time.perf_counter() - t0
-    got = pr["_ranks"].astype(np.float64)
-    both0 = (got == 0) & (ref == 0)
-    rel = np.where(both0, 0.0, np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300))
-    pr["max_rel_err_vs_fp64"] = float(rel.max())
-    cpu["pagerank_fp64"] = {"seconds": secs, "iterations": it, "threads": os.cpu_count(),
-                            "gteps": G.num_edges * it / secs / 1e9,
-                            "kind": "FP64 Jacobi restatement (oracle), all host threads"}
-
-
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
-
-
-class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 20 ms (the timed region
-    of a default run lasts well under a second)."""
-
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-
-    def __init__(self, index: int):
-        self.index = index
-        self.proc = None
-        self.lines = []
-
-    def start(self):
-        try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "20"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
-        except OSError:
-            self.proc = None
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
-    def stop(self) -> dict:
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        self.t.join(timeout=2)
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                mx.append(float(parts[2]))
-            except ValueError:
-                continue
-            for n, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
-
-
-def load_policy_model():
-    """The shipped learned round-policy model, or None."""
-    from grudon_gb300 import policy as P
-    return P.load_model() if P.MODEL_FILE.exists() else None
-
-
-def make_graphs(scale: int, threads: int):
-    import grudon_gb300 as g
-    a, b, c = RMAT_ABC
-    seed = g.rmat_seed(scale, EF)
-    G_cc = g.Graph.rmat(scale, EF, a, b, c, seed=seed, symmetrize=True, threads=threads)
-    G_ss = g.Graph.rmat(scale, EF, a, b, c, seed=seed, weighted=True, threads=threads)
-    return seed, G_cc, G_ss
-
-
-def cpu_baseline(G_cc, G_ss, p_cc, p_ss, steps: int = 1) -> dict:
-    """The oracle's restated round protocol, all host threads, run() only."""
-    from oracle import ffi as O
-    threads = os.cpu_count() or 1
-    L_cc = O.Layout(G_cc.row_offsets, G_cc.col_indices, mirror=p_cc, num_memory=NUM_MEMORY)
-    L_ss = O.Layout(G_ss.row_offsets, G_ss.col_indices, G_ss.weights, mirror=p_ss, num_memory=NUM_MEMORY)
-    t_total = 0.0
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        L_cc.run(O.ORC_CC, threads=threads)
-        L_ss.run(O.ORC_SSSP_W, threads=threads)
-        t_total += time.perf_counter() - t0
-    E = G_cc.num_edges + G_ss.num_edges
-    return {"value": steps * E / t_total / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
-            "seconds": t_total,
-            "sample": f"{steps} full step(s): CC + weighted SSSP to convergence on the same RMAT-{SCALE} graphs, "
-                      f"1C+{NUM_MEMORY}M, oracle restatement of the reference round protocol (reference "
-                      f"unbuildable: Galois/MPI absent), {threads} host threads"}
-
-
 def bench_reference_cpu_case(g, local) -> dict:
     """The reference's own CPU-runnable case: plain (delta-push) PageRank,
     damping 0.85, 20 iterations, seeded RMAT-16 ef16, 1 compute + 1 memory
@@ -414,51 +669,30 @@ def bench_reference_cpu_case(g, local) -> dict:
             "max_abs_rank_diff": float(np.abs(ranks - ref["ranks"]).max())}
 
 
-def run_reference(args):
-    ws, rank, _ = dist_env()
-    if rank != 0:
-        return
-    seed, G_cc, G_ss = make_graphs(args.scale, 0)
-    p_cc = G_cc.partition_edge_balanced(NUM_MEMORY)
-    p_ss = G_ss.partition_edge_balanced(NUM_MEMORY)
-    from oracle import ffi as O
-    threads = os.cpu_count() or 1
-    L_cc = O.Layout(G_cc.row_offsets, G_cc.col_indices, mirror=p_cc, num_memory=NUM_MEMORY)
-    L_ss = O.Layout(G_ss.row_offsets, G_ss.col_indices, G_ss.weights, mirror=p_ss, num_memory=NUM_MEMORY)
-    for _ in range(args.warmup):
-        L_cc.run(O.ORC_CC, threads=threads)
-        L_ss.run(O.ORC_SSSP_W, threads=threads)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        L_cc.run(O.ORC_CC, threads=threads)
-        L_ss.run(O.ORC_SSSP_W, threads=threads)
-    dt = time.perf_counter() - t0
-    E = G_cc.num_edges + G_ss.num_edges
-    value = args.steps * E / dt / 1e9
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": workload_config(args.scale, seed, G_cc, G_ss),
-        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
-                         "sample": f"each step: CC + weighted SSSP to convergence (full workload), "
-                                   f"{threads} host threads; reference itself unbuildable (Galois/MPI absent)"},
-        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
+def kernel_run(g, args, local, rank, threads):
+    """Host-driven steps only (plain launches), for per-kernel profilers."""
+    W = Workload(g, args.scale, threads, local)
+    try:
+        W.set_policy(g.GRD_POLICY_FIXED)
+        for _ in range(args.warmup + args.steps):
+            sts = [(c.init(), c.run(host_loop=True))[1] for c in W.ctxs]
+        if rank == 0:
+            print(json.dumps({"kernel_run": True, "scale": args.scale, "rounds": [st["rounds"] for st in sts],
+                              "launches_per_step": sum(st["kernel_launches"] for st in sts)}), flush=True)
+    finally:
+        W.close()
 
 
-def workload_config(scale, seed, G_cc, G_ss) -> dict:
-    return {
-        "workload": f"CC (symmetrised) + weighted SSSP (w in [1,255], source 0) to convergence, RMAT-{scale} "
-                    f"ef{EF} a/b/c/d .57/.19/.19/.05, 1 compute + {NUM_MEMORY} memory partitions, bitvector or list "
-                    f"sync and push or pull chosen per round",
-        "scale": scale, "edge_factor": EF, "seed": seed, "num_vertices": G_cc.num_vertices,
-        "E_cc_symmetrised": G_cc.num_edges, "E_sssp": G_ss.num_edges,
-        "partitions": f"1C+{NUM_MEMORY}M edge-balanced contiguous",
-        "l2": "inputs larger than L2 (CSR indices 0.27-0.5 GB > 129 MB), no flush",
-        "streams": "CC then SSSP within a step, each on its own ctx stream",
-    }
+def kernel_run_pr(g, args, local, rank, threads):
+    a, b, c = RMAT_ABC
+    G = g.Graph.rmat(args.scale, EF, a, b, c, seed=g.rmat_seed(args.scale, EF), threads=threads)
+    with g.Context(G, G.partition_edge_balanced(NUM_MEMORY), num_memory=NUM_MEMORY, device=local) as ctx:
+        ctx.set_algo(g.GRD_PR_PULL, max_rounds=args.warmup + args.steps, tolerance=0.0)
+        ctx.init()
+        st = ctx.run(host_loop=True)
+    if rank == 0:
+        print(json.dumps({"kernel_run_pr": True, "scale": args.scale, "iterations": st["rounds"],
+                          "edges": G.num_edges}), flush=True)
 
 
 def main():
@@ -474,303 +708,153 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import grudon_gb300 as g
+    from grudon_gb300.replicas import job_throughput
 
     threads = max(1, (os.cpu_count() or 1) // ws)
     if args.kernel_run_pr:
-        a, b, c = RMAT_ABC
-        G = g.Graph.rmat(args.pr_scale, EF, a, b, c, seed=g.rmat_seed(args.pr_scale, EF), threads=threads)
-        with g.Context(G, G.partition_edge_balanced(NUM_MEMORY), num_memory=NUM_MEMORY, device=local) as ctx:
-            ctx.set_algo(g.GRD_PR_PULL, max_rounds=args.warmup + args.steps, tolerance=0.0)
-            ctx.init()
-            st = ctx.run()
-        if rank == 0:
-            print(json.dumps({"kernel_run_pr": True, "scale": args.pr_scale, "iterations": st["rounds"],
-                              "edges": G.num_edges}), flush=True)
+        kernel_run_pr(g, args, local, rank, threads)
         return
-    seed, G_cc, G_ss = make_graphs(args.scale, threads)
-    p_cc = G_cc.partition_edge_balanced(NUM_MEMORY)
-    p_ss = G_ss.partition_edge_balanced(NUM_MEMORY)
-    if args.ingest_run:
-        for G, p in ((G_cc, p_cc), (G_ss, p_ss)):
-            with g.Context(G, p, num_memory=NUM_MEMORY, device=local, device_layout=True) as c:
-                for _ in range(args.warmup + args.steps):
-                    c.ingest(G, p)
-        if rank == 0:
-            print(json.dumps({"ingest_run": True, "scale": args.scale,
-                              "builds_per_graph": 1 + args.warmup + args.steps}), flush=True)
+    if args.kernel_run:
+        kernel_run(g, args, local, rank, threads)
         return
-    ctx_cc = g.Context(G_cc, p_cc, num_memory=NUM_MEMORY, device=local)
-    ctx_ss = g.Context(G_ss, p_ss, num_memory=NUM_MEMORY, device=local)
-    model = load_policy_model()
-
-    def set_policy(policy, offload=g.GRD_OFFLOAD_NDP):
-        for c, a in ((ctx_cc, g.GRD_CC), (ctx_ss, g.GRD_SSSP_W)):
-            c.set_algo(a, policy=policy, offload=offload)
-            c.set_policy(model if policy == g.GRD_POLICY_LEARNED else None)
-
-    # The headline runs the library's default schedule, the fixed threshold
-    # rule (push only: no in-edge view), unless --policy learned.  The shipped
-    # learned policy, when its model file is present, is timed next to it.
-    policy = g.GRD_POLICY_LEARNED if (args.policy == "learned" and model is not None) else g.GRD_POLICY_FIXED
-    set_policy(g.GRD_POLICY_FIXED)
-    E = G_cc.num_edges + G_ss.num_edges
-    slots = {id(c): sum(sum(c.layout_info(p)[:2]) for p in range(NUM_MEMORY)) for c in (ctx_cc, ctx_ss)}
-
-    def step(host_loop=False):
-        """Both algorithms to convergence, one after the other (run
-        concurrently on their two streams they were slower: their full-wave
-        push kernels compete for the SMs and L2)."""
-        out = []
-        for c in (ctx_cc, ctx_ss):
-            c.init()
-            out.append(c.run(host_loop=host_loop))
-        return out
 
     def barrier():
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    if args.kernel_run:
-        set_policy(policy)
-        for _ in range(args.warmup + args.steps):
-            sts = step(host_loop=True)
-        barrier()
-        if rank == 0:
-            print(json.dumps({"kernel_run": True, "workload": workload_config(args.scale, seed, G_cc, G_ss)["workload"],
-                              "policy": "learned" if policy == g.GRD_POLICY_LEARNED else "fixed",
-                              "rounds": [st["rounds"] for st in sts],
-                              "launches_per_step": sum(st["kernel_launches"] for st in sts)}), flush=True)
-        ctx_cc.close()
-        ctx_ss.close()
-        return
-
-    s_cc = torch.cuda.ExternalStream(ctx_cc.stream())
-    s_ss = torch.cuda.ExternalStream(ctx_ss.stream())
-    from grudon_gb300.replicas import job_throughput
     dev = torch.device("cuda", local) if ws > 1 else None
-
-    def timed():
-        """W warm-up steps, then K timed steps: every step runs both
-        algorithms to convergence, each as one device-driven CUDA-graph
-        launch; CUDA events on the ctx streams."""
-        for _ in range(args.warmup):
-            step()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        barrier()
-        ev0.record(s_cc)
-        agg = {"edges": 0, "launches": 0, "rounds": [], "device_loop": [], "push_rounds": 0, "pull_rounds": 0}
-        for _ in range(args.steps):
-            for st in step():
-                agg["edges"] += st["edges_scanned"]
-                agg["launches"] += st["kernel_launches"]
-                agg["rounds"].append(st["rounds"])
-                agg["device_loop"].append(st["device_loop"])
-                agg["push_rounds"] += st["push_rounds"]
-                agg["pull_rounds"] += st["pull_rounds"]
-        ev1.record(s_ss)
-        barrier()
-        thr, secs, _ = job_throughput(args.steps * E, ev0.elapsed_time(ev1) / 1e3, dev)
-        return thr / 1e9, secs * 1e3, agg
-
-    def summary(v, ms, a):
-        return {"value": v, "ms_per_step": ms / args.steps, "rounds_per_step": a["rounds"][:2],
-                "push_rounds_per_step": a["push_rounds"] / args.steps,
-                "pull_rounds_per_step": a["pull_rounds"] / args.steps, "gpu_launches": a["launches"]}
+    peak, peak_src = hbm_peak()
+    W = Workload(g, args.scale, threads, local)
+    model = load_policy_model()
+    learned = args.policy == "learned" and model is not None
+    W.set_policy(g.GRD_POLICY_LEARNED if learned else g.GRD_POLICY_FIXED, model)
+    streams = [torch.cuda.ExternalStream(c.stream()) for c in W.ctxs]
 
     clocks = ClockSampler(local)
     clocks.start()
-    runs = {}
-    if policy == g.GRD_POLICY_LEARNED:  # the plain method first (before the in-edge view exists)
-        runs["fixed"] = summary(*timed())
-        set_policy(policy)
-    value, dt_ms, agg = timed()
+    secs, agg = timed_steps(W, args, barrier, streams)
     clk = clocks.stop()
-    runs["learned" if policy == g.GRD_POLICY_LEARNED else "fixed"] = summary(value, dt_ms, agg)
+    thr, secs_max, _ = job_throughput(agg["units"], secs, dev)
+    value = thr / 1e9
 
-    # Stage timing for the roofline: the same steps driven from the host with
-    # CUDA events around every stage of every round (same kernels, same
-    # per-round choices).
-    for c in (ctx_cc, ctx_ss):
-        c.set_profiling(True)
-    prof = {"edge_map_ms": 0.0, "fwd_ms": 0.0, "bwd_ms": 0.0, "update_ms": 0.0, "rounds_ms": 0.0, "alg_bytes": 0.0,
-            "push_rounds": 0, "pull_rounds": 0, "lbs_ms": 0.0, "lbs_bytes": 0.0, "lbs_launches": 0,
-            "lbs_edges": 0}
-    for _ in range(args.steps):
-        for st, c, weighted, Eg in zip(step(host_loop=True), (ctx_cc, ctx_ss), (False, True),
-                                        (G_cc.num_edges, G_ss.num_edges)):
-            for i, k in enumerate(("fwd_ms", "edge_map_ms", "bwd_ms", "update_ms", "rounds_ms")):
-                prof[k] += st["stage_ms"][i]
-            wb = 4 if weighted else 0
-            push_edges = st["edges_scanned"] - st["pull_rounds"] * Eg
-            S = slots[id(c)]
-            prof["alg_bytes"] += (st["push_actives"] * 12 + push_edges * (12 + wb) +
-                                  st["pull_rounds"] * (Eg * (8 + wb) + S * 8 + S / 8))
-            prof["push_rounds"] += st["push_rounds"]
-            prof["pull_rounds"] += st["pull_rounds"]
-            # the load-balanced push kernel alone, by the push round's
-            # algorithmic bytes: DP/RB/SV of each active (12), then per edge
-            # its column index (4), weight (4, weighted) and the destination's
-            # read-modify-write (8)
-            prof["lbs_ms"] += st["lbs_ms"]
-            prof["lbs_launches"] += st["lbs_launches"]
-            prof["lbs_edges"] += st["lbs_edges"]
-            prof["lbs_bytes"] += st["lbs_actives"] * 12 + st["lbs_edges"] * (12 + wb)
-    for c in (ctx_cc, ctx_ss):
-        c.set_profiling(False)
+    prof = profile_pass(W)
+    roofline = roofline_of(W, prof, agg["ctx_ms"][2], peak, peak_src)
+    gpu_out = {"cc": W.cc.read_props(), "sssp": W.ss.read_props(), "pagerank": W.pr.read_ranks(),
+               "rounds": agg["rounds"][-1]}
+    gpu_out["verify"] = {"cc": W.cc.verify()["errors"], "sssp": W.ss.verify()["errors"]}
+    e2e = e2e_pass(W, args, barrier, streams, dev)
 
-    # Host->device bandwidth of the layout upload alone (both graphs, best of 3).
-    up_s = []
-    for _ in range(3):
-        barrier()
-        t0 = time.perf_counter()
-        up_bytes = sum(c.upload() for c in (ctx_cc, ctx_ss))
-        barrier()
-        up_s.append(time.perf_counter() - t0)
-    upload_gbs = up_bytes / min(up_s) / 1e9
-
-    # End to end through the C ABI with host buffers.  Results are read into
-    # pinned host arrays allocated once, as a serving loop keeps them.
-    res_cc = torch.empty(G_cc.num_vertices, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
-    res_ss = torch.empty(G_ss.num_vertices, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
-    barrier()
-    h2d = 0
-    t0 = time.perf_counter()
-    # Every step copies both graphs' layouts and reads both results back.  The
-    # copies are pipelined with the runs: CC's copy has the link to itself,
-    # SSSP's follows it and overlaps CC's run, and once CC's result is read
-    # the next step's CC copy overlaps SSSP's run.
-    # Runs and reads are queued (run(wait=False), read_props(wait=False)) and
-    # ordered by stream events: CC's run waits for SSSP's previous run, SSSP's
-    # for CC's, so the two never share the GPU, and the host waits only on
-    # work already finished, queuing each run before the GPU reaches it.
-    up_done, cc_done, ss_done = torch.cuda.Event(), torch.cuda.Event(), torch.cuda.Event()
-    h2d += ctx_cc.upload()
-    for k in range(args.steps):
-        up_done.record(s_cc)
-        s_ss.wait_event(up_done)
-        h2d += ctx_ss.upload()
-        ctx_cc.wait()  # CC's previous run; its stream then holds only this step's copy
-        if k:
-            s_cc.wait_event(ss_done)
-        ctx_cc.init()
-        ctx_cc.run(wait=False)
-        ctx_cc.read_props(out=res_cc, wait=False)
-        cc_done.record(s_cc)
-        if k + 1 < args.steps:
-            h2d += ctx_cc.upload()
-        ctx_ss.wait()
-        s_ss.wait_event(cc_done)
-        ctx_ss.init()
-        ctx_ss.run(wait=False)
-        ctx_ss.read_props(out=res_ss, wait=False)
-        ss_done.record(s_ss)
-    ctx_cc.wait()
-    ctx_ss.wait()
-    barrier()
-    e2e_thr, _, _ = job_throughput(args.steps * E, time.perf_counter() - t0, dev)
-    # the queued reads delivered the final results (checked outside the timed region)
-    if not (np.array_equal(res_cc, ctx_cc.read_props()) and np.array_equal(res_ss, ctx_ss.read_props())):
-        raise RuntimeError("queued result reads differ from a blocking read")
-    e2e = {"value": e2e_thr / 1e9, "unit": "GTEPS",
-           "h2d_bytes_per_step": h2d // args.steps,
-           "d2h_bytes_per_step": 4 * (G_cc.num_vertices + G_ss.num_vertices),
-           "upload_alone_gbs": upload_gbs}
-    ingest = bench_ingest(g, args, G_cc, G_ss, p_cc, p_ss, local, barrier, dev)
-
-    # The other schedule on the same contexts; the learned one must leave
-    # every result bit-identical.
-    results_identical = None
-    if model is not None:
-        if "learned" not in runs:
-            set_policy(g.GRD_POLICY_LEARNED)
-            runs["learned"] = summary(*timed())
-        outs = []
-        for pol in (g.GRD_POLICY_FIXED, g.GRD_POLICY_LEARNED):
-            set_policy(pol)
-            outs.append([(c.init(), c.run(), c.read_props())[2] for c in (ctx_cc, ctx_ss)])
-        results_identical = all(bool((a == b).all()) for a, b in zip(*outs))
-
-    # The reference's offload engine (NDPEngine: NO_OFFLOAD rounds, the
-    # compute partition pushing over the shipped adjacency, when the frontier
-    # holds at most V/20 vertices) against the all-NDP_OFFLOAD schedule it
-    # hard-codes, both with the fixed rule, timed back to back on the same
-    # contexts; results must be bit-identical.
-    set_policy(g.GRD_POLICY_FIXED)
-    ndp_run = summary(*timed())
-    base_props = [(c.init(), c.run(), c.read_props())[2] for c in (ctx_cc, ctx_ss)]
-    set_policy(g.GRD_POLICY_FIXED, g.GRD_OFFLOAD_ENGINE)
-    eng_run = summary(*timed())
-    sts = [(c.init(), c.run())[1] for c in (ctx_cc, ctx_ss)]
-    off_props = [c.read_props() for c in (ctx_cc, ctx_ss)]
-    offload = {"ndp": ndp_run,
-               "engine": eng_run | {"no_offload_rounds_per_step": [st["no_offload_rounds"] for st in sts]},
-               "engine_speedup_vs_ndp": eng_run["value"] / ndp_run["value"],
-               "results_bit_identical": all(bool((a == b).all()) for a, b in zip(base_props, off_props))}
-    set_policy(policy)
-
-    peaks = {}
-    pk = ROOT / "MEASURED_PEAKS.json"
-    if pk.exists():
-        peaks = json.loads(pk.read_text())
-    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    stage_ach = prof["alg_bytes"] / (prof["edge_map_ms"] / 1e3) / 1e9 if prof["edge_map_ms"] > 0 else 0.0
-    nl = max(prof["lbs_launches"], 1)
-    lbs_ach = prof["lbs_bytes"] / (prof["lbs_ms"] / 1e3) / 1e9 if prof["lbs_ms"] > 0 else 0.0
-    roofline = {"bound": "hbm", "kernel": "k_push_lbs (load-balanced push edge-map)",
-                "achieved": lbs_ach, "peak": hbm_peak, "unit": "GB/s", "frac": lbs_ach / hbm_peak,
-                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                # DRAM bytes per edge of the kernel in its ncu capture, times
-                # this run's average edges per launch
-                "traffic": DRAM_BYTES_PER_PUSH_EDGE * prof["lbs_edges"] / nl,
-                "alg_bytes_per_launch": prof["lbs_bytes"] / nl, "avg_launch_ms": prof["lbs_ms"] / nl,
-                "launches": prof["lbs_launches"],
-                "edge_map_stage": {"achieved": stage_ach, "frac": stage_ach / hbm_peak,
-                                   "kernels": "k_deg_* (list rounds), k_push_lbs, k_hub_push, k_diff_dirty (push) or k_pull* (pull)",
-                                   "share_of_rounds": prof["edge_map_ms"] / prof["rounds_ms"]
-                                   if prof["rounds_ms"] else None},
-                "push_rounds_per_step": prof["push_rounds"] / args.steps,
-                "pull_rounds_per_step": prof["pull_rounds"] / args.steps,
-                "stage_ms_per_step": {k: prof[k] / args.steps for k in
-                                      ("fwd_ms", "edge_map_ms", "bwd_ms", "update_ms", "rounds_ms")}}
-    pr = None
-    if not args.no_pagerank:
-        pr = bench_pagerank(g, args, local, hbm_peak, barrier, ws)
-    batch = bench_batch(g, args, local) if (args.batch or (ws == 1 and not args.no_batch)) else None
+    extras = {}
+    if not args.no_extras:
+        extras["policy"], extras["offload"] = bench_policy_offload(g, W, args, barrier, streams)
+        extras["ingest"] = bench_ingest(g, W, args, local, barrier, dev)
+    line = {
+        "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs_max * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32", "data": "synthetic",
+        "config": workload_config(args.scale, W.seed, W.V, W.E_cc, W.E_d,
+                                  csr_checksum(W.G_cc.row_offsets, W.G_cc.col_indices),
+                                  csr_checksum(W.G_d.row_offsets, W.G_d.col_indices, W.G_d.weights), ws),
+        "e2e": e2e, "gpu_launches": agg["launches"], "roofline": roofline, "clocks": clk,
+        "per_algorithm": {
+            name: {"ms": agg["ctx_ms"][i], "gteps": units / (agg["ctx_ms"][i] / 1e3) / 1e9}
+            for i, (name, units) in enumerate((("cc", W.E_cc), ("sssp", W.E_d),
+                                               ("pagerank", W.E_d * agg["pr_iterations"][-1])))},
+        "rounds_per_step": agg["rounds"][-1], "pagerank_iterations": agg["pr_iterations"][-1],
+        "device_loop": agg["device_loop"], "policy_headline": "learned" if learned else "fixed",
+        "edges_scanned_gteps": ws * agg["edges"] / secs_max / 1e9,
+    }
+    failed = False
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        parity, cpu = parity_and_cpu(W, gpu_out, agg["pr_iterations"][-1], os.cpu_count() or 1)
+        line["parity"] = parity
+        line["cpu_baseline"] = cpu
+        failed = not parity["ok"]
+    W.close()
+    if not args.no_extras:
+        extras["config2_rmat22"] = bench_rmat22(g, args, local, barrier, threads)
+        if rank == 0 and ws == 1:
+            extras["reference_cpu_case"] = bench_reference_cpu_case(g, local)
+        if args.batch or (ws == 1 and not args.no_batch):
+            extras["batch"] = bench_batch(g, args, local)
+    line.update(extras)
     if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dt_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": workload_config(args.scale, seed, G_cc, G_ss) | {"parallelism": f"replicas x{ws}"},
-            "e2e": e2e, "gpu_launches": agg["launches"], "roofline": roofline, "clocks": clk,
-            "rounds_per_step": agg["rounds"][:2], "device_loop": all(agg["device_loop"]),
-            "edges_scanned_gteps": ws * agg["edges"] / (dt_ms / 1e3) / 1e9,
-            "policy": {"headline": "learned" if policy == g.GRD_POLICY_LEARNED else "fixed",
-                       "model": "grudon_gb300/policy_model.json" if model is not None else None,
-                       **runs,
-                       "learned_speedup_vs_fixed": (runs["learned"]["value"] / runs["fixed"]["value"])
-                       if "learned" in runs else None,
-                       "results_bit_identical": results_identical},
-            "offload": offload,
-        }
-        if ws == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(G_cc, G_ss, p_cc, p_ss)
-            line["reference_cpu_case"] = bench_reference_cpu_case(g, local)
-            if pr is not None:
-                pr_fp64_check(pr, line["cpu_baseline"])
-        if pr is not None:
-            pr.pop("_graph", None)
-            pr.pop("_ranks", None)
-            line["pagerank_rmat24"] = pr
-        if batch is not None:
-            line["batch"] = batch
-        line["ingest"] = ingest
         print(json.dumps(line), flush=True)
-    ctx_cc.close()
-    ctx_ss.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+    if failed:
+        sys.exit("parity check failed on the benchmark graphs")
+
+
+# --------------------------------------------------------- reference arm --
+def run_reference(args):
+    """The reference algorithm on the host cores (the oracle's restatement,
+    all threads), on graphs built by the oracle's generator (no product
+    library is loaded).  Each step is a bounded sample: the steps take turns
+    over CC to convergence, SSSP to convergence and 4 PageRank iterations;
+    the value is the full step's units over the full step's estimated time
+    (mean CC time + mean SSSP time + iterations x mean iteration time)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import ffi as O
+    threads = os.cpu_count() or 1
+    a, b, c = RMAT_ABC
+    seed = O.rmat_seed(args.scale, EF)
+    ro_s, col_s, _ = O.gen_rmat(args.scale, EF, a, b, c, seed, symmetrize=True, threads=threads)
+    ro_d, col_d, w_d = O.gen_rmat(args.scale, EF, a, b, c, seed, weighted=True, threads=threads)
+    p_s, p_d = O.partition_edge_balanced(ro_s, NUM_MEMORY), O.partition_edge_balanced(ro_d, NUM_MEMORY)
+    V, E_cc, E_d = len(ro_s) - 1, len(col_s), len(col_d)
+    config = workload_config(args.scale, seed, V, E_cc, E_d, csr_checksum(ro_s, col_s),
+                             csr_checksum(ro_d, col_d, w_d), ws)
+    L_cc = O.Layout(ro_s, col_s, mirror=p_s, num_memory=NUM_MEMORY)
+    L_ss = O.Layout(ro_d, col_d, w_d, mirror=p_d, num_memory=NUM_MEMORY)
+    P = O.PrJacobi(ro_d, col_d, threads=threads)
+    # the PageRank step's iteration count under its own stop rule
+    P.init()
+    iters, _ = P.iterate(PR_MAX_ITERS, PR_TOL)
+    P.init()
+    times = {0: [], 1: [], 2: []}
+    sample_iters = 4
+
+    def sample(k):
+        kind = k % 3
+        t0 = time.perf_counter()
+        if kind == 0:
+            L_cc.run(O.ORC_CC, threads=threads)
+        elif kind == 1:
+            L_ss.run(O.ORC_SSSP_W, threads=threads)
+        else:
+            P.iterate(sample_iters)
+        return kind, time.perf_counter() - t0
+
+    for k in range(args.warmup):
+        sample(k)
+    for k in range(args.steps):
+        kind, dt = sample(k)
+        times[kind].append(dt / (sample_iters if kind == 2 else 1))
+    for kind in (0, 1, 2):  # every part sampled at least once
+        if not times[kind]:
+            times[kind].append(sample(kind)[1] / (sample_iters if kind == 2 else 1))
+    step_s = statistics.mean(times[0]) + statistics.mean(times[1]) + iters * statistics.mean(times[2])
+    units = E_cc + E_d + iters * E_d
+    value = units / step_s / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32", "data": "synthetic", "config": config,
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
+                         "sample": f"steps take turns over CC to convergence, weighted SSSP to convergence and "
+                                   f"{sample_iters} PageRank iterations (oracle restatements, {threads} host "
+                                   f"threads); value = full step units / (mean CC + mean SSSP + {iters} x mean "
+                                   f"iteration time); samples per part: {[len(times[k]) for k in (0, 1, 2)]}; "
+                                   f"reference itself unbuildable (Galois/MPI absent)"},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "pagerank_iterations": iters,
+        "seconds_cc_sssp_iteration": [statistics.mean(times[k]) for k in (0, 1, 2)],
+    }
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -406,12 +406,16 @@ class Context:
             raise ValueError("read_props(wait=False) needs the caller's out array")
         return self._read(self._lib.grd_read_props_async, dt, self.num_vertices, out)
 
-    def read_ranks(self, out=None) -> np.ndarray:
+    def read_ranks(self, out=None, wait: bool = True) -> np.ndarray:
+        """PageRank values; wait=False queues the copy like read_props."""
         if out is None:
+            if not wait:
+                raise ValueError("read_ranks(wait=False) needs the caller's out array")
             out = np.empty(self.num_vertices, dtype=np.float32)
         elif out.dtype != np.float32 or out.size < self.num_vertices or not out.flags["C_CONTIGUOUS"]:
             raise ValueError(f"out must be a contiguous float32 array of at least {self.num_vertices} elements")
-        self._check(self._lib.grd_read_ranks(self._ctx, out.ctypes.data_as(C.c_void_p), out.size))
+        fn = self._lib.grd_read_ranks if wait else self._lib.grd_read_ranks_async
+        self._check(fn(self._ctx, out.ctypes.data_as(C.c_void_p), out.size))
         return out
 
     def read_updates(self, out=None) -> np.ndarray:

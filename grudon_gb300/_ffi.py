@@ -64,7 +64,7 @@ class grd_stats(C.Structure):
                 ("actives_total", C.c_uint64), ("kernel_launches", C.c_uint64), ("stage_ms", C.c_double * 5),
                 ("device_loop", C.c_uint32), ("push_actives", C.c_uint64), ("lbs_ms", C.c_double),
                 ("lbs_edges", C.c_uint64), ("lbs_actives", C.c_uint64), ("lbs_launches", C.c_uint64),
-                ("no_offload_rounds", C.c_uint32)]
+                ("no_offload_rounds", C.c_uint32), ("pull_ms", C.c_double), ("pull_launches", C.c_uint64)]
 
 
 GRD_POLICY_FIXED, GRD_POLICY_LEARNED = 0, 1
@@ -148,6 +148,7 @@ SIGNATURES = {
     "grd_read_props": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_props_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_ranks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "grd_read_ranks_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_updates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_frontier": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_layout_info": (C.c_int, [C.c_void_p, C.c_uint32, u32p, u32p, u64p]),

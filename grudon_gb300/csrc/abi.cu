@@ -1258,16 +1258,32 @@ int grd_read_props(grd_ctx* ctx, void* host, size_t bytes) {
   return read_dev(ctx, host, ctx->st.prop, bytes, sizeof(uint32_t) * ctx->L.V);
 }
 
-int grd_read_props_async(grd_ctx* ctx, void* host, size_t bytes) {
+// A queued copy of a resident vertex array (props or ranks): refused while
+// the layout is incomplete (a failed grd_ingest may have left it half
+// rewritten).
+static int read_dev_async(grd_ctx* ctx, void* host, const void* dev, size_t bytes, size_t need) {
   if (!ctx || !host) return GRD_E_INVALID;
-  const size_t need = sizeof(uint32_t) * ctx->L.V;
+  if (!ctx->layout_valid) {
+    ctx->err = "the layout was left incomplete by a failed grd_ingest: ingest a matching graph first";
+    return GRD_E_INVALID;
+  }
   if (bytes < need) {
     ctx->err = "host buffer too small: need " + std::to_string(need) + " bytes";
     return GRD_E_INVALID;
   }
   CK(cudaSetDevice(ctx->device));
-  CK(cudaMemcpyAsync(host, ctx->st.prop, need, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(host, dev, need, cudaMemcpyDeviceToHost, ctx->stream));
   return GRD_OK;
+}
+
+int grd_read_props_async(grd_ctx* ctx, void* host, size_t bytes) {
+  if (!ctx) return GRD_E_INVALID;
+  return read_dev_async(ctx, host, ctx->st.prop, bytes, sizeof(uint32_t) * ctx->L.V);
+}
+
+int grd_read_ranks_async(grd_ctx* ctx, float* host, size_t count) {
+  if (!ctx) return GRD_E_INVALID;
+  return read_dev_async(ctx, host, ctx->st.ranks, count * sizeof(float), sizeof(float) * ctx->L.V);
 }
 
 int grd_read_ranks(grd_ctx* ctx, float* host, size_t count) {

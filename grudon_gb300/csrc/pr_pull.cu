@@ -786,10 +786,13 @@ int enqueue_fwd(grd_ctx* ctx) {
   return GRD_OK;
 }
 
-int enqueue_edge_map(grd_ctx* ctx) {
+// timed: CUDA events around the pull kernel (profiled host-driven runs).
+int enqueue_edge_map(grd_ctx* ctx, bool timed = false) {
   if (ctx->pr.T) {
     TRY(set_pull_smem(ctx));
+    if (timed) CK(cudaEventRecord(ctx->ev[5], ctx->stream));
     k_pr_pull<<<ctx->num_sms, PR_THREADS, pull_smem(ctx), ctx->stream>>>(pr_args(ctx));
+    if (timed) CK(cudaEventRecord(ctx->ev[6], ctx->stream));
     const uint64_t groups = (ctx->pr.T + 31) / 32;
     k_pr_fix<<<(uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((groups + 7) / 8, (uint64_t)ctx->num_sms * 8)),
                256, 0, ctx->stream>>>(pr_args(ctx));
@@ -884,13 +887,22 @@ int grd_pull_run(grd_ctx* ctx) {
   while (ctx->stats.rounds < ctx->params.max_rounds) {
     grd_prof_mark(ctx, 0);
     grd_prof_mark(ctx, 1);
-    TRY(enqueue_edge_map(ctx));
+    const bool timed = ctx->profiling && ctx->pr.T != 0;
+    TRY(enqueue_edge_map(ctx, timed));
     grd_prof_mark(ctx, 2);
     grd_prof_mark(ctx, 3);
     TRY(enqueue_update(ctx, 0, 0));
     grd_prof_mark(ctx, 4);
     TRY(read_round(ctx));
     grd_prof_collect(ctx);
+    if (timed) {
+      float ms = 0.0f;
+      if (cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]) == cudaSuccess) {
+        ctx->stats.pull_ms += ms;
+        ctx->stats.pull_launches += 1;
+      }
+      (void)cudaGetLastError();
+    }
     ctx->stats.rounds++;
     if (ctx->stats.last_residual < ctx->params.tolerance) {
       ctx->stats.converged = 1;

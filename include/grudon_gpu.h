@@ -164,6 +164,10 @@ typedef struct grd_stats {
   uint64_t lbs_edges, lbs_actives, lbs_launches;
   uint32_t no_offload_rounds; /* rounds run NO_OFFLOAD (counted in
                                  push_rounds too)                          */
+  /* With profiling, host-driven PR_PULL iterations: the edge-balanced pull
+   * kernel alone (CUDA events around each launch) and its launches. */
+  double pull_ms;
+  uint64_t pull_launches;
 } grd_stats;
 
 typedef struct grd_ctx grd_ctx;
@@ -305,6 +309,8 @@ int grd_read_props(grd_ctx* ctx, void* host, size_t bytes);
 int grd_read_props_async(grd_ctx* ctx, void* host, size_t bytes);
 /* PageRank values (pr_vals for PR_DELTA, ranks for PR_PULL), float[V]. */
 int grd_read_ranks(grd_ctx* ctx, float* host, size_t count);
+/* The ranks copy queued like grd_read_props_async (same rules). */
+int grd_read_ranks_async(grd_ctx* ctx, float* host, size_t count);
 /* Compute-side vertex_updates, gid order. */
 int grd_read_updates(grd_ctx* ctx, void* host, size_t bytes);
 /* Current compute frontier bitmap, ceil(V/32) uint32 words. */

@@ -67,6 +67,31 @@ def lib() -> C.CDLL:
         L.orc_pr_jacobi_fp64_mt.restype = C.c_uint32
         L.orc_pr_jacobi_fp64_mt.argtypes = [C.c_uint32, u64p, u32p, C.c_double, C.c_uint32, C.c_double, C.c_int,
                                             C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_rmat_seed.restype = C.c_uint64
+        L.orc_rmat_seed.argtypes = [C.c_uint32, C.c_uint32]
+        L.orc_gen_rmat.restype = C.c_void_p
+        L.orc_gen_rmat.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int,
+                                   C.c_int, C.c_int]
+        L.orc_graph_num_vertices.restype = C.c_uint32
+        L.orc_graph_num_vertices.argtypes = [C.c_void_p]
+        L.orc_graph_num_edges.restype = C.c_uint64
+        L.orc_graph_num_edges.argtypes = [C.c_void_p]
+        L.orc_graph_copy.restype = None
+        L.orc_graph_copy.argtypes = [C.c_void_p, u64p, u32p, u32p]
+        L.orc_graph_free.restype = None
+        L.orc_graph_free.argtypes = [C.c_void_p]
+        L.orc_prj_create.restype = C.c_void_p
+        L.orc_prj_create.argtypes = [C.c_uint32, u64p, u32p, C.c_double, C.c_int]
+        L.orc_prj_init.restype = None
+        L.orc_prj_init.argtypes = [C.c_void_p]
+        L.orc_prj_iterate.restype = C.c_uint32
+        L.orc_prj_iterate.argtypes = [C.c_void_p, C.c_uint32, C.c_double, C.POINTER(C.c_double)]
+        L.orc_prj_ranks.restype = None
+        L.orc_prj_ranks.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+        L.orc_prj_free.restype = None
+        L.orc_prj_free.argtypes = [C.c_void_p]
+        L.orc_partition_edge_balanced.restype = None
+        L.orc_partition_edge_balanced.argtypes = [C.c_uint32, u64p, C.c_uint32, u32p]
         _lib = L
     return _lib
 
@@ -200,3 +225,83 @@ def pr_jacobi_fp64_mt(ro, col, damping: float = 0.85, iters: int = 100, tol: flo
                                      threads or (os.cpu_count() or 1), pr.ctypes.data_as(C.POINTER(C.c_double)),
                                      C.byref(res))
     return pr, int(it), float(res.value)
+
+
+def rmat_seed(scale: int, edge_factor: int) -> int:
+    return int(lib().orc_rmat_seed(scale, edge_factor))
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19, seed=None,
+             symmetrize: bool = False, weighted: bool = False, threads: int = 0):
+    """The restated seeded RMAT generator: (row_offsets u64, col u32, weights
+    u32 or None), identical to the product generator's CSR for the same
+    arguments."""
+    if seed is None:
+        seed = rmat_seed(scale, edge_factor)
+    h = lib().orc_gen_rmat(scale, edge_factor, a, b, c, seed, int(symmetrize), int(weighted), threads)
+    if not h:
+        raise ValueError("oracle generator rejected the arguments")
+    try:
+        V = lib().orc_graph_num_vertices(h)
+        E = lib().orc_graph_num_edges(h)
+        ro = np.empty(V + 1, dtype=np.uint64)
+        col = np.empty(max(E, 1), dtype=np.uint32)
+        w = np.empty(max(E, 1), dtype=np.uint32) if weighted else None
+        lib().orc_graph_copy(h, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), _p32(w))
+    finally:
+        lib().orc_graph_free(h)
+    return ro, col[:E], (w[:E] if w is not None else None)
+
+
+def partition_edge_balanced(ro, num_memory: int) -> np.ndarray:
+    ro = np.ascontiguousarray(ro, dtype=np.uint64)
+    part = np.empty(len(ro) - 1, dtype=np.uint32)
+    lib().orc_partition_edge_balanced(len(ro) - 1, ro.ctypes.data_as(u64p), num_memory, part.ctypes.data_as(u32p))
+    return part
+
+
+def csr_checksum(ro, col, w=None) -> str:
+    """Order-sensitive 64-bit digest of a CSR (hex), computed with numpy so
+    that both benchmark arms can state which graph they ran."""
+    m = np.uint64(0x9E3779B97F4A7C15)
+    with np.errstate(over="ignore"):
+        acc = np.uint64(len(ro) - 1) * m
+        for arr in (ro, col, w):
+            if arr is None:
+                continue
+            a = np.ascontiguousarray(arr).astype(np.uint64, copy=False)
+            idx = np.arange(1, len(a) + 1, dtype=np.uint64)
+            acc = acc * np.uint64(31) + np.sum((a + np.uint64(1)) * (idx * m | np.uint64(1)), dtype=np.uint64)
+    return f"{int(acc):016x}"
+
+
+class PrJacobi:
+    """FP32-Kahan Jacobi PageRank (FP64 residual) on the host: the graph is
+    transposed once, then iterations run in bounded samples."""
+
+    def __init__(self, ro, col, damping: float = 0.85, threads: int = 0):
+        ro, col, _ = _csr(ro, col)
+        self.V = len(ro) - 1
+        self._keep = (ro, col)
+        self._h = lib().orc_prj_create(self.V, ro.ctypes.data_as(u64p), col.ctypes.data_as(u32p), damping,
+                                       threads or (os.cpu_count() or 1))
+
+    def init(self) -> None:
+        lib().orc_prj_init(self._h)
+
+    def iterate(self, iters: int, tol: float = 0.0):
+        """Runs up to `iters` iterations (stopping once the residual / V <
+        tol when tol > 0); returns (iterations, last residual / V)."""
+        r = C.c_double()
+        it = lib().orc_prj_iterate(self._h, iters, tol, C.byref(r))
+        return int(it), float(r.value)
+
+    def ranks(self) -> np.ndarray:
+        out = np.empty(self.V, dtype=np.float32)
+        lib().orc_prj_ranks(self._h, out.ctypes.data_as(C.POINTER(C.c_float)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_prj_free(self._h)
+            self._h = None

@@ -799,14 +799,33 @@ uint32_t orc_pr_jacobi_fp64(uint32_t V, const uint64_t* ro, const uint32_t* col,
 // depend on the thread count).  Used as the FP64 reference at full size.
 uint32_t orc_pr_jacobi_fp64_mt(uint32_t V, const uint64_t* ro, const uint32_t* col, double d, uint32_t iters,
                                double tol, int threads, double* pr, double* residual_out) {
+  // in-lists in ascending source order; thread t fills the destinations of
+  // [V*t/T, V*(t+1)/T) while scanning every row in source order
+  const int T = std::max(1, threads);
   std::vector<uint64_t> in_off((size_t)V + 1, 0);
-  for (uint64_t i = 0; i < ro[V]; ++i) in_off[col[i] + 1]++;
+  {
+    std::vector<std::thread> ts;
+    for (int t = 0; t < T; ++t)
+      ts.emplace_back([&, t] {
+        const uint32_t lo = (uint32_t)((uint64_t)V * t / T), hi = (uint32_t)((uint64_t)V * (t + 1) / T);
+        for (uint64_t i = 0; i < ro[V]; ++i)
+          if (col[i] >= lo && col[i] < hi) in_off[col[i] + 1]++;
+      });
+    for (auto& th : ts) th.join();
+  }
   for (uint32_t v = 0; v < V; ++v) in_off[v + 1] += in_off[v];
   std::vector<uint32_t> in_src(ro[V] ? ro[V] : 1);
   {
-    std::vector<uint64_t> cur(in_off.begin(), in_off.end() - 1);
-    for (uint32_t u = 0; u < V; ++u)
-      for (uint64_t i = ro[u]; i < ro[u + 1]; ++i) in_src[cur[col[i]]++] = u;
+    std::vector<std::thread> ts;
+    for (int t = 0; t < T; ++t)
+      ts.emplace_back([&, t] {
+        const uint32_t lo = (uint32_t)((uint64_t)V * t / T), hi = (uint32_t)((uint64_t)V * (t + 1) / T);
+        std::vector<uint64_t> cur(in_off.begin() + lo, in_off.begin() + hi);
+        for (uint32_t u = 0; u < V; ++u)
+          for (uint64_t i = ro[u]; i < ro[u + 1]; ++i)
+            if (col[i] >= lo && col[i] < hi) in_src[cur[col[i] - lo]++] = u;
+      });
+    for (auto& th : ts) th.join();
   }
   Pool pool(threads);
   std::vector<double> contrib(V);

@@ -100,3 +100,25 @@ def test_layout_rejects_bad_input():
         g.layout_preview(G, np.full(G.num_vertices, 7, dtype=np.uint32), 3, 0)
     with pytest.raises(g.GrdError):
         g.layout_preview(G, None, 0, 0)
+
+
+@pytest.mark.parametrize("scale,ef,sym,weighted", [(6, 4, False, False), (9, 8, True, True), (12, 16, False, True),
+                                                   (13, 16, True, False), (14, 32, False, True)])
+def test_oracle_generator_equals_product(scale, ef, sym, weighted):
+    """The oracle's restated RMAT generator (its own key sort) gives the
+    product generator's CSR, weights and edge-balanced partition bit for bit,
+    so the CPU reference arm runs on the benchmark's graphs without the
+    product library."""
+    from oracle import ffi as O
+    seed = g.rmat_seed(scale, ef)
+    assert O.rmat_seed(scale, ef) == seed
+    G = g.Graph.rmat(scale, ef, seed=seed, symmetrize=sym, weighted=weighted)
+    ro, col, w = O.gen_rmat(scale, ef, seed=seed, symmetrize=sym, weighted=weighted)
+    np.testing.assert_array_equal(G.row_offsets, ro)
+    np.testing.assert_array_equal(G.col_indices, col)
+    if weighted:
+        np.testing.assert_array_equal(G.weights, w)
+    else:
+        assert w is None
+    np.testing.assert_array_equal(G.partition_edge_balanced(3), O.partition_edge_balanced(ro, 3))
+    assert O.csr_checksum(G.row_offsets, G.col_indices, G.weights) == O.csr_checksum(ro, col, w)
