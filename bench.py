@@ -198,9 +198,11 @@ class Workload:
         self.G_d = g.Graph.rmat(scale, EF, a, b, c, seed=self.seed, weighted=True, threads=threads)
         self.p_cc = self.G_cc.partition_edge_balanced(NUM_MEMORY)
         self.p_d = self.G_d.partition_edge_balanced(NUM_MEMORY)
+        # PageRank reads no weights: its context holds the directed CSR alone
+        self.G_pr = g.Graph.from_csr(self.G_d.row_offsets, self.G_d.col_indices)
         self.cc = g.Context(self.G_cc, self.p_cc, num_memory=NUM_MEMORY, device=local)
         self.ss = g.Context(self.G_d, self.p_d, num_memory=NUM_MEMORY, device=local)
-        self.pr = g.Context(self.G_d, self.p_d, num_memory=NUM_MEMORY, device=local)
+        self.pr = g.Context(self.G_pr, self.p_d, num_memory=NUM_MEMORY, device=local)
         self.pr.set_algo(g.GRD_PR_PULL, max_rounds=PR_MAX_ITERS, tolerance=PR_TOL)
         self.ctxs = (self.cc, self.ss, self.pr)
         self.E_cc, self.E_d = self.G_cc.num_edges, self.G_d.num_edges
@@ -518,7 +520,7 @@ def bench_ingest(g, W, args, local, barrier, dev) -> dict:
     (layout.cpp, all host threads) and on the GPU (grd_ingest: the CSR
     uploaded from host memory, then proxies, translation slots, the relabelled
     CSR and, for PageRank, the in-edge view built by kernels)."""
-    graphs = ((W.G_cc, W.p_cc), (W.G_d, W.p_d), (W.G_d, W.p_d))
+    graphs = ((W.G_cc, W.p_cc), (W.G_d, W.p_d), (W.G_pr, W.p_d))
     t0 = time.perf_counter()
     for G, p in graphs[:2]:
         g.layout_preview(G, p, NUM_MEMORY, 0)
