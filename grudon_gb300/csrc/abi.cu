@@ -276,6 +276,8 @@ bool use_pull(const grd_ctx* ctx) {
 
 }  // namespace
 
+int grd_check_ready(grd_ctx* ctx) { return check_ready(ctx); }
+
 int grd_choose_round_mode(const grd_ctx* ctx) {
   if (policy_no_offload(ctx->params.offload, ctx->last_frontier, ctx->g.V)) return RM_NO_OFFLOAD;
   const bool pull = use_pull(ctx), list = !use_dense(ctx);
@@ -1186,6 +1188,7 @@ int grd_set_policy(grd_ctx* ctx, const grd_policy_model* model) {
 
 int grd_aggregate_values(grd_ctx* ctx, const uint32_t* gids, const uint32_t* values, size_t n) {
   TRY(check_ready(ctx));
+  TRY(grd_wait(ctx, nullptr));  // a queued run first: the call changes the ctx
   if (n == 0) return GRD_OK;
   if (!gids || !values) return GRD_E_INVALID;
   if (n > 0xFFFFFFFFull) {

@@ -126,6 +126,8 @@ struct grd_ctx {
   } while (0)
 
 int grd_ctx_init_stream(grd_ctx* ctx);
+// GRD_OK when the ctx can run stages: a complete layout, an algorithm, init done.
+int grd_check_ready(grd_ctx* ctx);
 int grd_ctx_init_device(grd_ctx* ctx);
 int grd_alloc_resident(grd_ctx* ctx);
 // On-device layout build (layout_dev.cu).

@@ -5,9 +5,7 @@
 //  * a serving process that reserved the device's memory up front for its own
 //    pool, so a new allocation would fail or evict that pool;
 //  * a latency-bound caller that must not take the allocator's implicit
-//    device synchronisation;
-//  * a host thread that is in the middle of capturing other work into a CUDA
-//    graph, where allocation calls are not permitted.
+//    device synchronisation.
 // grd_aggregate_values allocates its device staging buffer on first use and
 // whenever a larger batch arrives.  This variant stages the (gid, value) pairs
 // in the file-scope device array below instead, so it never allocates; the
@@ -53,11 +51,8 @@ int stage_address(grd_ctx* ctx, uint32_t** out) {
 }  // namespace
 
 extern "C" int grd_aggregate_values_noalloc(grd_ctx* ctx, const uint32_t* gids, const uint32_t* values, size_t n) {
-  if (!ctx) return GRD_E_INVALID;
-  if (ctx->algo < 0 || !ctx->inited) {
-    ctx->err = "grd_set_algo and grd_init must come first";
-    return GRD_E_INVALID;
-  }
+  TRY(grd_check_ready(ctx));   // the same readiness rules as grd_aggregate_values
+  TRY(grd_wait(ctx, nullptr));  // a queued run first: the call changes the ctx
   if (n == 0) return GRD_OK;
   if (!gids || !values) return GRD_E_INVALID;
   if (n > GRD_NOALLOC_MAX_VALUES) {

@@ -237,10 +237,9 @@ int grd_aggregate_values(grd_ctx* ctx, const uint32_t* gids,
                          const uint32_t* values, size_t n);
 
 /* grd_aggregate_values for callers that cannot allocate device memory — a
- * serving process whose memory is already reserved for its own pool, a
+ * serving process whose memory is already reserved for its own pool, or a
  * latency-bound caller that must not take the allocator's device
- * synchronisation, or a thread in the middle of capturing other work into a
- * CUDA graph.  No counterpart in the reference.  Same arguments and result as
+ * synchronisation.  No counterpart in the reference.  Same arguments and result as
  * grd_aggregate_values, but the pairs are staged in a fixed device array
  * inside the library (2 MiB, held by every GPU that loads the library until
  * exit) instead of an allocated buffer, so at most GRD_NOALLOC_MAX_VALUES

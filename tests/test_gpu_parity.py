@@ -271,7 +271,10 @@ def test_pr_pull_converges_and_stage_api(gpu):
         ctx.init()
         st = ctx.run()
         ref, it, _ = O.pr_jacobi_fp64(ro, ci, iters=100, tol=1e-7)
-        assert st["converged"] == 1 and abs(st["rounds"] - it) <= 1
+        assert st["converged"] == 1 and abs(st["rounds"] - it) <= 1  # FP64 may stop one iteration apart
+        P = O.PrJacobi(ro, ci, threads=2)  # the same FP32-Kahan arithmetic and stop rule
+        P.init()
+        assert P.iterate(100, 1e-7)[0] == st["rounds"]
         full = ctx.read_ranks()
         # the same iterations through the per-stage API
         ctx.init()
@@ -343,3 +346,50 @@ def test_small_rounds_run_back_to_back_in_one_kernel(gpu, algo, oalgo, offload):
                     assert ds["kernel_launches"] < 2 * ds["rounds"]
             else:
                 assert ds["rounds"] == 37 and ds["converged"] == 0
+
+
+def test_cc_sssp_rmat20_with_hub_rows_bit_exact(gpu):
+    """RMAT-20, 1C+3M: rows above the hub threshold exist (so the hub kernel
+    runs) and CC labels / weighted SSSP distances, round counts and the
+    verify() invariants equal the oracle's restated round protocol."""
+    import os
+    threads = os.cpu_count() or 1
+    for algo, oalgo, sym in ((g.GRD_CC, O.ORC_CC, True), (g.GRD_SSSP_W, O.ORC_SSSP_W, False)):
+        G = g.Graph.rmat(20, 16, symmetrize=sym, weighted=not sym)
+        part = G.partition_edge_balanced(3)
+        ref = O.Layout(G.row_offsets, G.col_indices, G.weights, part, 3).run(oalgo, threads=threads)
+        with g.Context(G, part, num_memory=3) as ctx:
+            assert len(ctx.read_layout("hubs")) > 0
+            ctx.set_algo(algo)
+            ctx.init()
+            st = ctx.run()
+            np.testing.assert_array_equal(ctx.read_props(), ref["props"])
+            assert st["rounds"] == ref["stats"]["rounds"]
+            assert st["bytes_synced"] == ref["stats"]["bytes_synced"]
+            assert ctx.verify()["errors"] == 0
+
+
+def test_pr_pull_reproducible_and_tight(gpu):
+    """PR_PULL sums every list in a fixed order and reduces the residual in a
+    fixed order: two runs give the same ranks, residual and iteration count
+    bit for bit, within 1e-5 relative error of FP64 Jacobi and one FP32 ulp
+    scale of the host FP32-Kahan restatement."""
+    G = g.Graph.rmat(16, 16)
+    ro, ci = G.row_offsets, G.col_indices
+    part = G.partition_edge_balanced(3)
+    with g.Context(G, part, num_memory=3) as ctx:
+        ctx.set_algo(g.GRD_PR_PULL, max_rounds=100, tolerance=1e-7)
+        runs = []
+        for _ in range(2):
+            ctx.init()
+            st = ctx.run()
+            runs.append((st["rounds"], st["last_residual"], ctx.read_ranks()))
+        assert runs[0][0] == runs[1][0] and runs[0][1] == runs[1][1]
+        np.testing.assert_array_equal(runs[0][2], runs[1][2])
+        it = runs[0][0]
+        ref, _, _ = O.pr_jacobi_fp64(ro, ci, iters=it)
+        assert _max_rel_err(runs[0][2], ref) <= 1e-5
+        P = O.PrJacobi(ro, ci, threads=2)
+        P.init()
+        assert P.iterate(100, 1e-7)[0] == it
+        assert _max_rel_err(runs[0][2], P.ranks().astype(np.float64)) <= 1e-5

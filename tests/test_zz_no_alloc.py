@@ -1,7 +1,7 @@
 """grd_aggregate_values_noalloc — the aggregate entry point for callers that
 cannot allocate device memory (a process whose device memory is reserved for
-its own pool, a caller that must not take the allocator's synchronisation, a
-thread that is capturing a CUDA graph) — against grd_aggregate_values.
+its own pool, or a caller that must not take the allocator's
+synchronisation) — against grd_aggregate_values.
 
 Collected last on purpose: it exercises the library's fixed staging array,
 and a failure here must not hide results of the other tests.  It passes run
@@ -66,3 +66,38 @@ def test_noalloc_rejects_oversize_and_bad_ids(gpu):
         assert _call(ctx, ctx._lib.grd_aggregate_values_noalloc, [G.num_vertices], [1]) == _ffi.GRD_E_INVALID
         full = np.arange(MAX, dtype=np.uint32) % G.num_vertices
         assert _call(ctx, ctx._lib.grd_aggregate_values_noalloc, full, full) == 0
+
+
+def test_noalloc_allocates_nothing_after_set_up(gpu):
+    """After the first call (the per-device address look-up), further calls
+    leave the device's free memory unchanged."""
+    import torch
+    G = g.Graph.rmat(12, 8)
+    rng = np.random.default_rng(3)
+    with g.Context(G) as ctx:
+        ctx.set_algo(g.GRD_CC)
+        ctx.init()
+        gids = rng.integers(0, G.num_vertices, 4096)
+        assert _call(ctx, ctx._lib.grd_aggregate_values_noalloc, gids, gids) == 0
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        for _ in range(2):
+            assert _call(ctx, ctx._lib.grd_aggregate_values_noalloc, gids, gids) == 0
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0
+
+
+def test_noalloc_refuses_an_incomplete_layout_like_the_allocating_one(gpu):
+    """A re-ingest that fails part-way leaves the layout incomplete: both
+    aggregate entry points then refuse the call."""
+    G = g.Graph.rmat(11, 8, symmetrize=True)
+    part = G.partition_edge_balanced(2)
+    with g.Context(G, part, num_memory=2, device_layout=True) as ctx:
+        ctx.set_algo(g.GRD_CC)
+        ctx.init()
+        swapped = (1 - part).astype(np.uint32)  # other owned and proxy counts
+        with pytest.raises(g.GrdError):
+            ctx.ingest(G, swapped)
+        for fn in (ctx._lib.grd_aggregate_values, ctx._lib.grd_aggregate_values_noalloc):
+            assert _call(ctx, fn, [1, 2], [0, 0]) == _ffi.GRD_E_INVALID
