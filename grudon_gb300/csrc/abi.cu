@@ -203,6 +203,40 @@ int grd_ensure_in_edges(grd_ctx* ctx) {
   return GRD_OK;
 }
 
+// Delta PageRank sums every in-hub (in-list longer than K_PULL_HUB) as its
+// 32-edge chunks: the chunk table lists, per hub, its first chunk, and per
+// chunk, its hub.  Built from the resident in-hub list whenever the layout
+// changed.
+int grd_pr_delta_hubs(grd_ctx* ctx) {
+  PullState& P = ctx->pull;
+  if (P.hub_gen == ctx->layout_gen) return GRD_OK;
+  const uint32_t nh = P.num_in_hubs;
+  std::vector<HubChunkD> hubs(nh);
+  if (nh) {
+    CK(cudaMemcpyAsync(hubs.data(), P.in_hubs, sizeof(HubChunkD) * nh, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  std::vector<uint32_t> coff(nh + 1, 0), chunk_hub;
+  for (uint32_t k = 0; k < nh; ++k) coff[k + 1] = coff[k] + (hubs[k].e1 - hubs[k].e0 + 31) / 32;
+  const uint32_t nc = coff[nh];
+  chunk_hub.resize(nc);
+  for (uint32_t k = 0; k < nh; ++k)
+    for (uint32_t q = coff[k]; q < coff[k + 1]; ++q) chunk_hub[q] = k;
+  if (!P.hub_coff) TRY(dev_alloc(ctx, &P.hub_coff, (size_t)nh + 1));  // the hub count is fixed for a ctx
+  if (nc > P.hub_chunk_cap || !P.chunk_hub) {
+    TRY(dev_alloc(ctx, &P.chunk_hub, std::max<size_t>(nc, 1)));
+    TRY(dev_alloc(ctx, &P.chunk_sum, std::max<size_t>(nc, 1)));
+    P.hub_chunk_cap = nc;
+  }
+  CK(cudaMemcpyAsync(P.hub_coff, coff.data(), sizeof(uint32_t) * (nh + 1), cudaMemcpyHostToDevice, ctx->stream));
+  if (nc)
+    CK(cudaMemcpyAsync(P.chunk_hub, chunk_hub.data(), sizeof(uint32_t) * nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));  // the host vectors go out of scope
+  P.num_hub_chunks = nc;
+  P.hub_gen = ctx->layout_gen;
+  return GRD_OK;
+}
+
 // ---------------------------------------------------------------- stages --
 namespace {
 
@@ -267,8 +301,19 @@ bool use_dense(const grd_ctx* ctx) {
 // for full frontiers, so the fixed rule pulls only when at least 1/pull_div of
 // the vertices are active and the in-edge view exists (it is built when pull
 // is requested).
-bool use_pull(const grd_ctx* ctx) {
+// Pull rounds are available when the in-edge view exists; delta PageRank
+// always has it (its fixed-order sums read it), but pulls only when asked to
+// (GRD_DIR_PULL, or the learned policy), so the plain method stays the push
+// method.
+bool pull_available(const grd_ctx* ctx) {
   if (!ctx->in_edges_alloc) return false;
+  if (ctx->algo != GRD_PR_DELTA) return true;
+  const grd_params& p = ctx->params;
+  return p.direction == GRD_DIR_PULL || (p.policy == GRD_POLICY_LEARNED && p.direction == GRD_DIR_AUTO);
+}
+
+bool use_pull(const grd_ctx* ctx) {
+  if (!pull_available(ctx)) return false;
   if (ctx->params.direction == GRD_DIR_PULL) return true;
   if (ctx->params.direction == GRD_DIR_PUSH) return false;
   return ctx->last_frontier * ctx->params.pull_div >= ctx->g.V;
@@ -288,7 +333,7 @@ PolicyArgs grd_policy_args(const grd_ctx* ctx) {
   PolicyArgs a{};
   a.direction = ctx->params.direction;
   a.format = ctx->params.frontier_format;
-  a.has_in = ctx->in_edges_alloc ? 1 : 0;
+  a.has_in = pull_available(ctx) ? 1 : 0;
   a.dense_div = ctx->params.dense_div;
   a.pull_div = ctx->params.pull_div;
   a.offload = ctx->params.offload;
@@ -356,9 +401,13 @@ static bool diff_aggregates(const grd_ctx* ctx) {
 
 // Kernels of the edge-map of one round in each mode.
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
+  const bool pr = ctx->algo == GRD_PR_DELTA;
+  const uint32_t hub_sums = ctx->pull.num_in_hubs ? 2 : 0;  // delta PageRank's in-hub chunk sums
   if (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)
-    return 1 + (ctx->pull.num_in_meds ? 1 : 0) + (ctx->pull.num_in_hubs ? 1 : 0);
-  return 3 + (ctx->g.num_hubs ? 1 : 0) + (mode == RM_PUSH_BITVEC ? 1 : 0);  // push, NO_OFFLOAD too
+    return pr ? 1 + hub_sums : 1 + (ctx->pull.num_in_meds ? 1 : 0) + (ctx->pull.num_in_hubs ? 1 : 0);
+  // push (NO_OFFLOAD too); PageRank's push adds the fixed-order sums
+  return 3 + (ctx->g.num_hubs ? 1 : 0) + (mode == RM_PUSH_BITVEC ? 1 : 0) +
+         (pr && (mode == RM_PUSH_BITVEC || mode == RM_PUSH_LIST) ? 1 + hub_sums : 0);
 }
 
 // Kernels of a whole round in each mode (edge-map + syncs + update).
@@ -373,7 +422,8 @@ uint32_t grd_round_launches(const grd_ctx* ctx, int mode) {
   // when the dirty diff aggregates); update
   const uint32_t bwd = mode == RM_PUSH_BITVEC && diff_aggregates(ctx) ? 0u
                                                                       : (mode == RM_PULL_BITVEC ? 1u : 0u) + groups;
-  const uint32_t sync = list ? 3 /*fwd, bwd, update lists*/ : (2 + bwd + 1);
+  // list: fwd, bwd (PageRank: one per partition), update lists
+  const uint32_t sync = list ? 2 + groups : (2 + bwd + 1);
   // push: the forward sync runs the degree passes (bitvector: both, list: the first)
   return sync + grd_edge_map_launches(ctx, mode) - (mode == RM_PUSH_LIST ? 1u : mode == RM_PUSH_BITVEC ? 2u : 0u);
 }
@@ -400,6 +450,24 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bo
     constexpr int A = decltype(a)::value;
     const uint32_t pull_hub_grid = std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8));
     const uint32_t pull_med_grid = std::min<uint32_t>((ctx->pull.num_in_meds + 7) / 8, grid_for(ctx, 8));
+    const PullState& PS = ctx->pull;
+    const PrHubs ph{PS.in_hubs, PS.hub_coff, PS.chunk_hub, PS.chunk_sum, PS.num_in_hubs, PS.num_hub_chunks};
+    const uint32_t hsum_grid = std::max<uint32_t>(1, std::min<uint32_t>((ph.nh + 255) / 256, grid_for(ctx, 4)));
+    if (A == A_PR_DELTA && (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)) {  // the fixed-order sums
+      if (mode == RM_PULL_LIST)
+        k_pr_delta_pull<true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      else
+        k_pr_delta_pull<false><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ph.nh) {
+        k_pr_delta_hub_chunks<0><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st, ph);
+        if (mode == RM_PULL_LIST)
+          k_pr_delta_hub_sum<0, true><<<hsum_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ph);
+        else
+          k_pr_delta_hub_sum<0, false><<<hsum_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ph);
+      }
+      CK_LAUNCH();
+      return GRD_OK;
+    }
     if (mode == RM_PULL_BITVEC) {
       k_pull<A, false><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
       if (ctx->pull.num_in_meds)
@@ -458,6 +526,20 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bo
     if (fork) {
       CK(cudaEventRecord(ctx->ev_join, ctx->side));
       CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+    }
+    if (A == A_PR_DELTA && mode == RM_PUSH_BITVEC) {  // the touched slots get the fixed-order sums
+      k_pr_delta_resum_bits<<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ph.nh) {
+        k_pr_delta_hub_chunks<1><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st, ph);
+        k_pr_delta_hub_sum<1, false><<<hsum_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ph);
+      }
+    }
+    if (A == A_PR_DELTA && mode == RM_PUSH_LIST) {
+      k_pr_delta_resum_list<<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+      if (ph.nh) {
+        k_pr_delta_hub_chunks<2><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st, ph);
+        k_pr_delta_hub_sum<2, false><<<hsum_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ph);
+      }
     }
     if (mode == RM_PUSH_BITVEC) {
       if constexpr (A != A_PR_DELTA && A != A_PR_PULL) {
@@ -542,7 +624,11 @@ static int enqueue_fwd_list_deg(grd_ctx* ctx) {
 int grd_enqueue_bwd_update_list(grd_ctx* ctx) {
   return dispatch(ctx->algo, [&](auto a) -> int {
     constexpr int A = decltype(a)::value;
-    k_bwd_list<A><<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+    if (A == A_PR_DELTA)  // partition by partition: each vertex sums its partitions' values in order
+      for (uint32_t p = 0; p < ctx->L.M; ++p)
+        k_bwd_list<A><<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st, p);
+    else
+      k_bwd_list<A><<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st, 0xFFFFFFFFu);
     k_update_list<A><<<grid_for(ctx, 4), 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->params.tolerance,
                                                                 ctx->params.damping);
     CK_LAUNCH();
@@ -909,7 +995,7 @@ int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
     return GRD_E_INVALID;
   }
   CK(cudaSetDevice(ctx->device));
-  if (algo == GRD_PR_PULL || p.direction == GRD_DIR_PULL ||
+  if (algo == GRD_PR_PULL || algo == GRD_PR_DELTA /* fixed-order sums */ || p.direction == GRD_DIR_PULL ||
       (p.policy == GRD_POLICY_LEARNED && p.direction == GRD_DIR_AUTO)) {  // the model may pull
     int rc = grd_ensure_in_edges(ctx);
     if (rc != GRD_OK) return rc;
@@ -1484,5 +1570,6 @@ int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks) {
   }
   CK_LAUNCH();
   if (ctx->algo == GRD_PR_PULL) return grd_pull_stage(ctx, -1);  // pull-specific init
+  if (ctx->algo == GRD_PR_DELTA) return grd_pr_delta_hubs(ctx);
   return GRD_OK;
 }

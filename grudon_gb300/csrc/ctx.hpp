@@ -39,6 +39,13 @@ struct PullState {
   grd::HubChunkD* in_meds = nullptr;  // destination slots with medium in-lists
   uint32_t num_in_meds = 0;
   uint64_t edges = 0;                 // in-edges read since init
+  // Delta PageRank's in-hub sums (32-edge chunks summed grid-wide): the
+  // first chunk of each hub, the hub of each chunk, the chunk sums.
+  uint32_t* hub_coff = nullptr;
+  uint32_t* chunk_hub = nullptr;
+  float* chunk_sum = nullptr;
+  uint32_t num_hub_chunks = 0, hub_chunk_cap = 0;
+  uint64_t hub_gen = ~0ull;  // layout generation the tables describe
 };
 
 struct grd_ctx {
@@ -141,6 +148,8 @@ void grd_prof_mark(grd_ctx* ctx, int i);
 void grd_prof_collect(grd_ctx* ctx);
 void grd_ctx_release_extras(grd_ctx* ctx);
 int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks);
+// Delta PageRank's in-hub chunk tables for the resident layout (abi.cu).
+int grd_pr_delta_hubs(grd_ctx* ctx);
 int grd_upload_layout(grd_ctx* ctx);
 int grd_ensure_in_edges(grd_ctx* ctx);
 int grd_read_counters(grd_ctx* ctx);

@@ -1550,6 +1550,170 @@ __global__ void __launch_bounds__(256) k_pull_hub(DevGraph g, DevState st, const
   }
 }
 
+// ---------------------------------------- delta PageRank: one fixed order --
+// Every delta-PageRank edge-map (push or pull, bitvector or list sync, the
+// one-CTA round) gives each memory-side destination slot the same value: its
+// in-list (ascending source slot) is cut into 32-edge chunks from the list's
+// start; a chunk's frontier contributions (0 for sources outside the
+// frontier and past the list's end) are added by a halving tree -- x[i] +=
+// x[i + o] for o = 16, 8, 4, 2, 1, which is the warp's xor butterfly -- and
+// the chunk sums are added in chunk order.  So the value depends on the graph
+// and the frontier only, not on the round mode or on thread timing, and the
+// oracle restates the same order.  The push's reductions still find the
+// slots it touches (the dirty set); their sums are then replaced by this one.
+// Warp-wide: every lane returns the sum.
+__device__ __forceinline__ float pr_delta_sum_warp(const DevGraph& g, const DevState& st, uint32_t d) {
+  const uint32_t lane = lane_id();
+  const uint32_t a = __ldg(&g.in_off[d]), b = __ldg(&g.in_off[d + 1]);
+  float acc = 0.0f;
+  for (uint32_t c = a; c < b; c += 32) {
+    const uint32_t e = c + lane;
+    float x = 0.0f;
+    if (e < b) {
+      const uint32_t src = __ldg(&g.in_src[e]);
+      if (test_bit(st.FB, src)) x = __uint_as_float(st.mprop[src]);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) x = __fadd_rn(x, __shfl_xor_sync(FULL, x, o));
+    acc = __fadd_rn(acc, x);
+  }
+  return acc;
+}
+
+// In-lists longer than K_PULL_HUB (the in-hubs) are summed grid-wide: every
+// 32-edge chunk by its own warp into a scratch array, then the chunk sums of
+// each list in chunk order by one thread -- the same order, in parallel.
+__device__ __forceinline__ bool pr_delta_long(const DevGraph& g, uint32_t d) {
+  return __ldg(&g.in_off[d + 1]) - __ldg(&g.in_off[d]) > K_PULL_HUB;
+}
+
+struct PrHubs {
+  const HubChunkD* hubs;      // (slot, e0, e1) of every in-hub
+  const uint32_t* coff;       // [nh + 1] first chunk of each hub
+  const uint32_t* chunk_hub;  // [nc] hub of each chunk
+  float* csum;                // [nc] chunk sums
+  uint32_t nh, nc;
+};
+
+// kMode 0: pull (every hub), 1: push + bitvector (touched: mupd != 0),
+// 2: push + list (touched: dirty bit claimed).
+template <int kMode>
+__device__ __forceinline__ bool pr_hub_needed(const DevState& st, uint32_t slot) {
+  if (kMode == 0) return true;
+  if (kMode == 1) return __ldcg(&st.mupd[slot]) != 0u;
+  return (__ldcg(&st.MD[slot >> 5]) >> (slot & 31)) & 1u;
+}
+
+__device__ __forceinline__ float pr_delta_chunk(const DevState& st, const DevGraph& g, uint32_t e, uint32_t end) {
+  float x = 0.0f;
+  if (e < end) {
+    const uint32_t src = __ldg(&g.in_src[e]);
+    if (test_bit(st.FB, src)) x = __uint_as_float(st.mprop[src]);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) x = __fadd_rn(x, __shfl_xor_sync(FULL, x, o));
+  return x;
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(256) k_pr_delta_hub_chunks(DevGraph g, DevState st, PrHubs h) {
+  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < h.nc; q += nw) {
+    const uint32_t k = h.chunk_hub[q];
+    const HubChunkD hc = h.hubs[k];
+    if (!pr_hub_needed<kMode>(st, hc.slot)) continue;
+    const float x = pr_delta_chunk(st, g, hc.e0 + 32u * (q - h.coff[k]) + lane_id(), hc.e1);
+    if (lane_id() == 0) h.csum[q] = x;
+  }
+}
+
+template <int kMode, bool kList>
+__global__ void __launch_bounds__(256) k_pr_delta_hub_sum(DevGraph g, DevState st, PrHubs h) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < h.nh; k += gridDim.x * blockDim.x) {
+    const uint32_t slot = h.hubs[k].slot;
+    if (!pr_hub_needed<kMode>(st, slot)) continue;
+    const uint32_t q0 = h.coff[k], q1 = h.coff[k + 1];
+    float acc = 0.0f;
+    uint32_t q = q0;
+    for (; q + 8 <= q1; q += 8) {
+      float x[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) x[i] = h.csum[q + i];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) acc = __fadd_rn(acc, x[i]);
+    }
+    for (; q < q1; ++q) acc = __fadd_rn(acc, h.csum[q]);
+    if (kMode != 0) {
+      st.mupd[slot] = __float_as_uint(acc);
+    } else if (acc > 0.0f) {  // pull: the warp kernel wrote the slot's dirty word first
+      st.mupd[slot] = __float_as_uint(acc);
+      if (kList)
+        mark_listed(st.MD, slot, st.DL, st.lc + L_DL);
+      else
+        red_or(st.MD + (slot >> 5), 1u << (slot & 31));
+    }
+  }
+}
+
+// Push + bitvector rounds: the slots the push touched (mupd != 0: every
+// contribution is positive) get the fixed-order sum; runs before the dirty
+// diff, which clears the forward bitvector.
+static __global__ void __launch_bounds__(256) k_pr_delta_resum_bits(DevGraph g, DevState st) {
+  const uint32_t lane = lane_id();
+  const uint64_t nwords = g.S / 32;
+  const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  for (uint64_t w = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nwords; w += nw) {
+    const uint32_t s = (uint32_t)(w * 32) + lane;
+    uint32_t m = __ballot_sync(FULL, __ldcg(&st.mupd[s]) != 0u && !pr_delta_long(g, s));
+    while (m) {
+      const uint32_t d = (uint32_t)(w * 32) + (uint32_t)(__ffs(m) - 1);
+      m &= m - 1;
+      const float v = pr_delta_sum_warp(g, st, d);
+      if (lane == 0) st.mupd[d] = __float_as_uint(v);
+    }
+  }
+}
+
+// Push + list rounds: the listed dirty slots get the fixed-order sum.
+static __global__ void __launch_bounds__(256) k_pr_delta_resum_list(DevGraph g, DevState st) {
+  const uint32_t n = __ldcg(&st.lc[L_DL]);
+  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < n; j += nw) {
+    const uint32_t d = st.DL[j];
+    if (pr_delta_long(g, d)) continue;  // k_pr_delta_hub_* sum it
+    const float v = pr_delta_sum_warp(g, st, d);
+    if (lane_id() == 0) st.mupd[d] = __float_as_uint(v);
+  }
+}
+
+// Pull rounds: every slot with in-edges gets the fixed-order sum; a slot with
+// a frontier in-neighbour (sum > 0) is dirty.  One warp per 32-slot word
+// writes the word's dirty bits; kList also lists the dirty slots.
+template <bool kList>
+__global__ void __launch_bounds__(256) k_pr_delta_pull(DevGraph g, DevState st) {
+  const uint32_t lane = lane_id();
+  const uint64_t nwords = g.S / 32;
+  const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  for (uint64_t w = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nwords; w += nw) {
+    const uint32_t s = (uint32_t)(w * 32) + lane;
+    const uint32_t deg = __ldg(&g.in_off[s + 1]) - __ldg(&g.in_off[s]);
+    uint32_t m = __ballot_sync(FULL, deg > 0 && deg <= K_PULL_HUB);  // long lists: k_pr_delta_hub_*
+    uint32_t dirty = 0;
+    while (m) {
+      const uint32_t i = (uint32_t)(__ffs(m) - 1);
+      m &= m - 1;
+      const uint32_t d = (uint32_t)(w * 32) + i;
+      const float v = pr_delta_sum_warp(g, st, d);
+      if (v > 0.0f) {  // the same in every lane
+        if (lane == 0) st.mupd[d] = __float_as_uint(v);
+        dirty |= 1u << i;
+      }
+    }
+    if (lane == 0) st.MD[w] = dirty;
+    if (kList && ((dirty >> lane) & 1u)) list_append(st.DL, st.lc + L_DL, s);
+  }
+}
+
 // -------------------------------------------------------- list-format sync --
 // List rounds carry the same data as bitvector rounds — the frontier's values
 // to their owning memory partitions, the dirty memory-side updates back — as
@@ -1588,32 +1752,38 @@ static __global__ void __launch_bounds__(256) k_fwd_list(DevGraph g, DevState st
 // vertex_updates, listing every gid whose entry became dirty.  Also retires
 // the old frontier (its FB and F bits), which nothing reads after the
 // edge-map.
+// PageRank runs it once per memory partition, in ascending order (part = p:
+// only that partition's dirty slots; the first launch also retires the old
+// frontier and counts the bytes), so every vertex receives its partitions'
+// sums in partition order, as in bitvector rounds; part = ~0: all at once.
 template <int A>
-__global__ void __launch_bounds__(256) k_bwd_list(DevGraph g, DevState st) {
+__global__ void __launch_bounds__(256) k_bwd_list(DevGraph g, DevState st, uint32_t part) {
   const uint32_t n = __ldcg(&st.lc[L_DL]);
   const uint32_t K = (uint32_t)__ldcg(&st.counters[C_ACTIVE]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  const bool first = part == 0u || part == 0xFFFFFFFFu;
+  if (first && blockIdx.x == 0 && threadIdx.x == 0) {
     st.counters[C_BYTES] += g.bv_bytes + 4ull * n;
     st.counters[C_REFBYTES] += g.bv_refbytes + 4ull * n;
     st.lc[L_FL] = 0;  // the update rebuilds it; entries below are read by index
   }
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < K; j += gridDim.x * blockDim.x) {
-    const uint32_t s = st.AL[j], gid = st.FL[j];
-    atomicAnd(&st.FB[s >> 5], ~(1u << (s & 31)));
-    atomicAnd(&st.F[gid >> 5], ~(1u << (gid & 31)));
-  }
+  if (first)
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < K; j += gridDim.x * blockDim.x) {
+      const uint32_t s = st.AL[j], gid = st.FL[j];
+      atomicAnd(&st.FB[s >> 5], ~(1u << (s & 31)));
+      atomicAnd(&st.F[gid >> 5], ~(1u << (gid & 31)));
+    }
   for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
     const uint32_t j = b + threadIdx.x;
     bool listed = false;
     uint32_t gid = 0;
-    if (j < n) {
-      const uint32_t s = st.DL[j];
+    const uint32_t s = j < n ? st.DL[j] : 0u;
+    if (j < n && (part == 0xFFFFFFFFu || g.tile_part[s / K_TILE_SLOTS] == part)) {
       const uint32_t v = st.mupd[s];
       gid = __ldg(&g.slot_gid[s]);
       retire_update<A>(st, s, v);
       atomicAnd(&st.MD[s >> 5], ~(1u << (s & 31)));
-      if (A == A_PR_DELTA) {
-        atomicAdd(reinterpret_cast<float*>(st.upd) + gid, __uint_as_float(v));
+      if (A == A_PR_DELTA) {  // one slot per vertex in this launch
+        st.upd[gid] = __float_as_uint(__fadd_rn(__uint_as_float(st.upd[gid]), __uint_as_float(v)));
         listed = claim_bit(st.UD, gid);
       } else if (v < __ldcg(&st.upd[gid])) {
         if (v < atomicMin(&st.upd[gid], v)) listed = claim_bit(st.UD, gid);
@@ -1778,6 +1948,7 @@ __device__ __forceinline__ void tiny_round(const DevGraph& g, const DevState& st
       const uint32_t v = st.prop[gid];
       st.AL[j] = s;
       st.mprop[s] = v;
+      if (A == A_PR_DELTA && !kCompute) atomicOr(&st.FB[s >> 5], 1u << (s & 31));  // the fixed-order sum reads it
       const uint32_t r0 = __ldg(&g.row_off[s]);
       d = __ldg(&g.row_off[s + 1]) - r0;
       s_rb[j] = r0;
@@ -1841,6 +2012,53 @@ __device__ __forceinline__ void tiny_round(const DevGraph& g, const DevState& st
     }
   }
   __syncthreads();
+  if (A == A_PR_DELTA && !kCompute) {  // the listed slots get the fixed-order sum
+    const uint32_t nd = __ldcg(&st.lc[L_DL]);
+    for (uint32_t j = tid >> 5; j < nd; j += K_TINY_THREADS / 32) {
+      const uint32_t d = st.DL[j];
+      if (pr_delta_long(g, d)) continue;
+      const float v = pr_delta_sum_warp(g, st, d);
+      if (lane_id() == 0) st.mupd[d] = __float_as_uint(v);
+    }
+    // long lists: every warp sums chunks, thread 0 adds them in order
+    __shared__ uint32_t s_long[K_TINY_THREADS];
+    __shared__ uint32_t s_nlong;
+    __shared__ float s_cs[K_TINY_THREADS];
+    __shared__ float s_acc;
+    for (uint32_t b = 0; b < nd; b += K_TINY_THREADS) {
+      __syncthreads();
+      if (tid == 0) s_nlong = 0;
+      __syncthreads();
+      if (b + tid < nd) {
+        const uint32_t d = st.DL[b + tid];
+        if (pr_delta_long(g, d)) s_long[atomicAdd(&s_nlong, 1u)] = d;
+      }
+      __syncthreads();
+      const uint32_t nl = s_nlong;
+      for (uint32_t i = 0; i < nl; ++i) {
+        const uint32_t d = s_long[i];
+        const uint32_t a = __ldg(&g.in_off[d]), e = __ldg(&g.in_off[d + 1]);
+        const uint32_t nch = (e - a + 31) / 32;
+        if (tid == 0) s_acc = 0.0f;
+        for (uint32_t c0 = 0; c0 < nch; c0 += K_TINY_THREADS) {
+          const uint32_t c1 = min(nch, c0 + K_TINY_THREADS);
+          for (uint32_t c = c0 + (tid >> 5); c < c1; c += K_TINY_THREADS / 32) {
+            const float x = pr_delta_chunk(st, g, a + 32u * c + lane_id(), e);
+            if (lane_id() == 0) s_cs[c - c0] = x;
+          }
+          __syncthreads();
+          if (tid == 0) {
+            float acc = s_acc;
+            for (uint32_t c = c0; c < c1; ++c) acc = __fadd_rn(acc, s_cs[c - c0]);
+            s_acc = acc;
+          }
+          __syncthreads();
+        }
+        if (tid == 0) st.mupd[d] = __float_as_uint(s_acc);
+      }
+    }
+    __syncthreads();
+  }
   // backward sync: retire the old frontier, send and aggregate the dirty
   // slots (NO_OFFLOAD: count the shipped adjacency instead, as k_retire_list)
   const uint32_t n = kCompute ? 0u : __ldcg(&st.lc[L_DL]);
@@ -1857,25 +2075,35 @@ __device__ __forceinline__ void tiny_round(const DevGraph& g, const DevState& st
   for (uint32_t j = tid; j < K; j += K_TINY_THREADS) {
     const uint32_t gid = st.FL[j];
     atomicAnd(&st.F[gid >> 5], ~(1u << (gid & 31)));
-  }
-  for (uint32_t b = 0; b < n; b += K_TINY_THREADS) {
-    const uint32_t j = b + tid;
-    bool listed = false;
-    uint32_t gid = 0;
-    if (j < n) {
-      const uint32_t s = st.DL[j];
-      const uint32_t v = st.mupd[s];
-      gid = __ldg(&g.slot_gid[s]);
-      retire_update<A>(st, s, v);
-      atomicAnd(&st.MD[s >> 5], ~(1u << (s & 31)));
-      if (A == A_PR_DELTA) {
-        atomicAdd(reinterpret_cast<float*>(st.upd) + gid, __uint_as_float(v));
-        listed = claim_bit(st.UD, gid);
-      } else if (v < __ldcg(&st.upd[gid])) {
-        if (v < atomicMin(&st.upd[gid], v)) listed = claim_bit(st.UD, gid);
-      }
+    if (A == A_PR_DELTA && !kCompute) {
+      const uint32_t s = st.AL[j];
+      atomicAnd(&st.FB[s >> 5], ~(1u << (s & 31)));
     }
-    block_append(st.UL, st.lc + L_UL, listed, gid);
+  }
+  // PageRank aggregates partition by partition (ascending), as the
+  // multi-kernel rounds do; min-aggregates in one pass
+  const uint32_t groups = A == A_PR_DELTA ? g.M : 1u;
+  for (uint32_t p = 0; p < groups; ++p) {
+    for (uint32_t b = 0; b < n; b += K_TINY_THREADS) {
+      const uint32_t j = b + tid;
+      bool listed = false;
+      uint32_t gid = 0;
+      const uint32_t s = j < n ? st.DL[j] : 0u;
+      if (j < n && (A != A_PR_DELTA || g.tile_part[s / K_TILE_SLOTS] == p)) {
+        const uint32_t v = st.mupd[s];
+        gid = __ldg(&g.slot_gid[s]);
+        retire_update<A>(st, s, v);
+        atomicAnd(&st.MD[s >> 5], ~(1u << (s & 31)));
+        if (A == A_PR_DELTA) {  // one slot per vertex in this pass
+          st.upd[gid] = __float_as_uint(__fadd_rn(__uint_as_float(st.upd[gid]), __uint_as_float(v)));
+          listed = claim_bit(st.UD, gid);
+        } else if (v < __ldcg(&st.upd[gid])) {
+          if (v < atomicMin(&st.upd[gid], v)) listed = claim_bit(st.UD, gid);
+        }
+      }
+      block_append(st.UL, st.lc + L_UL, listed, gid);
+    }
+    if (A == A_PR_DELTA) __syncthreads();
   }
   if (tid == 0) st.lc[L_FL] = 0;
   __syncthreads();

@@ -225,6 +225,28 @@ struct MemPart {
   uint32_t T() const { return n_owned + n_proxy; }
 };
 
+// In-edge lists of one memory partition: for each destination lid its
+// sources (owned lids) in ascending order.
+struct InEdges {
+  std::vector<uint64_t> off;
+  std::vector<uint32_t> src;
+};
+
+InEdges build_in_edges(const MemPart& P) {
+  InEdges IE;
+  IE.off.assign((size_t)P.T() + 1, 0);
+  const uint64_t E = P.dst.size();
+  for (uint64_t i = 0; i < E; ++i) IE.off[P.dst[i] + 1]++;
+  for (uint32_t d = 0; d < P.T(); ++d) IE.off[d + 1] += IE.off[d];
+  IE.src.resize(E);
+  std::vector<uint64_t> cur(IE.off.begin(), IE.off.end() - 1);
+  for (uint32_t u = 0; u < P.n_owned; ++u) {
+    const uint64_t r0 = u ? P.row_end[u - 1] : 0, r1 = P.row_end[u];
+    for (uint64_t i = r0; i < r1; ++i) IE.src[cur[P.dst[i]]++] = u;
+  }
+  return IE;
+}
+
 struct Layout {
   uint32_t V = 0, M = 0;
   std::vector<uint32_t> mirror;       // compute-side mirror_partition (lid = gid)
@@ -404,6 +426,8 @@ void run_protocol(const Layout& L, uint32_t source, uint32_t max_rounds, double 
   }
   const bool clear_updates = (A == ORC_PR_DELTA);
 
+  std::vector<InEdges> in_edges(A == ORC_PR_DELTA ? M : 0);
+  for (uint32_t p = 0; p < in_edges.size(); ++p) in_edges[p] = build_in_edges(L.parts[p]);
   std::vector<Bitset> fwd_bv(M), bwd_bv(M);
   std::vector<std::vector<T>> fwd_buf(M), bwd_buf(M);
   for (uint32_t p = 0; p < M; ++p) {
@@ -453,6 +477,44 @@ void run_protocol(const Layout& L, uint32_t source, uint32_t max_rounds, double 
       }
       // C4 gen_updates over dirty vertex_properties, ascending lid.
       std::vector<uint32_t> act = mprop[p].dirty.offsets();
+      if (A == ORC_PR_DELTA) {
+        // addUpdate's atomic adds leave each destination's sum in whatever
+        // order the threads ran; this restatement fixes one order (the one
+        // the GPU computes in every round mode): the destination's in-list
+        // (ascending source lid) in 32-edge chunks from its start, each chunk
+        // added by a halving tree (x[i] += x[i + o], o = 16 .. 1) over the
+        // frontier sources' values (0 elsewhere), the chunk sums in order.
+        // The destinations it touches, and so the dirty set, are unchanged.
+        const InEdges& IE = in_edges[p];
+        std::vector<uint8_t> active(P.T(), 0);
+        uint64_t sc = 0;
+        for (uint32_t lid : act) {
+          active[lid] = 1;
+          sc += (lid ? P.row_end[lid] - P.row_end[lid - 1] : P.row_end[lid]);
+        }
+        edges += sc;
+        pool.run(P.T(), 4096, [&](uint64_t b, uint64_t e) {
+          for (uint64_t d = b; d < e; ++d) {
+            bool touched = false;
+            float acc = 0.0f;
+            for (uint64_t c = IE.off[d]; c < IE.off[d + 1]; c += 32) {
+              float x[32];
+              for (int i = 0; i < 32; ++i) {
+                const uint64_t k = c + (uint64_t)i;
+                x[i] = 0.0f;
+                if (k < IE.off[d + 1] && active[IE.src[k]]) {
+                  x[i] = Bits<float>::from(Bits<T>::to(mprop[p].get(IE.src[k])));
+                  touched = true;
+                }
+              }
+              for (int o = 16; o; o >>= 1)
+                for (int i = 0; i < o; ++i) x[i] = x[i] + x[i + o];
+              acc = acc + x[0];
+            }
+            if (touched) mupd[p].set(d, Bits<T>::from(Bits<float>::to(acc)));
+          }
+        });
+      } else {
       std::atomic<uint64_t> scanned{0};
       pool.run(act.size(), 64, [&](uint64_t b, uint64_t e) {
         uint64_t sc = 0;
@@ -478,6 +540,7 @@ void run_protocol(const Layout& L, uint32_t source, uint32_t max_rounds, double 
         scanned.fetch_add(sc);
       });
       edges += scanned.load();
+      }
       // C5 pack dirty vertex_updates (master = compute 0 for every lid).
       bwd_buf[p].clear();
       for (uint32_t lid : mupd[p].dirty.offsets()) {
