@@ -452,7 +452,7 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bo
     const uint32_t pull_med_grid = std::min<uint32_t>((ctx->pull.num_in_meds + 7) / 8, grid_for(ctx, 8));
     const PullState& PS = ctx->pull;
     const PrHubs ph{PS.in_hubs, PS.hub_coff, PS.chunk_hub, PS.chunk_sum, PS.num_in_hubs, PS.num_hub_chunks};
-    const uint32_t hsum_grid = std::max<uint32_t>(1, std::min<uint32_t>((ph.nh + 255) / 256, grid_for(ctx, 4)));
+    const uint32_t hsum_grid = std::max<uint32_t>(1, std::min<uint32_t>((ph.nh + 7) / 8, grid_for(ctx, 8)));
     if (A == A_PR_DELTA && (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)) {  // the fixed-order sums
       if (mode == RM_PULL_LIST)
         k_pr_delta_pull<true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);

@@ -1627,22 +1627,30 @@ __global__ void __launch_bounds__(256) k_pr_delta_hub_chunks(DevGraph g, DevStat
   }
 }
 
+// One warp per hub: the chunk sums are loaded 128 at a time (coalesced) and
+// added in chunk order through shuffles (every lane keeps the same sum).
 template <int kMode, bool kList>
 __global__ void __launch_bounds__(256) k_pr_delta_hub_sum(DevGraph g, DevState st, PrHubs h) {
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < h.nh; k += gridDim.x * blockDim.x) {
+  const uint32_t lane = lane_id();
+  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < h.nh; k += nw) {
     const uint32_t slot = h.hubs[k].slot;
     if (!pr_hub_needed<kMode>(st, slot)) continue;
     const uint32_t q0 = h.coff[k], q1 = h.coff[k + 1];
     float acc = 0.0f;
-    uint32_t q = q0;
-    for (; q + 8 <= q1; q += 8) {
-      float x[8];
+    for (uint32_t q = q0; q < q1; q += 128) {
+      float x[4];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) x[i] = h.csum[q + i];
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t idx = q + 32u * i + lane;
+        x[i] = idx < q1 ? h.csum[idx] : 0.0f;  // past the end: adds nothing
+      }
 #pragma unroll
-      for (int i = 0; i < 8; ++i) acc = __fadd_rn(acc, x[i]);
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int l = 0; l < 32; ++l) acc = __fadd_rn(acc, __shfl_sync(FULL, x[i], l));
     }
-    for (; q < q1; ++q) acc = __fadd_rn(acc, h.csum[q]);
+    if (lane != 0) continue;
     if (kMode != 0) {
       st.mupd[slot] = __float_as_uint(acc);
     } else if (acc > 0.0f) {  // pull: the warp kernel wrote the slot's dirty word first
