@@ -406,6 +406,17 @@ class Context:
             raise ValueError("read_props(wait=False) needs the caller's out array")
         return self._read(self._lib.grd_read_props_async, dt, self.num_vertices, out)
 
+    def sssp_multi(self, sources) -> tuple:
+        """Distances from up to 64 sources at once (grd_sssp_multi): returns
+        (dist[n, V] uint32, stats).  The ctx's algorithm must be SSSP (hop or
+        weighted) and init() must have run."""
+        src = _u32(sources)
+        out = np.empty((len(src), self.num_vertices), dtype=np.uint32)
+        s = _ffi.grd_stats()
+        self._check(self._lib.grd_sssp_multi(self._ctx, src.ctypes.data_as(C.c_void_p), len(src),
+                                             out.ctypes.data_as(C.c_void_p), C.byref(s)))
+        return out, self._stats_dict(s)
+
     def read_ranks(self, out=None, wait: bool = True) -> np.ndarray:
         """PageRank values; wait=False queues the copy like read_props."""
         if out is None:

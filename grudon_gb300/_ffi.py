@@ -149,6 +149,7 @@ SIGNATURES = {
     "grd_read_props_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_ranks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_ranks_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "grd_sssp_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "grd_read_updates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_read_frontier": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "grd_layout_info": (C.c_int, [C.c_void_p, C.c_uint32, u32p, u32p, u64p]),

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-co
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall",
              "-Wno-unused-function"]
 
-CU_SOURCES = ["abi.cu", "pr_pull.cu", "graph_run.cu", "noalloc.cu", "policy.cu", "verify.cu", "layout_dev.cu"]
+CU_SOURCES = ["abi.cu", "pr_pull.cu", "graph_run.cu", "noalloc.cu", "msssp.cu", "policy.cu", "verify.cu", "layout_dev.cu"]
 CPP_SOURCES = ["graph_tools.cpp", "layout.cpp", "policy_io.cpp"]
 
 

@@ -41,6 +41,20 @@ int dev_alloc(grd_ctx* ctx, T** p, size_t count) {
   return rc;
 }
 
+// Stream-ordered scratch (cudaMallocAsync), for set-up passes.
+template <class T>
+int dev_alloc_async(grd_ctx* ctx, T** p, size_t count) {
+  void* d = nullptr;
+  const cudaError_t e = cudaMallocAsync(&d, sizeof(T) * std::max<size_t>(count, 1), ctx->stream);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    ctx->err = std::string("scratch allocation: ") + cudaGetErrorString(e);
+    return GRD_E_OOM;
+  }
+  *p = static_cast<T*>(d);
+  return GRD_OK;
+}
+
 template <class T>
 int upload(grd_ctx* ctx, T* dst, const std::vector<T>& src) {
   if (src.empty()) return GRD_OK;
@@ -203,35 +217,73 @@ int grd_ensure_in_edges(grd_ctx* ctx) {
   return GRD_OK;
 }
 
-// Delta PageRank sums every in-hub (in-list longer than K_PULL_HUB) as its
-// 32-edge chunks: the chunk table lists, per hub, its first chunk, and per
-// chunk, its hub.  Built from the resident in-hub list whenever the layout
-// changed.
+// Delta PageRank sums every list of more than 32 in-edges grid-wide by
+// 32-edge chunks: the table lists those slots (slot, first edge, end), per
+// list its first chunk, and per chunk its list.  Built on the device from the
+// in-edge view whenever the layout changed.
+static __global__ void __launch_bounds__(256) k_prd_mark(DevGraph g, uint32_t* flag, uint32_t* nch) {
+  for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.S; s += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t n = g.in_off[s + 1] - g.in_off[s];
+    const bool lng = n > K_PRD_SHORT;
+    flag[s] = lng ? 1u : 0u;
+    nch[s] = lng ? (n + 31) / 32 : 0u;
+  }
+}
+
+static __global__ void __launch_bounds__(256) k_prd_fill(DevGraph g, const uint32_t* flag, const uint32_t* pos,
+                                                         const uint32_t* cpos, HubChunkD* lists, uint32_t* coff,
+                                                         uint32_t* chunk_list) {
+  for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.S; s += (uint64_t)gridDim.x * blockDim.x) {
+    if (!flag[s]) continue;
+    const uint32_t k = pos[s], a = g.in_off[s], b = g.in_off[s + 1];
+    lists[k] = HubChunkD{(uint32_t)s, a, b};
+    coff[k] = cpos[s];
+    const uint32_t q1 = cpos[s] + (b - a + 31) / 32;
+    for (uint32_t q = cpos[s]; q < q1; ++q) chunk_list[q] = k;
+  }
+}
+
 int grd_pr_delta_hubs(grd_ctx* ctx) {
   PullState& P = ctx->pull;
   if (P.hub_gen == ctx->layout_gen) return GRD_OK;
-  const uint32_t nh = P.num_in_hubs;
-  std::vector<HubChunkD> hubs(nh);
-  if (nh) {
-    CK(cudaMemcpyAsync(hubs.data(), P.in_hubs, sizeof(HubChunkD) * nh, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+  const uint64_t S = ctx->L.S;
+  cudaStream_t s = ctx->stream;
+  uint32_t *flag = nullptr, *nch = nullptr, *pos = nullptr, *cpos = nullptr;
+  TRY(dev_alloc_async(ctx, &flag, S));
+  TRY(dev_alloc_async(ctx, &nch, S));
+  TRY(dev_alloc_async(ctx, &pos, S + 1));
+  TRY(dev_alloc_async(ctx, &cpos, S + 1));
+  const uint32_t grid = (uint32_t)ctx->num_sms * 8;
+  k_prd_mark<<<grid, 256, 0, s>>>(ctx->g, flag, nch);
+  CK_LAUNCH();
+  int rc = grd_scan_add_u32(ctx, flag, pos, S, true);
+  if (rc == GRD_OK) rc = grd_scan_add_u32(ctx, nch, cpos, S, true);
+  uint32_t tot[2] = {0, 0};
+  if (rc == GRD_OK) {
+    CK(cudaMemcpyAsync(&tot[0], pos + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&tot[1], cpos + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
   }
-  std::vector<uint32_t> coff(nh + 1, 0), chunk_hub;
-  for (uint32_t k = 0; k < nh; ++k) coff[k + 1] = coff[k] + (hubs[k].e1 - hubs[k].e0 + 31) / 32;
-  const uint32_t nc = coff[nh];
-  chunk_hub.resize(nc);
-  for (uint32_t k = 0; k < nh; ++k)
-    for (uint32_t q = coff[k]; q < coff[k + 1]; ++q) chunk_hub[q] = k;
-  if (!P.hub_coff) TRY(dev_alloc(ctx, &P.hub_coff, (size_t)nh + 1));  // the hub count is fixed for a ctx
-  if (nc > P.hub_chunk_cap || !P.chunk_hub) {
-    TRY(dev_alloc(ctx, &P.chunk_hub, std::max<size_t>(nc, 1)));
-    TRY(dev_alloc(ctx, &P.chunk_sum, std::max<size_t>(nc, 1)));
-    P.hub_chunk_cap = nc;
+  const uint32_t nl = tot[0], nc = tot[1];
+  if (rc == GRD_OK && (nl > P.prd_list_cap || !P.prd_lists)) {
+    rc = dev_alloc(ctx, &P.prd_lists, std::max<size_t>(nl, 1));
+    if (rc == GRD_OK) rc = dev_alloc(ctx, &P.hub_coff, (size_t)nl + 1);
+    if (rc == GRD_OK) P.prd_list_cap = nl;
   }
-  CK(cudaMemcpyAsync(P.hub_coff, coff.data(), sizeof(uint32_t) * (nh + 1), cudaMemcpyHostToDevice, ctx->stream));
-  if (nc)
-    CK(cudaMemcpyAsync(P.chunk_hub, chunk_hub.data(), sizeof(uint32_t) * nc, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));  // the host vectors go out of scope
+  if (rc == GRD_OK && (nc > P.hub_chunk_cap || !P.chunk_hub)) {
+    rc = dev_alloc(ctx, &P.chunk_hub, std::max<size_t>(nc, 1));
+    if (rc == GRD_OK) rc = dev_alloc(ctx, &P.chunk_sum, std::max<size_t>(nc, 1));
+    if (rc == GRD_OK) P.hub_chunk_cap = nc;
+  }
+  if (rc == GRD_OK) {
+    k_prd_fill<<<grid, 256, 0, s>>>(ctx->g, flag, pos, cpos, P.prd_lists, P.hub_coff, P.chunk_hub);
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(P.hub_coff + nl, &nc, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // nc lives on this stack frame
+  }
+  for (void* p : {(void*)flag, (void*)nch, (void*)pos, (void*)cpos}) cudaFreeAsync(p, s);
+  TRY(rc);
+  P.num_prd_lists = nl;
   P.num_hub_chunks = nc;
   P.hub_gen = ctx->layout_gen;
   return GRD_OK;
@@ -402,7 +454,7 @@ static bool diff_aggregates(const grd_ctx* ctx) {
 // Kernels of the edge-map of one round in each mode.
 uint32_t grd_edge_map_launches(const grd_ctx* ctx, int mode) {
   const bool pr = ctx->algo == GRD_PR_DELTA;
-  const uint32_t hub_sums = ctx->pull.num_in_hubs ? 2 : 0;  // delta PageRank's in-hub chunk sums
+  const uint32_t hub_sums = ctx->pull.num_prd_lists ? 2 : 0;  // delta PageRank's chunked long-list sums
   if (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)
     return pr ? 1 + hub_sums : 1 + (ctx->pull.num_in_meds ? 1 : 0) + (ctx->pull.num_in_hubs ? 1 : 0);
   // push (NO_OFFLOAD too); PageRank's push adds the fixed-order sums
@@ -451,7 +503,7 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bo
     const uint32_t pull_hub_grid = std::min<uint32_t>(ctx->pull.num_in_hubs, grid_for(ctx, 8));
     const uint32_t pull_med_grid = std::min<uint32_t>((ctx->pull.num_in_meds + 7) / 8, grid_for(ctx, 8));
     const PullState& PS = ctx->pull;
-    const PrHubs ph{PS.in_hubs, PS.hub_coff, PS.chunk_hub, PS.chunk_sum, PS.num_in_hubs, PS.num_hub_chunks};
+    const PrHubs ph{PS.prd_lists, PS.hub_coff, PS.chunk_hub, PS.chunk_sum, PS.num_prd_lists, PS.num_hub_chunks};
     const uint32_t hsum_grid = std::max<uint32_t>(1, std::min<uint32_t>((ph.nh + 7) / 8, grid_for(ctx, 8)));
     if (A == A_PR_DELTA && (mode == RM_PULL_BITVEC || mode == RM_PULL_LIST)) {  // the fixed-order sums
       if (mode == RM_PULL_LIST)

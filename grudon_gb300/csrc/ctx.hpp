@@ -31,6 +31,8 @@ struct PrPullState {
   float* hot_val = nullptr;      // [H] contributions of the hot sources
   double* resid_part = nullptr;  // [update blocks] residual partial sums
   uint32_t update_blocks = 0;
+  char* scratch = nullptr;       // set-up scratch, kept between set-ups
+  size_t scratch_cap = 0;
 };
 
 struct PullState {
@@ -39,8 +41,11 @@ struct PullState {
   grd::HubChunkD* in_meds = nullptr;  // destination slots with medium in-lists
   uint32_t num_in_meds = 0;
   uint64_t edges = 0;                 // in-edges read since init
-  // Delta PageRank's in-hub sums (32-edge chunks summed grid-wide): the
-  // first chunk of each hub, the hub of each chunk, the chunk sums.
+  // Delta PageRank's sums of lists of more than 32 in-edges (32-edge chunks
+  // summed grid-wide): the lists (slot, first edge, end), the first chunk of
+  // each, the list of each chunk, the chunk sums.
+  grd::HubChunkD* prd_lists = nullptr;
+  uint32_t num_prd_lists = 0, prd_list_cap = 0;
   uint32_t* hub_coff = nullptr;
   uint32_t* chunk_hub = nullptr;
   float* chunk_sum = nullptr;
@@ -95,6 +100,13 @@ struct grd_ctx {
   uint8_t* wgt8_dev = nullptr;     // their device staging copy
   unsigned char* h_small = nullptr;  // pinned small tables of the upload (hubs, tiles, partitions)
   grd_policy_model* policy_dev = nullptr;  // learned round policy (device copy)
+  // grd_sssp_multi (msssp.cu): 64 distance lanes per vertex, the lane masks,
+  // the active list with its degree prefix, the source-major output copy
+  uint32_t* ms_dist = nullptr;
+  unsigned long long* ms_mask = nullptr;
+  uint32_t* ms_list = nullptr;
+  uint32_t* ms_out = nullptr;
+  size_t ms_out_cap = 0;
   unsigned long long* verify_buf = nullptr;  // grd_verify per-block top ranks
   size_t verify_cap = 0;
   bool has_policy = false;
@@ -148,7 +160,7 @@ void grd_prof_mark(grd_ctx* ctx, int i);
 void grd_prof_collect(grd_ctx* ctx);
 void grd_ctx_release_extras(grd_ctx* ctx);
 int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks);
-// Delta PageRank's in-hub chunk tables for the resident layout (abi.cu).
+// Delta PageRank's chunked long-list tables for the resident layout (abi.cu).
 int grd_pr_delta_hubs(grd_ctx* ctx);
 int grd_upload_layout(grd_ctx* ctx);
 int grd_ensure_in_edges(grd_ctx* ctx);

@@ -1566,31 +1566,73 @@ __device__ __forceinline__ float pr_delta_sum_warp(const DevGraph& g, const DevS
   const uint32_t lane = lane_id();
   const uint32_t a = __ldg(&g.in_off[d]), b = __ldg(&g.in_off[d + 1]);
   float acc = 0.0f;
-  for (uint32_t c = a; c < b; c += 32) {
-    const uint32_t e = c + lane;
-    float x = 0.0f;
-    if (e < b) {
-      const uint32_t src = __ldg(&g.in_src[e]);
-      if (test_bit(st.FB, src)) x = __uint_as_float(st.mprop[src]);
+  for (uint32_t c = a; c < b; c += 4 * 32) {  // four chunks' loads in flight
+    uint32_t src[4];
+    float x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t e = c + 32u * q + lane;
+      src[q] = e < b ? __ldg(&g.in_src[e]) : 0xFFFFFFFFu;
     }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) x = __fadd_rn(x, __shfl_xor_sync(FULL, x, o));
-    acc = __fadd_rn(acc, x);
+    for (int q = 0; q < 4; ++q)
+      x[q] = (src[q] != 0xFFFFFFFFu && test_bit(st.FB, src[q])) ? __uint_as_float(st.mprop[src[q]]) : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) x[q] = __fadd_rn(x[q], __shfl_xor_sync(FULL, x[q], o));
+      if (c + 32u * q < b) acc = __fadd_rn(acc, x[q]);  // chunks past the list's end do not exist
+    }
   }
   return acc;
 }
 
-// In-lists longer than K_PULL_HUB (the in-hubs) are summed grid-wide: every
-// 32-edge chunk by its own warp into a scratch array, then the chunk sums of
-// each list in chunk order by one thread -- the same order, in parallel.
+// The same sum of a list of at most 32 in-edges by one lane: the halving
+// tree run on registers gives the bits of the xor butterfly, and 0 + x = x.
+__device__ __forceinline__ float pr_delta_sum_lane(const DevGraph& g, const DevState& st, uint32_t a, uint32_t n) {
+  float x[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    x[i] = 0.0f;
+    if ((uint32_t)i < n) {
+      const uint32_t src = __ldg(&g.in_src[a + i]);
+      if (test_bit(st.FB, src)) x[i] = __uint_as_float(st.mprop[src]);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1)
+#pragma unroll
+    for (int i = 0; i < o; ++i) x[i] = __fadd_rn(x[i], x[i + o]);
+  return __fadd_rn(0.0f, x[0]);
+}
+
+// Lists of more than 32 in-edges are summed grid-wide: every 32-edge chunk
+// by its own warp into a scratch array, then each list's chunk sums in chunk
+// order by one warp -- the same order, with the whole GPU on the chunks.
+constexpr uint32_t K_PRD_SHORT = 32;
+
 __device__ __forceinline__ bool pr_delta_long(const DevGraph& g, uint32_t d) {
-  return __ldg(&g.in_off[d + 1]) - __ldg(&g.in_off[d]) > K_PULL_HUB;
+  return __ldg(&g.in_off[d + 1]) - __ldg(&g.in_off[d]) > K_PRD_SHORT;
+}
+
+// Every lane with `want` gets the fixed-order sum of its slot d when the list
+// is short (at most 32 in-edges, summed by the lane itself); *long_list tells
+// the lanes whose list the grid-wide path sums.
+__device__ __forceinline__ float pr_delta_sum_slots(const DevGraph& g, const DevState& st, uint32_t d, bool want,
+                                                    bool* long_list) {
+  uint32_t a = 0, n = 0;
+  if (want) {
+    a = __ldg(&g.in_off[d]);
+    n = __ldg(&g.in_off[d + 1]) - a;
+  }
+  *long_list = want && n > K_PRD_SHORT;
+  return (want && n <= K_PRD_SHORT) ? pr_delta_sum_lane(g, st, a, n) : 0.0f;
 }
 
 struct PrHubs {
-  const HubChunkD* hubs;      // (slot, e0, e1) of every in-hub
-  const uint32_t* coff;       // [nh + 1] first chunk of each hub
-  const uint32_t* chunk_hub;  // [nc] hub of each chunk
+  const HubChunkD* hubs;      // (slot, e0, e1) of every list of more than 32 in-edges
+  const uint32_t* coff;       // [nh + 1] first chunk of each such list
+  const uint32_t* chunk_hub;  // [nc] list of each chunk
   float* csum;                // [nc] chunk sums
   uint32_t nh, nc;
 };
@@ -1627,8 +1669,9 @@ __global__ void __launch_bounds__(256) k_pr_delta_hub_chunks(DevGraph g, DevStat
   }
 }
 
-// One warp per hub: the chunk sums are loaded 128 at a time (coalesced) and
-// added in chunk order through shuffles (every lane keeps the same sum).
+// One warp per long list: the chunk sums are loaded 128 at a time
+// (coalesced) and added in chunk order through shuffles (every lane keeps the
+// same sum).
 template <int kMode, bool kList>
 __global__ void __launch_bounds__(256) k_pr_delta_hub_sum(DevGraph g, DevState st, PrHubs h) {
   const uint32_t lane = lane_id();
@@ -1672,13 +1715,10 @@ static __global__ void __launch_bounds__(256) k_pr_delta_resum_bits(DevGraph g, 
   const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
   for (uint64_t w = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nwords; w += nw) {
     const uint32_t s = (uint32_t)(w * 32) + lane;
-    uint32_t m = __ballot_sync(FULL, __ldcg(&st.mupd[s]) != 0u && !pr_delta_long(g, s));
-    while (m) {
-      const uint32_t d = (uint32_t)(w * 32) + (uint32_t)(__ffs(m) - 1);
-      m &= m - 1;
-      const float v = pr_delta_sum_warp(g, st, d);
-      if (lane == 0) st.mupd[d] = __float_as_uint(v);
-    }
+    const bool touched = __ldcg(&st.mupd[s]) != 0u;
+    bool lng;
+    const float v = pr_delta_sum_slots(g, st, s, touched, &lng);
+    if (touched && !lng) st.mupd[s] = __float_as_uint(v);
   }
 }
 
@@ -1686,11 +1726,12 @@ static __global__ void __launch_bounds__(256) k_pr_delta_resum_bits(DevGraph g, 
 static __global__ void __launch_bounds__(256) k_pr_delta_resum_list(DevGraph g, DevState st) {
   const uint32_t n = __ldcg(&st.lc[L_DL]);
   const uint32_t nw = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < n; j += nw) {
-    const uint32_t d = st.DL[j];
-    if (pr_delta_long(g, d)) continue;  // k_pr_delta_hub_* sum it
-    const float v = pr_delta_sum_warp(g, st, d);
-    if (lane_id() == 0) st.mupd[d] = __float_as_uint(v);
+  for (uint32_t j0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; j0 < n; j0 += nw * 32) {
+    const uint32_t j = j0 + lane_id();
+    const uint32_t d = j < n ? st.DL[j] : 0u;
+    bool lng;
+    const float v = pr_delta_sum_slots(g, st, d, j < n, &lng);
+    if (j < n && !lng) st.mupd[d] = __float_as_uint(v);  // in-hubs: k_pr_delta_hub_*
   }
 }
 
@@ -1704,21 +1745,13 @@ __global__ void __launch_bounds__(256) k_pr_delta_pull(DevGraph g, DevState st) 
   const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
   for (uint64_t w = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nwords; w += nw) {
     const uint32_t s = (uint32_t)(w * 32) + lane;
-    const uint32_t deg = __ldg(&g.in_off[s + 1]) - __ldg(&g.in_off[s]);
-    uint32_t m = __ballot_sync(FULL, deg > 0 && deg <= K_PULL_HUB);  // long lists: k_pr_delta_hub_*
-    uint32_t dirty = 0;
-    while (m) {
-      const uint32_t i = (uint32_t)(__ffs(m) - 1);
-      m &= m - 1;
-      const uint32_t d = (uint32_t)(w * 32) + i;
-      const float v = pr_delta_sum_warp(g, st, d);
-      if (v > 0.0f) {  // the same in every lane
-        if (lane == 0) st.mupd[d] = __float_as_uint(v);
-        dirty |= 1u << i;
-      }
-    }
-    if (lane == 0) st.MD[w] = dirty;
-    if (kList && ((dirty >> lane) & 1u)) list_append(st.DL, st.lc + L_DL, s);
+    bool lng;
+    const float v = pr_delta_sum_slots(g, st, s, true, &lng);  // an empty list sums to 0: not dirty
+    const bool dirty = !lng && v > 0.0f;
+    if (dirty) st.mupd[s] = __float_as_uint(v);
+    const uint32_t m = __ballot_sync(FULL, dirty);
+    if (lane == 0) st.MD[w] = m;  // in-hubs OR their bits in afterwards (k_pr_delta_hub_sum)
+    if (kList && dirty) list_append(st.DL, st.lc + L_DL, s);
   }
 }
 
@@ -2022,13 +2055,24 @@ __device__ __forceinline__ void tiny_round(const DevGraph& g, const DevState& st
   __syncthreads();
   if (A == A_PR_DELTA && !kCompute) {  // the listed slots get the fixed-order sum
     const uint32_t nd = __ldcg(&st.lc[L_DL]);
-    for (uint32_t j = tid >> 5; j < nd; j += K_TINY_THREADS / 32) {
-      const uint32_t d = st.DL[j];
-      if (pr_delta_long(g, d)) continue;
-      const float v = pr_delta_sum_warp(g, st, d);
-      if (lane_id() == 0) st.mupd[d] = __float_as_uint(v);
+    for (uint32_t j0 = (tid >> 5) * 32; j0 < nd; j0 += K_TINY_THREADS) {
+      const uint32_t j = j0 + lane_id();
+      const uint32_t d = j < nd ? st.DL[j] : 0u;
+      bool lng;
+      const float v = pr_delta_sum_slots(g, st, d, j < nd, &lng);
+      if (j < nd && !lng) st.mupd[d] = __float_as_uint(v);
+      // lists of 33..1024 in-edges: the whole warp, one after another
+      uint32_t m = __ballot_sync(FULL, lng && __ldg(&g.in_off[d + 1]) - __ldg(&g.in_off[d]) <= K_PULL_HUB);
+      while (m) {
+        const int l = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t dl = __shfl_sync(FULL, d, l);
+        const float x = pr_delta_sum_warp(g, st, dl);
+        if (lane_id() == 0) st.mupd[dl] = __float_as_uint(x);
+      }
     }
-    // long lists: every warp sums chunks, thread 0 adds them in order
+    // lists of more than 1024 in-edges: every warp sums chunks, thread 0 adds
+    // them in order
     __shared__ uint32_t s_long[K_TINY_THREADS];
     __shared__ uint32_t s_nlong;
     __shared__ float s_cs[K_TINY_THREADS];
@@ -2039,7 +2083,7 @@ __device__ __forceinline__ void tiny_round(const DevGraph& g, const DevState& st
       __syncthreads();
       if (b + tid < nd) {
         const uint32_t d = st.DL[b + tid];
-        if (pr_delta_long(g, d)) s_long[atomicAdd(&s_nlong, 1u)] = d;
+        if (__ldg(&g.in_off[d + 1]) - __ldg(&g.in_off[d]) > K_PULL_HUB) s_long[atomicAdd(&s_nlong, 1u)] = d;
       }
       __syncthreads();
       const uint32_t nl = s_nlong;

@@ -584,25 +584,37 @@ __global__ void __launch_bounds__(256) k_pr_tile_count(const uint32_t* start_bit
   }
 }
 
-// Stream-ordered scratch, released when the set-up returns.
+// Set-up scratch: slices of one device buffer kept by the ctx (allocated at
+// the first set-up, and again only if a layout ever needs more), so that a
+// set-up after every upload allocates nothing.
 struct Tmp {
   grd_ctx* ctx;
-  std::vector<void*> ptrs;
+  char* base = nullptr;
+  size_t cap = 0, used = 0;
   explicit Tmp(grd_ctx* c) : ctx(c) {}
-  ~Tmp() {
-    for (void* p : ptrs) cudaFreeAsync(p, ctx->stream);
+  int reserve(size_t words) {
+    const size_t bytes = words * sizeof(uint32_t) + 64 * 256;  // slices are 256-byte aligned
+    PrPullState& P = ctx->pr;
+    if (P.scratch_cap < bytes) {
+      void* d = nullptr;
+      TRY(grd_dev_alloc_bytes(ctx, &d, bytes));
+      P.scratch = static_cast<char*>(d);
+      P.scratch_cap = bytes;
+    }
+    base = P.scratch;
+    cap = P.scratch_cap;
+    used = 0;
+    return GRD_OK;
   }
   template <class T>
   int get(T** p, size_t count) {
-    void* d = nullptr;
-    const cudaError_t e = cudaMallocAsync(&d, sizeof(T) * std::max<size_t>(count, 1), ctx->stream);
-    if (e != cudaSuccess) {
-      (void)cudaGetLastError();
-      ctx->err = std::string("PageRank set-up scratch: ") + cudaGetErrorString(e);
-      return GRD_E_OOM;
+    const size_t bytes = ((sizeof(T) * std::max<size_t>(count, 1)) + 255) / 256 * 256;
+    if (used + bytes > cap) {
+      ctx->err = "PageRank set-up scratch too small";
+      return GRD_E_INVALID;
     }
-    ptrs.push_back(d);
-    *p = static_cast<T*>(d);
+    *p = reinterpret_cast<T*>(base + used);
+    used += bytes;
     return GRD_OK;
   }
 };
@@ -656,6 +668,7 @@ int pr_prepare(grd_ctx* ctx) {
   }
 
   Tmp tmp(ctx);
+  TRY(tmp.reserve(2 * PR_HIST + (V / 32 + 2) + (V + 1) + V + 4 * S + 1 + (T + 1) + (E + 1)));
   // (1) hot set: the highest out-degrees, at most PR_HOT_CAP vertices, cut at
   // a histogram bucket boundary
   uint32_t *hist = nullptr;

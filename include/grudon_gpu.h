@@ -252,6 +252,22 @@ int grd_aggregate_values(grd_ctx* ctx, const uint32_t* gids,
 int grd_aggregate_values_noalloc(grd_ctx* ctx, const uint32_t* gids,
                                  const uint32_t* values, size_t n);
 
+/* SSSP from up to GRD_MS_MAX_SOURCES sources at once over the ctx's resident
+ * graph (the batched-sources workload): 64 distance lanes per vertex, and each
+ * round relaxes every edge once for all of its source's changed lanes, so
+ * the CSR is held and read once however many sources run.  Per lane this is
+ * the reference's SSSP (src/graph_algorithms/sssp.cpp:61-113, seeded at
+ * :40-46 with one source; here n) and the distances equal n single-source
+ * runs.  The ctx's algorithm (grd_set_algo) must be GRD_SSSP_HOP or
+ * GRD_SSSP_W, and grd_init must have run; sources may repeat.  dist_out
+ * receives n * V uint32 distances, source-major (UINT32_MAX: unreachable).
+ * Runs to convergence or params.max_rounds rounds; stats (may be null) gets
+ * rounds, converged and edges scanned.  Allocates its device arrays on the
+ * first call (about 280 B per vertex). */
+#define GRD_MS_MAX_SOURCES 64
+int grd_sssp_multi(grd_ctx* ctx, const uint32_t* sources, uint32_t n,
+                   uint32_t* dist_out, grd_stats* stats);
+
 /* Full run: init() already called; loops rounds until the frontier is empty
  * or params.max_rounds.  flags: GRD_RUN_STRICT. */
 int grd_run(grd_ctx* ctx, uint32_t flags, grd_stats* stats);
