@@ -515,6 +515,8 @@ def bench_policy_offload(g, W, args, barrier, streams):
                           "pull_rounds_per_step": a["pull_rounds"] / args.steps,
                           "results_bit_identical": all(bool((x == y).all()) for x, y in zip(base_props, props))}
         out["learned_speedup_vs_fixed"] = out["learned"]["value"] / out["fixed"]["value"]
+    if model is not None:
+        out["grid4096_cc"] = policy_grid(g, model)
     W.set_policy(g.GRD_POLICY_FIXED, offload=g.GRD_OFFLOAD_ENGINE)
     s, a = timed_steps(W, args, barrier, streams, which=(0, 1))
     sts = [(c.init(), c.run())[1] for c in (W.cc, W.ss)]
@@ -525,6 +527,36 @@ def bench_policy_offload(g, W, args, barrier, streams):
                "no_offload_rounds_per_step": [st["no_offload_rounds"] for st in sts],
                "results_bit_identical": all(bool((x == y).all()) for x, y in zip(base_props, props))}
     return {"cc_sssp": out, "model": "grudon_gb300/policy_model.json" if model is not None else None}, offload
+
+
+def policy_grid(g, model) -> dict:
+    """The learned policy on a graph family where pull rounds pay: CC on the
+    held-out 4096 x 4096 grid (not a training graph), 1000 rounds, 1C+3M,
+    fixed rule against the shipped model; results must be bit-identical."""
+    import numpy as np
+    import torch
+    G = g.Graph.grid(4096, seed=4096)
+    res, outs = {}, []
+    with g.Context(G, G.partition_edge_balanced(NUM_MEMORY), NUM_MEMORY) as ctx:
+        s = torch.cuda.ExternalStream(ctx.stream())
+        for name, pol in (("fixed", g.GRD_POLICY_FIXED), ("learned", g.GRD_POLICY_LEARNED)):
+            ctx.set_algo(g.GRD_CC, policy=pol, max_rounds=1000)
+            ctx.set_policy(model if pol == g.GRD_POLICY_LEARNED else None)
+            best, st = float("inf"), None
+            for _ in range(2):
+                ctx.init()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                st = ctx.run()
+                e1.record(s)
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            outs.append(ctx.read_props())
+            res[name] = {"ms": best, "rounds": st["rounds"], "push_rounds": st["push_rounds"],
+                         "pull_rounds": st["pull_rounds"]}
+    res["learned_speedup_vs_fixed"] = res["fixed"]["ms"] / res["learned"]["ms"]
+    res["results_bit_identical"] = bool(np.array_equal(outs[0], outs[1]))
+    return res
 
 
 def bench_ingest(g, W, args, local, barrier, dev) -> dict:
@@ -575,33 +607,44 @@ def bench_batch(g, args, local) -> dict:
     E1 = sum(x.num_edges for x in sym) + 20 * sum(x.num_edges for x in dirg)
     _, _, plain_s = B.run_plain_graphs(sym, dirg, 20, local)
     Uc, Up = B.Union(sym), B.Union(dirg)
+    reps = 3
+
+    def time_union(cc_kw, cc_policy, model_, num_memory):
+        """One union per algorithm: CC with the given schedule and policy, 20
+        PageRank iterations; seconds per (CC + PageRank) pass, best of reps."""
+        pc = Uc.graph.partition_edge_balanced(num_memory) if num_memory > 1 else None
+        pp = Up.graph.partition_edge_balanced(num_memory) if num_memory > 1 else None
+        with g.Context(Uc.graph, pc, num_memory, local) as cc_, g.Context(Up.graph, pp, num_memory, local) as pr_:
+            cc_.set_algo(g.GRD_CC, policy=cc_policy, **cc_kw)
+            cc_.set_policy(model_)
+            pr_.set_algo(g.GRD_PR_PULL, max_rounds=20, tolerance=0.0)
+            best_ = float("inf")
+            for k in range(reps + 1):
+                t0_ = time.perf_counter()
+                for c_ in (cc_, pr_):
+                    c_.init()
+                    c_.run()
+                cc_.synchronize()
+                if k:
+                    best_ = min(best_, time.perf_counter() - t0_)
+            return best_, cc_.read_props()
+
+    # batching alone: the unions with the library defaults and the fixed rule
+    union_fixed_s, props_fixed = time_union({}, g.GRD_POLICY_FIXED, None, 1)
     tune_cc = autotune.tune(Uc.graph, g.GRD_CC, lambda c: c.init(), device=local, reps=2)
     best = tune_cc.best
-    part = Uc.graph.partition_edge_balanced(best.num_memory) if best.num_memory > 1 else None
     model = load_policy_model()
     pol = g.GRD_POLICY_LEARNED if model is not None else g.GRD_POLICY_FIXED
-    ctx_c = g.Context(Uc.graph, part, best.num_memory, local)
-    ctx_c.set_algo(g.GRD_CC, policy=pol, **best.params())
-    ctx_c.set_policy(model)
-    part = Up.graph.partition_edge_balanced(best.num_memory) if best.num_memory > 1 else None
-    ctx_p = g.Context(Up.graph, part, best.num_memory, local)
-    ctx_p.set_algo(g.GRD_PR_PULL, max_rounds=20, tolerance=0.0)
-    for c in (ctx_c, ctx_p):  # warm-up
-        c.init()
-        c.run()
-    reps = 3
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        for c in (ctx_c, ctx_p):
-            c.init()
-            c.run()
-    ctx_c.synchronize()
-    batched_s = (time.perf_counter() - t0) / reps
-    ctx_c.close()
-    ctx_p.close()
+    # + the autotuned schedule, then + the learned round policy
+    union_tuned_s, _ = time_union(best.params(), g.GRD_POLICY_FIXED, None, best.num_memory)
+    batched_s, props_learned = time_union(best.params(), pol, model, best.num_memory)
     part1 = {"graphs": len(spec), "vertices": int(Uc.sizes.sum()), "edges_cc": Uc.graph.num_edges,
              "edges_pr": Up.graph.num_edges, "generate_s": t_gen,
              "plain_s": plain_s, "batched_s": batched_s, "speedup": plain_s / batched_s,
+             "union_fixed_s": union_fixed_s, "union_tuned_s": union_tuned_s,
+             "speedup_batching": plain_s / union_fixed_s, "speedup_autotune": union_fixed_s / union_tuned_s,
+             "speedup_learned_policy": union_tuned_s / batched_s,
+             "results_bit_identical": bool(np.array_equal(props_fixed, props_learned)),
              "batched_gteps": E1 / batched_s / 1e9, "plain_gteps": E1 / plain_s / 1e9,
              "autotuned": best.__dict__, "tune_table_ms": [round(r["ms"], 3) for r in tune_cc.table]}
 
@@ -645,6 +688,8 @@ def bench_batch(g, args, local) -> dict:
     total_plain, total_batched = plain_s + plain2, batched_s + batched2
     return {"part1_graphs": part1, "part2_sssp_sources": part2,
             "end_to_end_speedup": total_plain / total_batched,
+            "shares": "part 1 splits into batching (plain -> one union per algorithm, library defaults, fixed "
+                      "rule), the autotuned schedule and the learned policy; part 2's gain is the shared CSR",
             "policy": "learned" if model is not None else "fixed",
             "note": "plain: one ctx per graph (per source) with the fixed per-round rule; batched: part 1 one "
                     "union per algorithm, autotuned schedule and the learned round policy (CC; PageRank is "
