@@ -516,7 +516,7 @@ def bench_policy_offload(g, W, args, barrier, streams):
                           "results_bit_identical": all(bool((x == y).all()) for x, y in zip(base_props, props))}
         out["learned_speedup_vs_fixed"] = out["learned"]["value"] / out["fixed"]["value"]
     if model is not None:
-        out["grid4096_cc"] = policy_grid(g, model)
+        out["held_out"] = policy_held_out(g, model)
     W.set_policy(g.GRD_POLICY_FIXED, offload=g.GRD_OFFLOAD_ENGINE)
     s, a = timed_steps(W, args, barrier, streams, which=(0, 1))
     sts = [(c.init(), c.run())[1] for c in (W.cc, W.ss)]
@@ -529,21 +529,21 @@ def bench_policy_offload(g, W, args, barrier, streams):
     return {"cc_sssp": out, "model": "grudon_gb300/policy_model.json" if model is not None else None}, offload
 
 
-def policy_grid(g, model) -> dict:
-    """The learned policy on a graph family where pull rounds pay: CC on the
-    held-out 4096 x 4096 grid (not a training graph), 1000 rounds, 1C+3M,
-    fixed rule against the shipped model; results must be bit-identical."""
+def policy_leg(g, model, G, algo, max_rounds=None, reps=2) -> dict:
+    """The fixed rule against the shipped model on one graph that no model
+    was trained on: 1C+3M, device-driven runs, best of `reps`; the results
+    (labels, distances or ranks) must be bit-identical."""
     import numpy as np
     import torch
-    G = g.Graph.grid(4096, seed=4096)
     res, outs = {}, []
+    kw = {} if max_rounds is None else {"max_rounds": max_rounds}
     with g.Context(G, G.partition_edge_balanced(NUM_MEMORY), NUM_MEMORY) as ctx:
         s = torch.cuda.ExternalStream(ctx.stream())
         for name, pol in (("fixed", g.GRD_POLICY_FIXED), ("learned", g.GRD_POLICY_LEARNED)):
-            ctx.set_algo(g.GRD_CC, policy=pol, max_rounds=1000)
+            ctx.set_algo(algo, policy=pol, **kw)
             ctx.set_policy(model if pol == g.GRD_POLICY_LEARNED else None)
             best, st = float("inf"), None
-            for _ in range(2):
+            for _ in range(reps):
                 ctx.init()
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record(s)
@@ -551,12 +551,24 @@ def policy_grid(g, model) -> dict:
                 e1.record(s)
                 e1.synchronize()
                 best = min(best, e0.elapsed_time(e1))
-            outs.append(ctx.read_props())
+            outs.append(ctx.read_ranks() if algo == g.GRD_PR_DELTA else ctx.read_props())
             res[name] = {"ms": best, "rounds": st["rounds"], "push_rounds": st["push_rounds"],
                          "pull_rounds": st["pull_rounds"]}
     res["learned_speedup_vs_fixed"] = res["fixed"]["ms"] / res["learned"]["ms"]
     res["results_bit_identical"] = bool(np.array_equal(outs[0], outs[1]))
     return res
+
+
+def policy_held_out(g, model) -> dict:
+    """The learned policy on two held-out workloads: CC on a 3000 x 3000 grid
+    (weights in [1,255], 1000 rounds) and delta PageRank (the reference's own
+    algorithm, which the fixed rule runs push-only) on the benchmark's
+    RMAT-22 directed graph."""
+    a, b, c = RMAT_ABC
+    out = {"grid3000_cc": policy_leg(g, model, g.Graph.grid(3000, seed=3000), g.GRD_CC, max_rounds=1000)}
+    G = g.Graph.rmat(22, EF, a, b, c, seed=g.rmat_seed(22, EF))
+    out["rmat22_pr_delta"] = policy_leg(g, model, G, g.GRD_PR_DELTA)
+    return out
 
 
 def bench_ingest(g, W, args, local, barrier, dev) -> dict:

@@ -217,13 +217,17 @@ def test_fused_inference_follows_the_model(gpu):
 def test_trained_policy_gain_on_held_out_graphs(gpu):
     """Train on the plain method's timings of small RMAT and grid graphs;
     on held-out graphs the learned choices' measured time is compared with
-    the fixed rule's on the same measured table."""
+    the fixed rule's on the same measured table.  The grid family (pull
+    rounds with list sync beat the push there) and delta PageRank (the fixed
+    rule never pulls it) must gain; RMAT CC/SSSP, where the fixed rule is
+    already near the per-round best, must not lose more than 5 %."""
     train_tabs = []
     for s in (11, 12, 13):
         Gs = g.Graph.rmat(s, 16, symmetrize=True)
         Gw = g.Graph.rmat(s, 16, weighted=True)
         train_tabs.append(P.collect(Gs, g.GRD_CC, f"cc-rmat{s}", reps=2))
         train_tabs.append(P.collect(Gw, g.GRD_SSSP_W, f"sssp-rmat{s}", reps=2))
+        train_tabs.append(P.collect(Gw, g.GRD_PR_DELTA, f"pr-rmat{s}", reps=2))
     for k in (48, 96, 128):
         Gg = g.Graph.grid(k, seed=k)
         train_tabs.append(P.collect(Gg, g.GRD_SSSP_W, f"sssp-grid{k}", reps=2, stride=2))
@@ -232,16 +236,22 @@ def test_trained_policy_gain_on_held_out_graphs(gpu):
     m, curve = P.train(x, y, mask, steps=3000, lr=2e-3, seed=5)
     assert curve[-1] < curve[0]
     Gh = g.Graph.grid(112, seed=1)
+    Gw = g.Graph.rmat(14, 16, weighted=True)
     held = [P.collect(g.Graph.rmat(14, 16, symmetrize=True), g.GRD_CC, "cc-rmat14", reps=2),
-            P.collect(g.Graph.rmat(14, 16, weighted=True), g.GRD_SSSP_W, "sssp-rmat14", reps=2),
+            P.collect(Gw, g.GRD_SSSP_W, "sssp-rmat14", reps=2), P.collect(Gw, g.GRD_PR_DELTA, "pr-rmat14", reps=2),
             P.collect(Gh, g.GRD_SSSP_W, "sssp-grid112", reps=2), P.collect(Gh, g.GRD_CC, "cc-grid112", reps=2)]
-    tot = {"chosen_ms": 0.0, "fixed_ms": 0.0, "best_ms": 0.0}
+    fam = {"all": ("",), "grid": ("grid",), "pr": ("pr-",), "rmat-cc-sssp": ("cc-rmat", "sssp-rmat")}
+    tot = {f: {"chosen_ms": 0.0, "fixed_ms": 0.0, "best_ms": 0.0} for f in fam}
     report = {}
     for t in held:
         r = P.table_totals(t, P.choose(m, t))
         report[t.name] = r
-        for k in tot:
-            tot[k] += r[k]
+        for f, keys in fam.items():
+            if any(k in t.name for k in keys):
+                for k in tot[f]:
+                    tot[f][k] += r[k]
     print(json.dumps({"held_out": report, "total": tot}, indent=1))
-    assert tot["best_ms"] <= tot["chosen_ms"]
-    assert tot["chosen_ms"] <= 1.05 * tot["fixed_ms"], tot
+    assert tot["all"]["best_ms"] <= tot["all"]["chosen_ms"]
+    assert tot["grid"]["chosen_ms"] < tot["grid"]["fixed_ms"], tot["grid"]
+    assert tot["pr"]["chosen_ms"] < tot["pr"]["fixed_ms"], tot["pr"]
+    assert tot["rmat-cc-sssp"]["chosen_ms"] <= 1.05 * tot["rmat-cc-sssp"]["fixed_ms"], tot["rmat-cc-sssp"]
