@@ -58,7 +58,9 @@ int dev_alloc_async(grd_ctx* ctx, T** p, size_t count) {
 template <class T>
 int upload(grd_ctx* ctx, T* dst, const std::vector<T>& src) {
   if (src.empty()) return GRD_OK;
-  CK(cudaMemcpyAsync(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, ctx->stream));
+  const auto it = ctx->pinned_twin.find(src.data());
+  const void* from = it != ctx->pinned_twin.end() ? it->second : (const void*)src.data();
+  CK(cudaMemcpyAsync(dst, from, sizeof(T) * src.size(), cudaMemcpyHostToDevice, ctx->stream));
   ctx->upload_bytes += sizeof(T) * src.size();
   return GRD_OK;
 }
@@ -151,13 +153,11 @@ static __global__ void __launch_bounds__(256) k_widen_weights(const uint8_t* __r
     w[i] = w8[i];
 }
 
-int grd_upload_layout(grd_ctx* ctx) {
+// The out-edge columns and the edge weights of both views (out-edge weights
+// below 256 travel as bytes and are widened on the device).
+static int upload_out_edges(grd_ctx* ctx) {
   const Layout& L = ctx->L;
   DevGraph& g = ctx->g;
-  ctx->upload_bytes = 0;
-  ctx->layout_gen++;  // derived arrays (PR_PULL) are rebuilt from the new copy
-  TRY(upload(ctx, (uint32_t*)g.slot_gid, L.slot_gid));
-  TRY(upload(ctx, (uint32_t*)g.row_off, L.row_off));
   TRY(upload(ctx, (uint32_t*)g.col, L.col));
   if (L.weighted && !ctx->wgt8_host.empty()) {
     TRY(upload(ctx, ctx->wgt8_dev, ctx->wgt8_host));
@@ -166,6 +166,34 @@ int grd_upload_layout(grd_ctx* ctx) {
   } else if (L.weighted) {
     TRY(upload(ctx, (uint32_t*)g.wgt, L.wgt));
   }
+  if (ctx->in_edges_alloc && L.weighted) TRY(upload(ctx, (uint32_t*)g.in_wgt, L.in_wgt));
+  ctx->out_edges_stale = false;
+  return GRD_OK;
+}
+
+int grd_ensure_out_edges(grd_ctx* ctx) {
+  if (!ctx->out_edges_stale) return GRD_OK;
+  const uint64_t b = ctx->upload_bytes;
+  TRY(upload_out_edges(ctx));
+  ctx->upload_bytes = b;  // not part of the caller's upload
+  return GRD_OK;
+}
+
+int grd_upload_layout(grd_ctx* ctx) {
+  const Layout& L = ctx->L;
+  DevGraph& g = ctx->g;
+  ctx->upload_bytes = 0;
+  ctx->layout_gen++;  // derived arrays (PR_PULL) are rebuilt from the new copy
+  TRY(upload(ctx, (uint32_t*)g.slot_gid, L.slot_gid));
+  TRY(upload(ctx, (uint32_t*)g.row_off, L.row_off));
+  // A Jacobi PageRank ctx reads the in-edge sources, the row offsets
+  // (out-degrees) and the slot map only: its out-edges and weights follow
+  // when another algorithm or a layout read needs them (grd_ensure_out_edges).
+  const bool pr_pull_only = ctx->algo == GRD_PR_PULL && ctx->in_edges_alloc;
+  if (pr_pull_only)
+    ctx->out_edges_stale = true;
+  else
+    TRY(upload_out_edges(ctx));
   // the small tables, from their pinned copy (a pageable copy would block
   // the caller until the stream's earlier copies are done)
   static_assert(sizeof(HubChunk) == sizeof(HubChunkD), "hub chunk layout");
@@ -183,7 +211,6 @@ int grd_upload_layout(grd_ctx* ctx) {
   if (ctx->in_edges_alloc) {
     TRY(upload(ctx, (uint32_t*)g.in_off, L.in_off));
     TRY(upload(ctx, (uint32_t*)g.in_src, L.in_src));
-    if (L.weighted) TRY(upload(ctx, (uint32_t*)g.in_wgt, L.in_wgt));
   }
   // stream-ordered: the pinned host arrays belong to the ctx and outlive the
   // copies; the small pageable ones are staged before the copy call returns
@@ -199,7 +226,8 @@ int grd_ensure_in_edges(grd_ctx* ctx) {
   TRY(dev_alloc(ctx, (uint32_t**)&ctx->g.in_src, std::max<size_t>(L.E, 4)));
   if (L.weighted) TRY(dev_alloc(ctx, (uint32_t**)&ctx->g.in_wgt, std::max<size_t>(L.E, 4)));
   ctx->in_edges_alloc = true;
-  grd_pin_host(ctx, {&ctx->L.in_off, &ctx->L.in_src, &ctx->L.in_wgt});
+  for (const auto* v : {&ctx->L.in_off, &ctx->L.in_src, &ctx->L.in_wgt})
+    grd_pin_twin(ctx, v->data(), v->size() * sizeof(uint32_t));
   TRY(upload(ctx, (uint32_t*)ctx->g.in_off, L.in_off));
   TRY(upload(ctx, (uint32_t*)ctx->g.in_src, L.in_src));
   if (L.weighted) TRY(upload(ctx, (uint32_t*)ctx->g.in_wgt, L.in_wgt));
@@ -972,7 +1000,7 @@ void grd_ctx_destroy(grd_ctx* ctx) {
   grd_ctx_release_extras(ctx);
   grd_graph_release(ctx);
   for (void* p : ctx->allocs) cudaFree(p);
-  for (void* p : ctx->host_registered) cudaHostUnregister(p);
+  for (auto& t : ctx->pinned_twin) cudaFreeHost(t.second);
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
@@ -1047,6 +1075,7 @@ int grd_set_algo(grd_ctx* ctx, int algo, const grd_params* params) {
     return GRD_E_INVALID;
   }
   CK(cudaSetDevice(ctx->device));
+  if (algo != GRD_PR_PULL) TRY(grd_ensure_out_edges(ctx));
   if (algo == GRD_PR_PULL || algo == GRD_PR_DELTA /* fixed-order sums */ || p.direction == GRD_DIR_PULL ||
       (p.policy == GRD_POLICY_LEARNED && p.direction == GRD_DIR_AUTO)) {  // the model may pull
     int rc = grd_ensure_in_edges(ctx);
@@ -1495,6 +1524,7 @@ int grd_read_layout(grd_ctx* ctx, int which, void* host, size_t cap_bytes, size_
     return GRD_E_INVALID;
   }
   CK(cudaSetDevice(ctx->device));
+  if (which == GRD_LAYOUT_COL || which == GRD_LAYOUT_WGT || which == GRD_LAYOUT_IN_WGT) TRY(grd_ensure_out_edges(ctx));
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(host, src, n, cudaMemcpyDeviceToHost));
   return GRD_OK;
@@ -1566,8 +1596,12 @@ int grd_ctx_init_device(grd_ctx* ctx) {
     TRY(grd_dev_alloc_bytes(ctx, &p, L.E));
     ctx->wgt8_dev = static_cast<uint8_t*>(p);
   }
-  grd_pin_host(ctx, {&ctx->L.col, &ctx->L.wgt, &ctx->L.row_off, &ctx->L.slot_gid});
-  grd_pin_host_bytes(ctx, ctx->wgt8_host);
+  for (const auto* v : {&ctx->L.col, &ctx->L.row_off, &ctx->L.slot_gid})
+    grd_pin_twin(ctx, v->data(), v->size() * sizeof(uint32_t));
+  if (ctx->wgt8_host.empty())
+    grd_pin_twin(ctx, ctx->L.wgt.data(), ctx->L.wgt.size() * sizeof(uint32_t));
+  else
+    grd_pin_twin(ctx, ctx->wgt8_host.data(), ctx->wgt8_host.size());
   {  // pinned copy of the small tables: hubs, tile partitions, partition bases, sizes, owned counts
     const size_t nh = sizeof(HubChunk) * L.hubs.size(), nt = sizeof(uint32_t) * L.tile_part.size(),
                  nm = sizeof(uint32_t) * L.M;
@@ -1583,30 +1617,24 @@ int grd_ctx_init_device(grd_ctx* ctx) {
   return grd_upload_layout(ctx);
 }
 
-// Pins large host layout arrays so grd_upload copies run at full
-// host->device bandwidth; pageable copies still work if pinning fails.
-void grd_pin_host_bytes(grd_ctx* ctx, std::vector<uint8_t>& v) {
-  if (v.size() < (1u << 20)) return;
-  if (cudaHostRegister(v.data(), v.size(), cudaHostRegisterDefault) == cudaSuccess) {
-    ctx->host_registered.push_back(v.data());
-  } else {
+// A pinned twin of a large host layout array: one copy into memory the driver
+// allocated pinned (cudaHostAlloc), made once, from which every grd_upload
+// reads.  Such memory keeps its full host->device rate even when the copy
+// comes after the buffer sat idle, where memory pinned in place
+// (cudaHostRegister) ran a cold copy at a fraction of it.  The layout arrays
+// never change after creation, so the twin stays equal to them.  Without a
+// twin (a small array, or pinned memory refused) uploads read the pageable
+// array.
+void grd_pin_twin(grd_ctx* ctx, const void* data, size_t bytes) {
+  if (bytes < (1u << 20) || ctx->pinned_twin.count(data)) return;
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
     (void)cudaGetLastError();
-    std::fprintf(stderr, "grudon: pinning %zu B of host weights failed; uploads use pageable copies\n", v.size());
+    std::fprintf(stderr, "grudon: no pinned twin for %zu B of host layout; uploads read pageable memory\n", bytes);
+    return;
   }
-}
-
-void grd_pin_host(grd_ctx* ctx, std::initializer_list<std::vector<uint32_t>*> arrays) {
-  for (auto* v : arrays) {
-    if (v->size() * sizeof(uint32_t) < (1u << 20)) continue;
-    const cudaError_t e = cudaHostRegister(v->data(), v->size() * sizeof(uint32_t), cudaHostRegisterDefault);
-    if (e == cudaSuccess) {
-      ctx->host_registered.push_back(v->data());
-    } else {
-      (void)cudaGetLastError();
-      std::fprintf(stderr, "grudon: pinning %zu B of host layout failed (%s); uploads use pageable copies\n",
-                   v->size() * sizeof(uint32_t), cudaGetErrorString(e));
-    }
-  }
+  std::memcpy(p, data, bytes);
+  ctx->pinned_twin.emplace(data, p);
 }
 
 int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks) {

@@ -4,6 +4,7 @@
 
 #include <initializer_list>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/grudon_gpu.h"
@@ -75,6 +76,10 @@ struct grd_ctx {
   unsigned long long* h_seed = nullptr;      // = h_counters + NUM_COUNTERS
   uint64_t upload_bytes = 0;
   bool in_edges_alloc = false;
+  // Host layout: the out-edge columns and the weights of both views were left
+  // out of the last upload (a PR_PULL ctx reads neither); uploaded again
+  // before anything reads them.
+  bool out_edges_stale = false;
   uint64_t layout_gen = 0;     // bumped whenever a layout array is rewritten
   PullState pull;
   PrPullState pr;
@@ -95,7 +100,9 @@ struct grd_ctx {
   // profiling events: [0..4] bracket the stages of a round, [5..6] the
   // load-balanced push kernel
   cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  std::vector<void*> host_registered;  // layout arrays pinned for H2D uploads
+  // Pinned twins of the large host layout arrays (cudaHostAlloc, filled once
+  // at creation), keyed by the array's data pointer: uploads read the twin.
+  std::unordered_map<const void*, void*> pinned_twin;
   std::vector<uint8_t> wgt8_host;  // weights as bytes when all are < 256 (uploaded instead of L.wgt)
   uint8_t* wgt8_dev = nullptr;     // their device staging copy
   unsigned char* h_small = nullptr;  // pinned small tables of the upload (hubs, tiles, partitions)
@@ -153,8 +160,7 @@ int grd_alloc_resident(grd_ctx* ctx);
 int grd_device_layout_check(const grd_csr* graph, uint32_t M, std::string* why);
 int grd_device_layout_build(grd_ctx* ctx, const grd_csr* graph, const uint32_t* mirror_part, bool first);
 int grd_device_in_edges(grd_ctx* ctx);
-void grd_pin_host(grd_ctx* ctx, std::initializer_list<std::vector<uint32_t>*> arrays);
-void grd_pin_host_bytes(grd_ctx* ctx, std::vector<uint8_t>& v);
+void grd_pin_twin(grd_ctx* ctx, const void* data, size_t bytes);
 int grd_dev_alloc_bytes(grd_ctx* ctx, void** p, size_t bytes);
 void grd_prof_mark(grd_ctx* ctx, int i);
 void grd_prof_collect(grd_ctx* ctx);
@@ -164,6 +170,7 @@ int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks);
 int grd_pr_delta_hubs(grd_ctx* ctx);
 int grd_upload_layout(grd_ctx* ctx);
 int grd_ensure_in_edges(grd_ctx* ctx);
+int grd_ensure_out_edges(grd_ctx* ctx);
 int grd_read_counters(grd_ctx* ctx);
 int grd_fold_counters(grd_ctx* ctx);
 int grd_sync_init_counters(grd_ctx* ctx);

@@ -212,6 +212,41 @@ def test_upload_sends_byte_weights_and_derives_vertex_arrays(gpu):
 
 
 @pytest.mark.gpu
+def test_pagerank_pull_upload_leaves_out_edges_until_needed(gpu):
+    """A Jacobi PageRank ctx re-uploads only what it reads (slot map, row
+    offsets, the in-edge sources).  The out-edge columns and the weights
+    follow before another algorithm or a layout read needs them, and every
+    result stays that of a full upload."""
+    G = g.Graph.rmat(12, 8, symmetrize=True, weighted=True)
+    part = G.partition_edge_balanced(3)
+    E = G.num_edges
+    with g.Context(G, part, num_memory=3) as ctx, g.Context(G, part, num_memory=3) as ref_ctx:
+        ref_ctx.set_algo(g.GRD_PR_PULL, max_rounds=30)
+        ref_ctx.init()
+        ref_ctx.run()
+        ranks = ref_ctx.read_ranks()
+        ctx.set_algo(g.GRD_PR_PULL, max_rounds=30)  # builds the in-edge view
+        ctx.set_algo(g.GRD_CC)
+        full = ctx.upload()
+        ctx.set_algo(g.GRD_PR_PULL, max_rounds=30)
+        slim = ctx.upload()
+        assert full - slim == 4 * E + E + 4 * E  # u32 columns, byte weights, in-edge weights
+        ctx.init()
+        ctx.run()
+        np.testing.assert_array_equal(ctx.read_ranks(), ranks)
+        for name in ("col", "wgt", "in_wgt"):
+            np.testing.assert_array_equal(ctx.read_layout(name), ref_ctx.read_layout(name), err_msg=name)
+        assert ctx.upload() == slim
+        for algo in (g.GRD_CC, g.GRD_SSSP_W):  # the columns come back before the push runs
+            ctx.set_algo(algo)
+            ctx.init()
+            ctx.run()
+            ref = O.run(O.ORC_CC if algo == g.GRD_CC else O.ORC_SSSP_W, G.row_offsets, G.col_indices,
+                        G.weights, mirror=part, num_memory=3)
+            np.testing.assert_array_equal(ctx.read_props(), ref["props"])
+
+
+@pytest.mark.gpu
 def test_read_into_caller_arrays(gpu):
     """read_props / read_updates / read_ranks fill a caller's array (a
     serving loop keeps pinned result buffers) and refuse one of the wrong
