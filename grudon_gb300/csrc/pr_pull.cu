@@ -189,6 +189,20 @@ __device__ __forceinline__ void pr_tile(const PrArgs& a, const float* s_hot, uin
   }
   const float piece = has_left ? left : (through ? __fsub_rn(s, c) : 0.0f);
   const uint32_t thr_mask = __ballot_sync(FULL, through);
+  if (thr_mask == FULL) {
+    // The whole tile lies inside the list it starts in (an interior tile of
+    // a long in-list): the head is the 32 lane pieces folded in lane order,
+    // the same steps the walk below takes, with every lane folding the
+    // broadcast pieces instead of one lane stepping through the warp.
+    float hs = 0.0f, hc = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) kahan_add(hs, hc, __shfl_sync(FULL, piece, i));
+    if (lane == 31) {
+      a.piece[t] = make_uint4(__float_as_uint(__fsub_rn(hs, hc)), __float_as_uint(s), __float_as_uint(c), k);
+      a.pflags[t] = F_HEAD | F_HEAD_THROUGH;
+    }
+    return;
+  }
   // Chains across lanes, walked in lane order: lanes 0..30 continue their open
   // list into the next lanes; lane 31 (whose open list, if any, is the tile's
   // tail) walks the tile's head: the list the tile starts inside.
