@@ -1008,22 +1008,28 @@ static __global__ void __launch_bounds__(256) k_fwd_xfer_deg(DevGraph g, DevStat
 }
 
 // One warp per 256-edge chunk.  The warp stages a window of up to LBS_WIN
-// consecutive actives (their DP, row start minus DP, and source value) in
-// shared memory, 32 at a time with coalesced loads, only as many as the
-// chunk's edges need (one group of 32 for a typical degree) — one window
-// covers the whole chunk unless more than LBS_WIN actives fall inside it.
+// consecutive actives (their DP, and the pair row start minus DP / source
+// value) in shared memory, 32 at a time with coalesced loads, only as many
+// as the chunk's edges need (one group of 32 for a typical degree) — one
+// window covers the whole chunk unless more than LBS_WIN actives fall inside
+// it, and a chunk of that many low-degree rows takes a second window.
 // The row of each of the window's edge positions comes from a mark-and-scan:
 // every active with edges marks the position where its row starts, then a
 // running max over the 256 positions.  Marks carry a per-warp generation
 // number above the window index, so the mark array is never cleared: the
 // current window always marks position 0, and its marks outrank every older
-// one.  An edge then costs three shared loads (its row, the row's edge base,
-// the source value), and lane l takes positions l, l+32, ...: one load
-// instruction of the warp reads 32 consecutive edges, whose destinations
-// (sorted within a row) share sectors.  All 8 edges of a lane are loaded
-// (index, weight, current value) before any update is issued, keeping 8
-// independent memory chains in flight per lane.
-constexpr uint32_t LBS_WIN = 256;
+// one.  An edge then costs two shared loads (its row, then the row's edge
+// base and source value as one 8-byte load), and lane l takes positions l,
+// l+32, ...: one load instruction of the warp reads 32 consecutive edges,
+// whose destinations (sorted within a row) share sectors.  All 8 edges of a
+// lane are loaded (index, weight, current value) before any update is
+// issued, keeping 8 independent memory chains in flight per lane.
+// The kernel is bound by the latency of those chains, and the L1 that the
+// shared memory leaves sets how many of them are in flight: 20 KB per block
+// (5 blocks per SM) leaves most of the SM's 256 KB to L1; 34 KB per block
+// (a 256-active window) ran 14-22 % slower, and 39-40 KB per block, which
+// leaves only the minimum L1, ran 2x slower.
+constexpr uint32_t LBS_WIN = 128;
 constexpr int LBS_JBITS = 9;  // window index bits of a mark
 static_assert(LBS_WIN <= (1u << LBS_JBITS), "window index fits its mark field");
 
@@ -1035,8 +1041,7 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
   constexpr uint32_t GEN_MAX = (1u << (32 - LBS_JBITS)) - 1u;
   static_assert(LBS_CHUNK == 8 * 32, "each lane owns 8 consecutive edge positions");
   __shared__ uint32_t s_dp[8][LBS_WIN];   // DP of window active j
-  __shared__ uint32_t s_bmd[8][LBS_WIN];  // its row start - DP: edge index = bmd + position
-  __shared__ uint32_t s_sv[8][LBS_WIN];   // its source value
+  __shared__ uint2 s_bs[8][LBS_WIN];     // its (row start - DP, source value): edge index = .x + position
   __shared__ uint32_t s_src[8][LBS_CHUNK];
   const uint32_t K = (uint32_t)__ldcg(&st.counters[C_ACTIVE]);
   const uint32_t m = (uint32_t)__ldcg(&st.counters[C_MEDGES]);
@@ -1044,8 +1049,7 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
   const uint32_t nchunks = (m + LBS_CHUNK - 1) / LBS_CHUNK;
   const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
   uint32_t* dp = s_dp[w];
-  uint32_t* bmd = s_bmd[w];
-  uint32_t* svs = s_sv[w];
+  uint2* bs = s_bs[w];
   uint32_t* srcs = s_src[w];
   uint32_t gen = GEN_MAX;  // the first step clears the marks
   for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + w; c < nchunks; c += nwarps) {
@@ -1070,8 +1074,7 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
         const uint32_t nx = i0 + nw * 32 + 32;
         const uint32_t tl = (lane == 31) ? (nx < K ? st.DP[nx] : m) : 0u;
         dp[nw * 32 + lane] = av;
-        bmd[nw * 32 + lane] = bv - av;
-        svs[nw * 32 + lane] = source_value<A>(vv);
+        bs[nw * 32 + lane] = make_uint2(bv - av, source_value<A>(vv));
         cover = __shfl_sync(FULL, tl, 31);
         ++nw;
       } while (nw < (uint32_t)SW && cover < e_end);
@@ -1120,9 +1123,10 @@ __global__ void __launch_bounds__(256, 5) k_push_lbs(DevGraph g, DevState st) {
         cand[k] = 0;
         if (eid < wend) {
           const uint32_t j = srcs[k * 32 + lane] & ((1u << LBS_JBITS) - 1u);
-          const uint32_t ed = bmd[j] + eid;
+          const uint2 b = bs[j];
+          const uint32_t ed = b.x + eid;
           dst[k] = __ldg(&g.col[ed]);
-          cand[k] = svs[j];
+          cand[k] = b.y;
           if (A == A_SSSP_W) cand[k] = relax_cand<A>(cand[k], __ldg(&g.wgt[ed]));
         }
       }

@@ -49,6 +49,7 @@ constexpr uint32_t PR_THREADS = 1024;  // k_pr_pull: one block per SM
 constexpr uint32_t PR_HOT_CAP = 32768; // hot sources in shared memory (128 KB)
 constexpr uint32_t PR_HOT_BIT = 0x80000000u;
 constexpr int PR_HIST = 128;           // out-degree histogram buckets (4 per octave)
+constexpr uint32_t PR_FINE = 4096;     // exact-degree bins when the cap falls inside a bucket
 static_assert(PR_TILE == 32 * PR_LANE, "a tile is one warp's lanes");
 
 // Tile piece flags.
@@ -507,6 +508,15 @@ __global__ void __launch_bounds__(256) k_pr_deg_hist(DevGraph g, uint32_t* cnt, 
     }
 }
 
+// Exact out-degree counts in [lo, lo + n): the histogram bucket that the hot
+// set's cap falls in, split so that the cut lands on an exact degree.
+__global__ void __launch_bounds__(256) k_pr_deg_fine(DevGraph g, uint32_t lo, uint32_t n, uint32_t* cnt) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += gridDim.x * blockDim.x) {
+    const uint32_t d = g.outdeg[v] - lo;  // wraps for degrees below lo
+    if (d < n) atomicAdd(&cnt[d], 1u);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_pr_hot_words(DevGraph g, uint32_t hot_deg, uint32_t H, uint32_t* words) {
   const uint32_t lane = lane_id();
   const uint32_t nwords = (g.V + 31) / 32;
@@ -682,9 +692,12 @@ int pr_prepare(grd_ctx* ctx) {
   }
 
   Tmp tmp(ctx);
-  TRY(tmp.reserve(2 * PR_HIST + (V / 32 + 2) + (V + 1) + V + 4 * S + 1 + (T + 1) + (E + 1)));
+  TRY(tmp.reserve(2 * PR_HIST + PR_FINE + (V / 32 + 2) + (V + 1) + V + 4 * S + 1 + (T + 1) + (E + 1)));
   // (1) hot set: the highest out-degrees, at most PR_HOT_CAP vertices, cut at
-  // a histogram bucket boundary
+  // a histogram bucket boundary, then inside the next bucket at an exact
+  // degree (RMAT's degree plateaus put tens of thousands of vertices in one
+  // bucket: at RMAT-24 the bucket cut alone keeps 12 959 hot sources, the
+  // exact cut about 32 700)
   uint32_t *hist = nullptr;
   TRY(tmp.get(&hist, 2 * PR_HIST));
   CK(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * PR_HIST, s));
@@ -697,12 +710,37 @@ int pr_prepare(grd_ctx* ctx) {
   uint64_t nondangling = 0, cum = 0;
   uint32_t H = 0, hot_deg = 0;
   for (int b = 0; b < PR_HIST; ++b) nondangling += h_hist[b];
+  int cut = -1;  // the bucket the cap falls in
   for (int b = PR_HIST - 1; b >= 0; --b) {
     if (!h_hist[b]) continue;
-    if (cum + h_hist[b] > PR_HOT_CAP) break;
+    if (cum + h_hist[b] > PR_HOT_CAP) {
+      cut = b;
+      break;
+    }
     cum += h_hist[b];
     H = (uint32_t)cum;
     hot_deg = h_hist[PR_HIST + b];
+  }
+  if (cut >= 8) {  // bucket 4m + f holds the degrees [(4 + f) << (m - 2), (5 + f) << (m - 2))
+    const uint32_t m = (uint32_t)cut / 4, f = (uint32_t)cut % 4;
+    const uint32_t lo = (4u + f) << (m - 2), width = 1u << (m - 2);
+    if (width > 1 && width <= PR_FINE) {
+      uint32_t* fine = nullptr;
+      TRY(tmp.get(&fine, PR_FINE));
+      CK(cudaMemsetAsync(fine, 0, sizeof(uint32_t) * width, s));
+      k_pr_deg_fine<<<grid(ctx, V), 256, 0, s>>>(g, lo, width, fine);
+      CK_LAUNCH();
+      std::vector<uint32_t> h_fine(width);
+      CK(cudaMemcpyAsync(h_fine.data(), fine, sizeof(uint32_t) * width, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (int d = (int)width - 1; d >= 0; --d) {
+        if (!h_fine[d]) continue;
+        if (cum + h_fine[d] > PR_HOT_CAP) break;
+        cum += h_fine[d];
+        H = (uint32_t)cum;
+        hot_deg = lo + (uint32_t)d;
+      }
+    }
   }
   if (H == 0) hot_deg = 0;
   // (2) hot ranks: per 32-vertex word, then its exclusive scan
