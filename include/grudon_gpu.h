@@ -212,8 +212,12 @@ const char* grd_create_error(void);
 
 /* Re-uploads the layout arrays from the host copy kept at create time
  * (timed host->device traffic for end-to-end runs). Returns bytes copied.
- * The copies are queued on the ctx stream (pinned host memory) and the call
- * returns at once; every later call on the ctx sees the new data. */
+ * The copies are queued on the ctx stream from pinned copies of the layout
+ * made at create time, and the call returns at once; every later call on the
+ * ctx sees the new data.  A ctx whose algorithm is GRD_PR_PULL copies what
+ * that algorithm reads (slot map, row offsets, the in-edge view's offsets
+ * and sources); the out-edge columns and the weights follow before another
+ * algorithm or grd_read_layout needs them. */
 int grd_upload(grd_ctx* ctx, uint64_t* bytes_copied);
 
 /* Algorithm selection and per-stage round API -----------------------------*/

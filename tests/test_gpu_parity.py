@@ -293,6 +293,31 @@ def test_pr_pull_vs_fp64_oracle(gpu, num_memory):
         assert st["edges_scanned"] == 40 * G.num_edges
 
 
+def test_pr_pull_rmat20_exact_degree_hot_cut(gpu):
+    """RMAT-20: the 32 768-source cap of the shared-memory hot set falls
+    inside an out-degree histogram bucket (degrees 64-79), so the set is cut
+    at an exact degree inside it (about 32 100 hot sources instead of the
+    bucket boundary's 25 300).  A hot source read from the wrong place would
+    show in the ranks: they stay within 1e-5 of FP64 Jacobi, and two runs
+    agree bit for bit."""
+    G = g.Graph.rmat(20, 16)
+    ro, ci = G.row_offsets, G.col_indices
+    deg = np.diff(ro.astype(np.int64))
+    assert 25_000 < int((deg >= 80).sum()) <= 32_768 < int((deg >= 64).sum())  # the cap falls in [64, 80)
+    with g.Context(G, G.partition_edge_balanced(3), num_memory=3) as ctx:
+        ctx.set_algo(g.GRD_PR_PULL, max_rounds=30, tolerance=0.0)
+        runs = []
+        for _ in range(2):
+            ctx.init()
+            st = ctx.run()
+            assert st["rounds"] == 30
+            runs.append(ctx.read_ranks())
+    np.testing.assert_array_equal(runs[0], runs[1])
+    ref, it, _ = O.pr_jacobi_fp64_mt(ro, ci, iters=30)
+    assert it == 30
+    assert _max_rel_err(runs[0], ref) <= 1e-5
+
+
 def test_pr_pull_converges_and_stage_api(gpu):
     G = g.Graph.rmat(12, 8)
     ro, ci = G.row_offsets, G.col_indices
