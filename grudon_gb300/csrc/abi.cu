@@ -1005,6 +1005,7 @@ void grd_ctx_destroy(grd_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
   if (ctx->h_small) cudaFreeHost(ctx->h_small);
+  if (ctx->ingest_stage) cudaFreeHost(ctx->ingest_stage);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->side) cudaStreamDestroy(ctx->side);

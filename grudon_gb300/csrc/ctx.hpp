@@ -106,6 +106,10 @@ struct grd_ctx {
   std::vector<uint8_t> wgt8_host;  // weights as bytes when all are < 256 (uploaded instead of L.wgt)
   uint8_t* wgt8_dev = nullptr;     // their device staging copy
   unsigned char* h_small = nullptr;  // pinned small tables of the upload (hubs, tiles, partitions)
+  // Pinned staging copy of a caller's CSR for grd_ingest (grown on demand):
+  // host threads copy the caller's arrays in, the copy engine reads them out.
+  unsigned char* ingest_stage = nullptr;
+  size_t ingest_stage_bytes = 0;
   grd_policy_model* policy_dev = nullptr;  // learned round policy (device copy)
   // grd_sssp_multi (msssp.cu): 64 distance lanes per vertex, the lane masks,
   // the active list with its degree prefix, the source-major output copy
