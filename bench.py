@@ -342,9 +342,10 @@ def e2e_pass(W, args, barrier, streams, dev):
     """End to end through the C ABI with host buffers: every step copies the
     three layouts from pinned host memory and reads the three results back
     into pinned host arrays.  Copies are pipelined with the runs: while one
-    context runs, the next one's layout is on the link; runs and reads are
-    queued (run(wait=False), read(wait=False)) and ordered by stream events so
-    that the three runs never share the GPU."""
+    context runs, the next one's layout is on the link and then its set-up
+    (init) runs; runs and reads are queued (run(wait=False), read(wait=False))
+    and ordered by stream events so that the three runs never share the
+    GPU."""
     import numpy as np
     import torch
     from grudon_gb300.replicas import job_throughput
@@ -378,9 +379,9 @@ def e2e_pass(W, args, barrier, streams, dev):
                 streams[j].wait_event(up_done[i])
                 h2d += W.ctxs[j].upload()
             c.wait()
+            c.init()  # set-up after this context's upload; may overlap the previous context's run
             if k or i:
                 streams[i].wait_event(run_done[(i - 1) % n])
-            c.init()
             c.run(wait=False)
             read(i, c, False)
             run_done[i].record(streams[i])

@@ -5,9 +5,12 @@
 //   pr[v] = (1-d)*[outdeg(v) > 0] + sum_{u->v} d * pr[u] / outdeg(u)
 // One iteration is one round of src/GraphAlgorithm.cpp:145-701 with every
 // non-dangling vertex in the frontier:
-//   forward sync   the compute partition sends c[u] = d*pr[u]/outdeg(u) to the
-//                  owned slot of u in its mirror partition (k_pr_update writes
-//                  it there as it forms the rank; k_pr_fwd at init);
+//   forward sync   the compute partition's contributions c[u] = d*pr[u]/outdeg(u)
+//                  are what the memory partitions read: all partitions share
+//                  one HBM, so the pull gathers them straight from the compute
+//                  partition's array (vertex_properties, written by
+//                  k_pr_update as it forms the rank), and the send only copies
+//                  the hot sources' values (k_pr_update; k_pr_fwd at init);
 //   edge-map       every memory partition sums, per destination slot, its
 //                  in-edges' contributions with a Kahan-compensated FP32 sum
 //                  (k_pr_pull, k_pr_fix);
@@ -26,8 +29,8 @@
 // running sum lane by lane (in lane order), and one that crosses tiles
 // continues tile by tile (k_pr_fix, in tile order).  The hottest sources (the
 // highest out-degrees, up to PR_HOT_CAP of them) are staged in shared memory
-// each iteration; their in-edges carry the hot index instead of the slot, so
-// about a third of the gathers never leave the SM.
+// each iteration; their in-edges carry the hot index instead of the source
+// vertex, so about a third of the gathers never leave the SM.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -61,7 +64,7 @@ struct PrArgs {
   const uint32_t* src;
   const uint32_t* start_bits;
   const uint32_t* tile_nz;
-  const uint32_t* mprop;  // contributions (FP32 bits) at the owned source slots
+  const uint32_t* contrib;  // [V] contributions (FP32 bits) by vertex: the compute partition's array
   const float* hot_val;
   float* part;
   uint4* piece;
@@ -101,8 +104,8 @@ __device__ __forceinline__ uint4 ld_stream_v4(const uint32_t* p) {
 // One source value: a hot source from the shared-memory copy, the others from
 // global memory.  (One generic load for both kinds measured slower: 0.868 ms
 // against 0.840 ms per RMAT-24 pull.)
-__device__ __forceinline__ float pr_gather(const float* s_hot, const uint32_t* mprop, uint32_t code) {
-  return (code & PR_HOT_BIT) ? s_hot[code & ~PR_HOT_BIT] : __uint_as_float(__ldg(mprop + code));
+__device__ __forceinline__ float pr_gather(const float* s_hot, const uint32_t* contrib, uint32_t code) {
+  return (code & PR_HOT_BIT) ? s_hot[code & ~PR_HOT_BIT] : __uint_as_float(__ldg(contrib + code));
 }
 
 // One 512-edge tile (warp-wide).  kFull: all 512 in-edges exist (every tile
@@ -145,7 +148,7 @@ __device__ __forceinline__ void pr_tile(const PrArgs& a, const float* s_hot, uin
   const uint32_t lane0_sb = __shfl_sync(FULL, sb, 0);
   float v[PR_LANE];
 #pragma unroll
-  for (int j = 0; j < (int)PR_LANE; ++j) v[j] = (kFull || (uint32_t)j < n) ? pr_gather(s_hot, a.mprop, code[j]) : 0.0f;
+  for (int j = 0; j < (int)PR_LANE; ++j) v[j] = (kFull || (uint32_t)j < n) ? pr_gather(s_hot, a.contrib, code[j]) : 0.0f;
   // fold in stored order; a list that opens in this lane and closes in it is
   // complete
   uint32_t k = k_first;
@@ -347,8 +350,9 @@ __global__ void __launch_bounds__(256) k_pr_fix(PrArgs a) {
 // -------------------------------------------------------- update / fwd --
 // Per vertex: the partial sums of its slots' in-lists (stored contiguously,
 // partition order) merged with Kahan (an exactly zero partial adds nothing and
-// is skipped), the new rank, the L1 residual, and the new contribution sent to
-// the vertex's owned slot (and to the hot array when the vertex is hot).
+// is skipped), the new rank, the L1 residual, and the new contribution in the
+// vertex's entry of vertex_properties, which the next pull gathers from (and
+// in the hot array when the vertex is hot).
 // Warps take 32 consecutive vertices (the hot rank is a ballot prefix), two
 // such words per step with every independent load issued before the partial
 // sums, whose addresses depend on the list offsets.
@@ -366,7 +370,7 @@ __global__ void __launch_bounds__(256) k_pr_update(DevGraph g, DevState st, PrUp
   const uint32_t nw = gridDim.x * (blockDim.x >> 5);
   for (uint32_t w0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * UPD_WORDS; w0 < nwords;
        w0 += nw * UPD_WORDS) {
-    uint32_t v[UPD_WORDS], deg[UPD_WORDS], b[UPD_WORDS], e[UPD_WORDS], os[UPD_WORDS];
+    uint32_t v[UPD_WORDS], deg[UPD_WORDS], b[UPD_WORDS], e[UPD_WORDS];
     float ov[UPD_WORDS];
     bool valid[UPD_WORDS];
 #pragma unroll
@@ -377,7 +381,6 @@ __global__ void __launch_bounds__(256) k_pr_update(DevGraph g, DevState st, PrUp
       b[q] = valid[q] ? __ldg(&u.voff[v[q]]) : 0u;
       e[q] = valid[q] ? __ldg(&u.voff[v[q] + 1]) : 0u;
       ov[q] = valid[q] ? st.ranks[v[q]] : 0.0f;
-      os[q] = valid[q] ? st.own_slot[v[q]] : 0u;
     }
 #pragma unroll
     for (int q = 0; q < UPD_WORDS; ++q) {
@@ -399,7 +402,6 @@ __global__ void __launch_bounds__(256) k_pr_update(DevGraph g, DevState st, PrUp
         const float contrib = deg[q] ? __fdiv_rn(__fmul_rn(u.damping, nv), (float)deg[q]) : 0.0f;
         const uint32_t cb = __float_as_uint(contrib);
         st.prop[v[q]] = cb;
-        st.mprop[os[q]] = cb;
         if (hot) u.hot_val[u.hot_base[w0 + q] + __popc(hm & ((1u << lane) - 1u))] = contrib;
       }
     }
@@ -416,8 +418,8 @@ __global__ void __launch_bounds__(256) k_pr_update(DevGraph g, DevState st, PrUp
   }
 }
 
-// Initial contributions (from init()'s vertex_properties) to the owned slots
-// and the hot array.
+// Initial contributions (init()'s vertex_properties) of the hot sources to
+// the hot array.
 __global__ void __launch_bounds__(256) k_pr_fwd(DevGraph g, DevState st, PrUpd u) {
   const uint32_t lane = lane_id();
   const uint32_t nwords = (g.V + 31) / 32;
@@ -429,9 +431,7 @@ __global__ void __launch_bounds__(256) k_pr_fwd(DevGraph g, DevState st, PrUpd u
     const bool hot = valid && u.H != 0 && deg != 0 && deg >= u.hot_deg;
     const uint32_t hm = __ballot_sync(FULL, hot);
     if (valid) {
-      const uint32_t cb = st.prop[v];
-      st.mprop[st.own_slot[v]] = cb;
-      if (hot) u.hot_val[u.hot_base[w] + __popc(hm & ((1u << lane) - 1u))] = __uint_as_float(cb);
+      if (hot) u.hot_val[u.hot_base[w] + __popc(hm & ((1u << lane) - 1u))] = __uint_as_float(st.prop[v]);
     }
   }
 }
@@ -529,7 +529,8 @@ __global__ void __launch_bounds__(256) k_pr_hot_words(DevGraph g, uint32_t hot_d
   }
 }
 
-// Code of every owned slot: the hot rank with the top bit, or the slot.
+// Code of every owned slot: the hot rank with the top bit, or the slot's vertex
+// (the pull gathers cold sources' contributions by vertex).
 __global__ void __launch_bounds__(256) k_pr_slot_code(DevGraph g, DevState st, uint32_t hot_deg, uint32_t H,
                                                       const uint32_t* hot_base, uint32_t* code) {
   const uint32_t lane = lane_id();
@@ -543,7 +544,7 @@ __global__ void __launch_bounds__(256) k_pr_slot_code(DevGraph g, DevState st, u
     const uint32_t m = __ballot_sync(FULL, hot);
     if (valid) {
       const uint32_t s = st.own_slot[v];
-      code[s] = hot ? (PR_HOT_BIT | (hot_base[w] + __popc(m & ((1u << lane) - 1u)))) : s;
+      code[s] = hot ? (PR_HOT_BIT | (hot_base[w] + __popc(m & ((1u << lane) - 1u)))) : v;
     }
   }
 }
@@ -807,7 +808,7 @@ int pr_prepare(grd_ctx* ctx) {
 
 PrArgs pr_args(grd_ctx* ctx) {
   PrPullState& P = ctx->pr;
-  return PrArgs{P.src, P.start_bits, P.tile_nz, ctx->st.mprop, P.hot_val, P.part, P.piece, P.piece_flags,
+  return PrArgs{P.src, P.start_bits, P.tile_nz, ctx->st.prop, P.hot_val, P.part, P.piece, P.piece_flags,
                 P.E, P.T, P.H};
 }
 
