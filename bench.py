@@ -44,10 +44,10 @@ SCALE, EF, NUM_MEMORY = 24, 16, 3
 RMAT_ABC = (0.57, 0.19, 0.19)
 PR_MAX_ITERS, PR_TOL = 100, 1e-7
 # DRAM bytes (read + write) per in-edge of k_pr_pull in its ncu capture
-# (PageRank RMAT-22, 65.2 M in-edges): 291.9 MB per launch.
-DRAM_BYTES_PER_PULL_EDGE = 291.9e6 / 65.24e6
-# ... and of k_push_lbs (CC round 0 on RMAT-21): 249.9 MB for 50.2 M edges.
-DRAM_BYTES_PER_PUSH_EDGE = 249.9e6 / 50.2e6
+# (PageRank RMAT-22, 65.2 M in-edges): 292.0 MB per launch.
+DRAM_BYTES_PER_PULL_EDGE = 292.0e6 / 65.24e6
+# ... and of k_push_lbs (CC round 0 on RMAT-21): 251.0 MB for 50.2 M edges.
+DRAM_BYTES_PER_PUSH_EDGE = 251.0e6 / 50.2e6
 
 
 def parse():
