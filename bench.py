@@ -341,11 +341,13 @@ def roofline_of(W, prof, pr_run_ms, peak, peak_src):
 def e2e_pass(W, args, barrier, streams, dev):
     """End to end through the C ABI with host buffers: every step copies the
     three layouts from pinned host memory and reads the three results back
-    into pinned host arrays.  Copies are pipelined with the runs: while one
-    context runs, the next one's layout is on the link and then its set-up
-    (init) runs; runs and reads are queued (run(wait=False), read(wait=False))
-    and ordered by stream events so that the three runs never share the
-    GPU."""
+    into pinned host arrays.  Copies are pipelined with the runs, one step
+    ahead: once a step's three runs are queued, the next step's layouts are
+    queued on each context's own stream, so CC's and SSSP's copies overlap
+    the long PageRank run and PageRank's copy (queued behind its own run)
+    overlaps the next CC and SSSP runs.  Runs and reads are queued
+    (run(wait=False), read(wait=False)) and ordered by stream events so that
+    the three runs never share the GPU."""
     import numpy as np
     import torch
     from grudon_gb300.replicas import job_throughput
@@ -357,7 +359,6 @@ def e2e_pass(W, args, barrier, streams, dev):
     def read(i, c, wait):
         return c.read_ranks(out=res[i], wait=wait) if i == 2 else c.read_props(out=res[i], wait=wait)
 
-    up_done = [torch.cuda.Event() for _ in range(3)]
     run_done = [torch.cuda.Event() for _ in range(3)]
     n = len(W.ctxs)
     # the three uploads alone, one after another (link bandwidth)
@@ -369,15 +370,10 @@ def e2e_pass(W, args, barrier, streams, dev):
     barrier()
     t0 = time.perf_counter()
     marks = []
-    h2d = W.ctxs[0].upload()
+    h2d = sum(c.upload() for c in W.ctxs)  # the first step's layouts
     for k in range(args.steps):
         marks.append(time.perf_counter())
         for i, c in enumerate(W.ctxs):
-            j = (i + 1) % n
-            if j or k + 1 < args.steps:  # the next layout goes on the link once this one is there
-                up_done[i].record(streams[i])
-                streams[j].wait_event(up_done[i])
-                h2d += W.ctxs[j].upload()
             c.wait()
             c.init()  # set-up after this context's upload; may overlap the previous context's run
             if k or i:
@@ -385,6 +381,8 @@ def e2e_pass(W, args, barrier, streams, dev):
             c.run(wait=False)
             read(i, c, False)
             run_done[i].record(streams[i])
+        if k + 1 < args.steps:  # the next step's layouts, each behind its own context's run and read
+            h2d += sum(c.upload() for c in W.ctxs)
     sts = [c.wait() for c in W.ctxs]
     barrier()
     secs = time.perf_counter() - t0
