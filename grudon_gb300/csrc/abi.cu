@@ -548,27 +548,29 @@ int grd_enqueue_edge_map_mode(grd_ctx* ctx, int mode, int degree_passes_done, bo
       CK_LAUNCH();
       return GRD_OK;
     }
-    if (mode == RM_PULL_BITVEC) {
-      k_pull<A, false><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-      if (ctx->pull.num_in_meds)
-        k_pull_med<A, false><<<pull_med_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_meds,
-                                                                     ctx->pull.num_in_meds);
-      if (ctx->pull.num_in_hubs)
-        k_pull_hub<A, false><<<pull_hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_hubs,
-                                                                     ctx->pull.num_in_hubs);
-      CK_LAUNCH();
-      return GRD_OK;
-    }
-    if (mode == RM_PULL_LIST) {
-      k_pull<A, true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
-      if (ctx->pull.num_in_meds)
-        k_pull_med<A, true><<<pull_med_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_meds,
-                                                                    ctx->pull.num_in_meds);
-      if (ctx->pull.num_in_hubs)
-        k_pull_hub<A, true><<<pull_hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_hubs,
-                                                                    ctx->pull.num_in_hubs);
-      CK_LAUNCH();
-      return GRD_OK;
+    if constexpr (A != A_PR_DELTA) {  // the generic pull serves CC and SSSP
+      if (mode == RM_PULL_BITVEC) {
+        k_pull<A, false><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+        if (ctx->pull.num_in_meds)
+          k_pull_med<A, false><<<pull_med_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_meds,
+                                                                       ctx->pull.num_in_meds);
+        if (ctx->pull.num_in_hubs)
+          k_pull_hub<A, false><<<pull_hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_hubs,
+                                                                       ctx->pull.num_in_hubs);
+        CK_LAUNCH();
+        return GRD_OK;
+      }
+      if (mode == RM_PULL_LIST) {
+        k_pull<A, true><<<grid_for(ctx, 8), 256, 0, ctx->stream>>>(ctx->g, ctx->st);
+        if (ctx->pull.num_in_meds)
+          k_pull_med<A, true><<<pull_med_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_meds,
+                                                                      ctx->pull.num_in_meds);
+        if (ctx->pull.num_in_hubs)
+          k_pull_hub<A, true><<<pull_hub_grid, 256, 0, ctx->stream>>>(ctx->g, ctx->st, ctx->pull.in_hubs,
+                                                                      ctx->pull.num_in_hubs);
+        CK_LAUNCH();
+        return GRD_OK;
+      }
     }
     const uint32_t B = lbs_blocks(ctx);
     if (degree_passes_done < 1) k_deg_reduce<<<B, 256, 0, ctx->stream>>>(ctx->g, ctx->st);

@@ -1334,9 +1334,9 @@ __global__ void __launch_bounds__(256) k_diff_aggregate(DevGraph g, DevState st)
 // this round's frontier still holds the value it last sent, whose
 // relaxation has already been applied, so it cannot lower anything — the
 // values and the dirty set equal those of the push over the frontier, with no
-// atomics.  Delta PageRank adds only frontier sources (bit test in FB), in
-// ascending source order, so its sums are reproducible.  PR_PULL folds every
-// source with a Kahan sum.
+// atomics.  Delta PageRank pulls with its fixed-order sums (k_pr_delta_pull
+// below) and Jacobi PageRank with k_pr_pull (pr_pull.cu); kahan_add is the
+// compensated step both PageRank sums use.
 constexpr uint32_t K_PULL_HUB = 1024;  // = PULL_HUB of the layout
 constexpr uint32_t K_PULL_MED = 64;    // = PULL_MED of the layout
 constexpr uint32_t PULL_CH = 256;      // staged in-edges per warp step
@@ -1349,43 +1349,28 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 }
 
 // Value contributed by one in-edge (bit pattern), and the fold identity.
+// The generic pull serves the min algorithms (CC, SSSP): delta PageRank pulls
+// with its fixed-order sums (k_pr_delta_pull) and Jacobi PageRank with
+// k_pr_pull (pr_pull.cu).
 template <int A>
 __device__ __forceinline__ uint32_t pull_value(const DevState& st, uint32_t src, uint32_t w) {
+  static_assert(A == A_CC || A == A_SSSP_HOP || A == A_SSSP_W, "min algorithms only");
   const uint32_t v = st.mprop[src];
   if (A == A_SSSP_HOP) return v == 0xFFFFFFFFu ? v : v + 1u;
   if (A == A_SSSP_W) return sat_add(v, w);
-  if (A == A_PR_DELTA) return test_bit(st.FB, src) ? v : 0u;
-  return v;  // CC, PR_PULL
+  return v;  // CC
 }
 
 template <int A>
 struct PullAcc {
-  uint32_t best = 0xFFFFFFFFu;  // min algorithms
-  float s = 0.0f, c = 0.0f;     // sums (c: Kahan compensation, PR_PULL)
-  __device__ __forceinline__ void fold(uint32_t v) {
-    if (A == A_PR_PULL)
-      kahan_add(s, c, __uint_as_float(v));
-    else if (A == A_PR_DELTA)
-      s = __fadd_rn(s, __uint_as_float(v));
-    else
-      best = min(best, v);
-  }
+  static_assert(A == A_CC || A == A_SSSP_HOP || A == A_SSSP_W, "min algorithms only");
+  uint32_t best = 0xFFFFFFFFu;
+  __device__ __forceinline__ void fold(uint32_t v) { best = min(best, v); }
 };
 
 // Writes the pulled value of destination slot d; returns its dirty bit.
 template <int A>
-__device__ __forceinline__ bool pull_commit(const DevState& st, uint32_t d, const PullAcc<A>& a, bool has) {
-  if (A == A_PR_PULL) {
-    if (has) st.mupd[d] = __float_as_uint(__fsub_rn(a.s, a.c));
-    return has;
-  }
-  if (A == A_PR_DELTA) {  // every frontier contribution is > 0
-    if (a.s > 0.0f) {
-      st.mupd[d] = __float_as_uint(a.s);
-      return true;
-    }
-    return false;
-  }
+__device__ __forceinline__ bool pull_commit(const DevState& st, uint32_t d, const PullAcc<A>& a, bool) {
   if (a.best < st.mupd[d]) {
     st.mupd[d] = a.best;
     return true;
@@ -1443,7 +1428,6 @@ __global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
     }
     bool dirty = false;
     if (!hub) dirty = pull_commit<A>(st, d, acc, has);
-    else if (A == A_PR_PULL) dirty = true;  // the hub kernel writes the value
     const uint32_t m = __ballot_sync(FULL, dirty);
     if (lane == 0) st.MD[d >> 5] = m;
     // S is a multiple of 256, so every warp of a block runs the same
@@ -1452,18 +1436,16 @@ __global__ void __launch_bounds__(256) k_pull(DevGraph g, DevState st) {
   }
 }
 
-// Bit pattern of a fold's result (the value pull_commit stores).
+// A fold's result (the value pull_commit stores).
 template <int A>
 __device__ __forceinline__ uint32_t pull_part(const PullAcc<A>& acc) {
-  if (A == A_PR_PULL) return __float_as_uint(__fsub_rn(acc.s, acc.c));
-  if (A == A_PR_DELTA) return __float_as_uint(acc.s);
   return acc.best;
 }
 
 // Medium in-lists (more than K_PULL_MED, at most K_PULL_HUB in-edges): one
 // warp per destination; lane l folds the elements l, l+32, ... (coalesced),
-// then the 32 partials combine by a butterfly (a fixed order, so sums are
-// reproducible).  Keeps the per-lane fold of k_pull balanced: its longest
+// then the 32 partials combine by a butterfly of mins.  Keeps the per-lane
+// fold of k_pull balanced: its longest
 // list is K_PULL_MED.  Runs after k_pull, whose dirty word for the slot is
 // already written: a dirty destination ORs its bit in.
 template <int A, bool kList = false>
@@ -1488,17 +1470,11 @@ __global__ void __launch_bounds__(256) k_pull_med(DevGraph g, DevState st, const
       acc.fold(pull_value<A>(st, __ldg(&g.in_src[q]), A == A_SSSP_W ? __ldg(&g.in_wgt[q]) : 0u));
     uint32_t part = pull_part<A>(acc);
 #pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      const uint32_t other = __shfl_xor_sync(FULL, part, o);
-      if (A == A_PR_PULL || A == A_PR_DELTA)
-        part = __float_as_uint(__fadd_rn(__uint_as_float(part), __uint_as_float(other)));
-      else
-        part = min(part, other);
-    }
+    for (int o = 16; o; o >>= 1) part = min(part, __shfl_xor_sync(FULL, part, o));
     if (lane == 0) {
       PullAcc<A> tot;
       tot.fold(part);
-      if (pull_commit<A>(st, hc.slot, tot, true) && A != A_PR_PULL) {
+      if (pull_commit<A>(st, hc.slot, tot, true)) {
         if (kList)
           mark_listed(st.MD, hc.slot, st.DL, st.lc + L_DL);
         else
@@ -1509,8 +1485,8 @@ __global__ void __launch_bounds__(256) k_pull_med(DevGraph g, DevState st, const
 }
 
 // Long in-lists: one block per destination; thread t folds the elements t,
-// t+256, ... (coalesced), then thread 0 folds the 256 partials in thread
-// order (a fixed order, so sums are reproducible).  Runs after k_pull, whose
+// t+256, ... (coalesced), then thread 0 takes the min of the 256 partials.
+// Runs after k_pull, whose
 // dirty word for the slot is already written: a dirty hub ORs its bit in.
 template <int A, bool kList = false>
 __global__ void __launch_bounds__(256) k_pull_hub(DevGraph g, DevState st, const HubChunkD* hubs, uint32_t n) {
@@ -1531,19 +1507,12 @@ __global__ void __launch_bounds__(256) k_pull_hub(DevGraph g, DevState st, const
     }
     for (; q < hc.e1; q += 256)
       acc.fold(pull_value<A>(st, __ldg(&g.in_src[q]), A == A_SSSP_W ? __ldg(&g.in_wgt[q]) : 0u));
-    uint32_t part;
-    if (A == A_PR_PULL)
-      part = __float_as_uint(__fsub_rn(acc.s, acc.c));
-    else if (A == A_PR_DELTA)
-      part = __float_as_uint(acc.s);
-    else
-      part = acc.best;
-    s_part[threadIdx.x] = part;
+    s_part[threadIdx.x] = pull_part<A>(acc);
     __syncthreads();
     if (threadIdx.x == 0) {
       PullAcc<A> tot;
       for (int i = 0; i < 256; ++i) tot.fold(s_part[i]);
-      if (pull_commit<A>(st, hc.slot, tot, true) && A != A_PR_PULL) {
+      if (pull_commit<A>(st, hc.slot, tot, true)) {
         if (kList)
           mark_listed(st.MD, hc.slot, st.DL, st.lc + L_DL);
         else
