@@ -616,7 +616,9 @@ def bench_batch(g, args, local) -> dict:
     dirg = [B.make_graph(s) for s in spec]
     t_gen = time.perf_counter() - t_gen
     E1 = sum(x.num_edges for x in sym) + 20 * sum(x.num_edges for x in dirg)
-    _, _, plain_s = B.run_plain_graphs(sym, dirg, 20, local)
+    lab_seq, rk_seq, plain_s = B.run_plain_graphs(sym, dirg, 20, local)
+    lab_con, rk_con, plain_con_s = B.run_plain_graphs(sym, dirg, 20, local, concurrent=True)
+    plain_same = all(bool(np.array_equal(a, b)) for a, b in zip(lab_seq + rk_seq, lab_con + rk_con))
     Uc, Up = B.Union(sym), B.Union(dirg)
     reps = 3
 
@@ -652,6 +654,8 @@ def bench_batch(g, args, local) -> dict:
     part1 = {"graphs": len(spec), "vertices": int(Uc.sizes.sum()), "edges_cc": Uc.graph.num_edges,
              "edges_pr": Up.graph.num_edges, "generate_s": t_gen,
              "plain_s": plain_s, "batched_s": batched_s, "speedup": plain_s / batched_s,
+             "plain_concurrent_s": plain_con_s, "speedup_vs_concurrent_plain": plain_con_s / batched_s,
+             "plain_concurrent_results_identical": plain_same,
              "union_fixed_s": union_fixed_s, "union_tuned_s": union_tuned_s,
              "speedup_batching": plain_s / union_fixed_s, "speedup_autotune": union_fixed_s / union_tuned_s,
              "speedup_learned_policy": union_tuned_s / batched_s,
@@ -702,7 +706,9 @@ def bench_batch(g, args, local) -> dict:
             "shares": "part 1 splits into batching (plain -> one union per algorithm, library defaults, fixed "
                       "rule), the autotuned schedule and the learned policy; part 2's gain is the shared CSR",
             "policy": "learned" if model is not None else "fixed",
-            "note": "plain: one ctx per graph (per source) with the fixed per-round rule; batched: part 1 one "
+            "note": "plain: one ctx per graph (per source) with the fixed per-round rule, run one after another; "
+                    "part 1 also times the same contexts with all runs queued at once (plain_concurrent_s); "
+                    "batched: part 1 one "
                     "union per algorithm, autotuned schedule and the learned round policy (CC; PageRank is "
                     "Jacobi pull), part 2 one multi-source call; timings exclude layout build"}
 

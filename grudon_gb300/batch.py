@@ -95,9 +95,12 @@ class Union:
 
 
 def run_plain_graphs(graphs_cc: Sequence[Graph], graphs_pr: Sequence[Graph], pr_iters: int = 20, device: int = 0,
-                     num_memory: int = 1):
-    """One ctx per graph, algorithms run graph after graph (the unbatched
-    path).  Returns (labels, ranks, seconds)."""
+                     num_memory: int = 1, concurrent: bool = False):
+    """One ctx per graph (the unbatched path).  concurrent=False runs the
+    algorithms graph after graph, each run waited for; concurrent=True
+    initialises every ctx, then queues all runs at once (GRD_RUN_ASYNC, one
+    stream per ctx, so small graphs' runs overlap on the GPU) and waits for
+    them.  Returns (labels, ranks, seconds)."""
     import time
     ctxs = [(Context(Gc, None, num_memory, device), Context(Gp, None, num_memory, device))
             for Gc, Gp in zip(graphs_cc, graphs_pr)]
@@ -106,13 +109,24 @@ def run_plain_graphs(graphs_cc: Sequence[Graph], graphs_pr: Sequence[Graph], pr_
         pr.set_algo(GRD_PR_PULL, max_rounds=pr_iters, tolerance=0.0)
     labels, ranks = [], []
     t0 = time.perf_counter()
-    for cc, pr in ctxs:
-        cc.init()
-        cc.run()
-        pr.init()
-        pr.run()
-    for cc, pr in ctxs:
-        cc.synchronize()
+    if concurrent:
+        for cc, pr in ctxs:
+            cc.init()
+            pr.init()
+        for cc, pr in ctxs:
+            cc.run(wait=False)
+            pr.run(wait=False)
+        for cc, pr in ctxs:
+            cc.wait()
+            pr.wait()
+    else:
+        for cc, pr in ctxs:
+            cc.init()
+            cc.run()
+            pr.init()
+            pr.run()
+        for cc, pr in ctxs:
+            cc.synchronize()
     secs = time.perf_counter() - t0
     for cc, pr in ctxs:
         labels.append(cc.read_props())
