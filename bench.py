@@ -73,6 +73,9 @@ def parse():
     ap.add_argument("--kernel-run-pr", action="store_true",
                     help="only run PageRank (RMAT-{scale}) for warmup + steps iterations from the host: the "
                          "target of per-kernel profilers")
+    ap.add_argument("--ingest-run", action="store_true",
+                    help="only build the three contexts' partition layouts on the GPU (RMAT-{scale}) and "
+                         "re-ingest each warmup + steps times: the target of per-kernel profilers")
     return ap.parse_args()
 
 
@@ -762,6 +765,32 @@ def kernel_run(g, args, local, rank, threads):
         W.close()
 
 
+def ingest_run(g, args, local, rank, threads):
+    """Device-layout contexts for the workload's three graphs (CC symmetrised,
+    SSSP weighted, PageRank with its in-edge view), each re-ingested
+    warmup + steps times."""
+    a, b, c = RMAT_ABC
+    seed = g.rmat_seed(args.scale, EF)
+    G_cc = g.Graph.rmat(args.scale, EF, a, b, c, seed=seed, symmetrize=True, threads=threads)
+    G_d = g.Graph.rmat(args.scale, EF, a, b, c, seed=seed, weighted=True, threads=threads)
+    G_pr = g.Graph.from_csr(G_d.row_offsets, G_d.col_indices)
+    graphs = ((G_cc, G_cc.partition_edge_balanced(NUM_MEMORY)), (G_d, G_d.partition_edge_balanced(NUM_MEMORY)),
+              (G_pr, G_d.partition_edge_balanced(NUM_MEMORY)))
+    ctxs = [g.Context(G, p, num_memory=NUM_MEMORY, device=local, device_layout=True) for G, p in graphs]
+    try:
+        ctxs[2].set_algo(g.GRD_PR_PULL)  # builds its in-edge view
+        h2d = 0
+        for _ in range(args.warmup + args.steps):
+            h2d = sum(ctx.ingest(G, p) for ctx, (G, p) in zip(ctxs, graphs))
+        for ctx in ctxs:
+            ctx.synchronize()
+    finally:
+        for ctx in ctxs:
+            ctx.close()
+    if rank == 0:
+        print(json.dumps({"ingest_run": True, "scale": args.scale, "h2d_bytes_per_ingest": h2d}), flush=True)
+
+
 def kernel_run_pr(g, args, local, rank, threads):
     a, b, c = RMAT_ABC
     G = g.Graph.rmat(args.scale, EF, a, b, c, seed=g.rmat_seed(args.scale, EF), threads=threads)
@@ -792,6 +821,9 @@ def main():
     threads = max(1, (os.cpu_count() or 1) // ws)
     if args.kernel_run_pr:
         kernel_run_pr(g, args, local, rank, threads)
+        return
+    if args.ingest_run:
+        ingest_run(g, args, local, rank, threads)
         return
     if args.kernel_run:
         kernel_run(g, args, local, rank, threads)
