@@ -247,6 +247,45 @@ def test_pagerank_pull_upload_leaves_out_edges_until_needed(gpu):
 
 
 @pytest.mark.gpu
+def test_upload_queued_behind_an_async_run(gpu):
+    """The end-to-end pipeline's pattern: each step queues a run and the
+    read of its result, then the next step's upload on the same ctx before
+    waiting.  The upload lands after the run on the ctx stream; every step's
+    result equals the oracle's (CC, weighted SSSP) or the first step's
+    (Jacobi PageRank, whose slim upload leaves the out-edges stale)."""
+    G = g.Graph.rmat(13, 8, symmetrize=True, weighted=True)
+    part = G.partition_edge_balanced(3)
+    V = G.num_vertices
+    refs = {a: O.run(o, G.row_offsets, G.col_indices, G.weights, mirror=part, num_memory=3)["props"]
+            for a, o in ((g.GRD_CC, O.ORC_CC), (g.GRD_SSSP_W, O.ORC_SSSP_W))}
+    with g.Context(G, part, num_memory=3) as cc, g.Context(G, part, num_memory=3) as ss, \
+            g.Context(G, part, num_memory=3) as pr:
+        cc.set_algo(g.GRD_CC)
+        ss.set_algo(g.GRD_SSSP_W)
+        pr.set_algo(g.GRD_PR_PULL, max_rounds=20, tolerance=0.0)
+        outs = [np.empty(V, np.uint32), np.empty(V, np.uint32), np.empty(V, np.float32)]
+        first_ranks = None
+        for _ in range(3):
+            for c in (cc, ss, pr):
+                c.wait()
+                c.init()
+                c.run(wait=False)
+            cc.read_props(out=outs[0], wait=False)
+            ss.read_props(out=outs[1], wait=False)
+            pr.read_ranks(out=outs[2], wait=False)
+            for c in (cc, ss, pr):
+                c.upload()  # the next step's layout, behind this step's run and read
+            for c in (cc, ss, pr):
+                c.wait()
+                c.synchronize()
+            np.testing.assert_array_equal(outs[0], refs[g.GRD_CC])
+            np.testing.assert_array_equal(outs[1], refs[g.GRD_SSSP_W])
+            if first_ranks is None:
+                first_ranks = outs[2].copy()
+            np.testing.assert_array_equal(outs[2], first_ranks)
+
+
+@pytest.mark.gpu
 def test_read_into_caller_arrays(gpu):
     """read_props / read_updates / read_ranks fill a caller's array (a
     serving loop keeps pinned result buffers) and refuse one of the wrong
