@@ -59,7 +59,8 @@ template <class T>
 int upload(grd_ctx* ctx, T* dst, const std::vector<T>& src) {
   if (src.empty()) return GRD_OK;
   const auto it = ctx->pinned_twin.find(src.data());
-  const void* from = it != ctx->pinned_twin.end() ? it->second : (const void*)src.data();
+  const bool twin = it != ctx->pinned_twin.end() && it->second.bytes == sizeof(T) * src.size();
+  const void* from = twin ? it->second.p : (const void*)src.data();
   CK(cudaMemcpyAsync(dst, from, sizeof(T) * src.size(), cudaMemcpyHostToDevice, ctx->stream));
   ctx->upload_bytes += sizeof(T) * src.size();
   return GRD_OK;
@@ -1002,7 +1003,7 @@ void grd_ctx_destroy(grd_ctx* ctx) {
   grd_ctx_release_extras(ctx);
   grd_graph_release(ctx);
   for (void* p : ctx->allocs) cudaFree(p);
-  for (auto& t : ctx->pinned_twin) cudaFreeHost(t.second);
+  for (auto& t : ctx->pinned_twin) cudaFreeHost(t.second.p);
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
@@ -1625,9 +1626,9 @@ int grd_ctx_init_device(grd_ctx* ctx) {
 // reads.  Such memory keeps its full host->device rate even when the copy
 // comes after the buffer sat idle, where memory pinned in place
 // (cudaHostRegister) ran a cold copy at a fraction of it.  The layout arrays
-// never change after creation, so the twin stays equal to them.  Without a
-// twin (a small array, or pinned memory refused) uploads read the pageable
-// array.
+// never change after creation, so the twin stays equal to them; an upload
+// still uses a twin only when its size matches the array's.  Without a twin
+// (a small array, or pinned memory refused) uploads read the pageable array.
 void grd_pin_twin(grd_ctx* ctx, const void* data, size_t bytes) {
   if (bytes < (1u << 20) || ctx->pinned_twin.count(data)) return;
   void* p = nullptr;
@@ -1637,7 +1638,7 @@ void grd_pin_twin(grd_ctx* ctx, const void* data, size_t bytes) {
     return;
   }
   std::memcpy(p, data, bytes);
-  ctx->pinned_twin.emplace(data, p);
+  ctx->pinned_twin.emplace(data, grd_ctx::PinnedTwin{p, bytes});
 }
 
 int grd_enqueue_init(grd_ctx* ctx, uint32_t blocks) {

@@ -102,7 +102,11 @@ struct grd_ctx {
   cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   // Pinned twins of the large host layout arrays (cudaHostAlloc, filled once
   // at creation), keyed by the array's data pointer: uploads read the twin.
-  std::unordered_map<const void*, void*> pinned_twin;
+  struct PinnedTwin {
+    void* p;
+    size_t bytes;
+  };
+  std::unordered_map<const void*, PinnedTwin> pinned_twin;
   std::vector<uint8_t> wgt8_host;  // weights as bytes when all are < 256 (uploaded instead of L.wgt)
   uint8_t* wgt8_dev = nullptr;     // their device staging copy
   unsigned char* h_small = nullptr;  // pinned small tables of the upload (hubs, tiles, partitions)
